@@ -1,0 +1,349 @@
+"""Benchmark: the 30-qubit random layered circuit (complex128, 40 layers of
+U3 on every qubit + CX on a random perfect matching, from |0...0>) through
+the engine's public API, one GPU per rank (replicas: the workload does not
+shard).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step applies the whole circuit once to a state resident in HBM (16 GiB,
+larger than L2, so no flush is needed between steps).  `value` is effective
+HBM GB/s under the per-gate byte accounting (each dense 1-qubit gate reads and
+writes the state once, 2S; each CX touches half of it, S): 3000 S per
+circuit.  `roofline` is the tile kernel's own traffic (2S per tile pass)
+over its average launch time.  `e2e` repeats the step through host SoA
+buffers (pinned), the upload and the download inside the timed region.
+`cpu_baseline` times the restated SIMD_PARALLEL strategy on this host's
+cores on a bounded sample of the same circuit.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "30q HBM GB/s vs peak; served circuits/s, p50/p99 ms at fidelity≥1-1e-6"
+N_QUBITS = 30
+LAYERS = 40
+SEED = 0
+
+
+def per_gate_bytes_in_S(qc) -> float:
+    """Algorithmic bytes of the per-gate path, in units of the state size S."""
+    from code_mojo_gb300 import butterfly as bfy
+    ctx = bfy.ExecContext()
+    ctx.execution_strategy = bfy.ExecutionStrategy.GPU
+    return bfy.plan_stats(qc, ctx)["bytes_in_S"]
+
+
+def measured_peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clock and throttle reasons during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(n_gpus: int):
+    """Returns (rank, world, local_rank); initialises torch.distributed for N>1."""
+    if n_gpus > 1 or "RANK" in os.environ:
+        import torch
+        import torch.distributed as dist
+        rank = int(os.environ.get("RANK", 0))
+        world = int(os.environ.get("WORLD_SIZE", 1))
+        local = int(os.environ.get("LOCAL_RANK", 0))
+        if world > 1:
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl")
+        return rank, world, local
+    return 0, 1, 0
+
+
+def barrier_max(value: float, world: int) -> float:
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int) -> None:
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+def cpu_sample(qc, n: int, gates: int, threads: int) -> dict:
+    """Times the restated SIMD_PARALLEL strategy on the first `gates` gates of
+    the circuit at full size n (a bounded sample); returns GB/s under the
+    per-gate accounting."""
+    from code_mojo_gb300 import butterfly as bfy
+    from oracle import pyoracle as O
+    sample = bfy.QuantumCircuit(n)
+    sample.transformations = qc.transformations[:gates]
+    bytes_S = per_gate_bytes_in_S(sample)
+    S = 16.0 * (1 << n)
+    re = np.zeros(1 << n)
+    im = np.zeros(1 << n)
+    re[0] = 1.0
+    t0 = time.perf_counter()
+    O.run_inplace(sample, re, im, strategy=O.OR_SIMD_PARALLEL, threads=threads, chunks=threads)
+    dt = time.perf_counter() - t0
+    return {"value": bytes_S * S / dt / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
+            "sample": f"first {gates} gates of the {n}-qubit {LAYERS}-layer circuit at full size "
+                      f"({bytes_S:.0f} S of per-gate traffic in {dt:.2f} s), restated SIMD_PARALLEL strategy",
+            "seconds": dt}
+
+
+def run_reference(args) -> None:
+    rank, world, local = dist_setup(args.gpus)
+    if rank != 0:
+        return
+    from code_mojo_gb300 import workloads as W
+    from oracle import pyoracle as O
+    qc = W.random_layered_circuit(N_QUBITS, LAYERS, SEED)
+    threads = O.num_cores()
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_sample(qc, N_QUBITS, args.ref_gates, threads)
+        if i >= args.warmup:
+            vals.append(r)
+    v = float(np.median([r["value"] for r in vals]))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "GB/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.median([r["seconds"] for r in vals])) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"random layered circuit, {N_QUBITS} qubits, {LAYERS} layers (U3 + CX matching), "
+                               f"complex128, from |0>; each step a bounded sample: first {args.ref_gates} gates",
+                   "qubits": N_QUBITS, "layers": LAYERS, "seed": SEED},
+        "cpu_baseline": {"value": v, "unit": "GB/s", "cores": threads, "kind": "port", "sample": vals[0]["sample"]},
+        "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def autotune_width(st, qc, candidates) -> tuple[int, dict]:
+    """Fusion width: times one layer-block of the circuit at each width and
+    keeps the fastest per unit of work."""
+    from code_mojo_gb300 import autotune
+    return autotune.pick_tile_qubits(st, qc, candidates)
+
+
+def run_ours(args) -> None:
+    rank, world, local = dist_setup(args.gpus)
+    import torch
+    torch.cuda.set_device(local)
+    from code_mojo_gb300 import butterfly as bfy
+    from code_mojo_gb300 import workloads as W
+
+    n = N_QUBITS
+    S = 16.0 * (1 << n)
+    qc = W.random_layered_circuit(n, LAYERS, SEED)
+    pg_bytes = per_gate_bytes_in_S(qc) * S
+    st = bfy.QuantumState(n)
+    stream = torch.cuda.ExternalStream(st.stream_ptr())
+
+    K, tune = autotune_width(st, qc, [int(k) for k in args.widths.split(",")])
+    ctx = bfy.ExecContext()
+    ctx.execution_strategy = bfy.ExecutionStrategy.GPU_FUSED
+    ctx.gpu_tile_qubits = K
+    ctx.gpu_sync = False
+    plan = bfy.plan_stats(qc, ctx)
+
+    st.set_basis(0)
+    for _ in range(args.warmup):
+        bfy.execute(st, qc, ctx)
+    st.sync()
+    barrier(world)
+    st.launch_count(reset=True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        st.sync()
+        e0.record(stream)
+        for _ in range(args.steps):
+            bfy.execute(st, qc, ctx)
+        e1.record(stream)
+        e1.synchronize()
+    launches = st.launch_count()
+    ms = e0.elapsed_time(e1)
+    ms = barrier_max(ms, world)
+    ms_step = ms / args.steps
+    norm = st.norm2()
+
+    # per-gate path: one circuit (the plain strategy the fused one is compared with)
+    per_gate = None
+    if args.per_gate_steps > 0:
+        pctx = ctx.copy()
+        pctx.execution_strategy = bfy.ExecutionStrategy.GPU
+        bfy.execute(st, qc, pctx)
+        st.sync()
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        for _ in range(args.per_gate_steps):
+            bfy.execute(st, qc, pctx)
+        p1.record(stream)
+        p1.synchronize()
+        pms = p0.elapsed_time(p1) / args.per_gate_steps
+        per_gate = {"ms_per_circuit": pms, "GB_per_s": pg_bytes / (pms * 1e-3) / 1e9,
+                    "launches_per_circuit": len(qc.transformations),
+                    "frac_of_hbm_peak": pg_bytes / (pms * 1e-3) / 1e9 / measured_peaks()[0]}
+
+    # e2e through the public API with host SoA buffers (pinned)
+    e2e = None
+    if args.e2e_steps > 0:
+        N = 1 << n
+        hre = torch.zeros(N, dtype=torch.float64, pin_memory=True)
+        him = torch.zeros(N, dtype=torch.float64, pin_memory=True)
+        hre[0] = 1.0
+        lib = __import__("code_mojo_gb300._ffi", fromlist=["lib"])
+        L = lib.lib()
+        ectx = ctx.copy()
+        ectx.gpu_sync = True
+
+        def e2e_step():
+            lib.check(L.bf_state_upload_soa(st.handle, hre.data_ptr(), him.data_ptr()))
+            bfy.execute(st, qc, ectx)
+            lib.check(L.bf_state_download_soa(st.handle, hre.data_ptr(), him.data_ptr()))
+
+        e2e_step()
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            e2e_step()
+        dt = (time.perf_counter() - t0) / args.e2e_steps
+        dt = barrier_max(dt, world)
+        e2e = {"value": pg_bytes * world / dt / 1e9, "unit": "GB/s", "h2d_bytes_per_step": 2 * 8 * N,
+               "d2h_bytes_per_step": 2 * 8 * N, "ms_per_step": dt * 1e3}
+        del hre, him
+
+    cpu = None
+    if rank == 0 and args.cpu_gates > 0:
+        from oracle import pyoracle as O
+        cpu = cpu_sample(qc, n, args.cpu_gates, O.num_cores())
+        cpu.pop("seconds", None)
+
+    if rank != 0:
+        st.close()
+        return
+    peak, peak_src = measured_peaks()
+    value = pg_bytes * world / (ms_step * 1e-3) / 1e9
+    tile_launch_ms = ms_step / max(1, plan["tile_passes"] + plan["gate_kernels"])
+    achieved = 2 * S / (tile_launch_ms * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "df64", "data": "synthetic",
+        "config": {"workload": f"random layered circuit, {n} qubits, {LAYERS} layers (U3 on every qubit + CX on a "
+                               f"random perfect matching), complex128 (FP64 storage, double-float arithmetic), "
+                               f"from |0>; fused tile passes, fusion width autotuned",
+                   "qubits": n, "layers": LAYERS, "seed": SEED, "state_bytes": int(S), "tile_qubits": K,
+                   "l2": "state (16 GiB) larger than L2; no flush", "parallelism": f"replicas x{world}"},
+        "gate_passes_per_s": len(qc.transformations) * world / (ms_step * 1e-3),
+        "circuits_per_s": world / (ms_step * 1e-3),
+        "per_gate_bytes_per_circuit": pg_bytes,
+        "fused_plan": plan,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "kernel": "bf::k_tile<bf::PolDF>",
+                     "bytes_per_launch": 2 * S, "avg_launch_ms": tile_launch_ms, "peak_source": f"{peak_src} hbm_gbs"},
+        "autotune": tune,
+        "per_gate_path": per_gate,
+        "gpu_launches": launches,
+        "norm_after": norm,
+        "clocks": clk.summary(),
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    st.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--widths", default="10,11,12,13")
+    ap.add_argument("--per-gate-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-gates", type=int, default=45)
+    ap.add_argument("--ref-gates", type=int, default=45)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,118 @@
+"""ctypes binding of the C ABI in include/bfgpu.h (libbfgpu.so).
+
+This is the binding a Python caller (or a test) uses; a Mojo caller binds the
+same symbols through its FFI.  The library is loaded from the package's
+_lib/ directory; a missing library is an error, never a silent fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_lib" / "libbfgpu.so"
+
+# status codes
+BF_OK, BF_EINVAL, BF_ENOMEM, BF_ECUDA, BF_EUNSUPPORTED, BF_ETIMEDOUT, BF_EBUSY = 0, -1, -2, -3, -4, -5, -6
+# dtypes
+BF_C128, BF_C64 = 0, 1
+# gate kinds (GateKind)
+BF_GATE_H, BF_GATE_P, BF_GATE_X, BF_GATE_Y, BF_GATE_Z, BF_GATE_RX, BF_GATE_RY, BF_GATE_RZ, BF_GATE_CUSTOM = range(9)
+# op kinds
+(BF_OP_GATE, BF_OP_SWAP, BF_OP_QREV, BF_OP_UNITARY, BF_OP_CUNITARY, BF_OP_BITREV, BF_OP_PERMUTE,
+ BF_OP_CSWAP) = range(8)
+BF_OPF_FUSE_WITH_NEXT = 1
+BF_STRATEGY_GPU, BF_STRATEGY_GPU_FUSED = 8, 9
+BF_SPEC_ALL = 127
+
+
+class bf_op(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("gate", C.c_int32),
+        ("target", C.c_int32),
+        ("target2", C.c_int32),
+        ("controls", C.c_uint64),
+        ("ncontrols", C.c_int32),
+        ("flags", C.c_uint32),
+        ("arg", C.c_double),
+        ("mat", C.c_double * 8),
+        ("data", C.POINTER(C.c_double)),
+        ("qubits", C.POINTER(C.c_int32)),
+        ("nqubits", C.c_int64),
+    ]
+
+
+assert C.sizeof(bf_op) == 128, C.sizeof(bf_op)
+
+
+class bf_exec_opts(C.Structure):
+    _fields_ = [
+        ("strategy", C.c_int32),
+        ("validate", C.c_int32),
+        ("specialized", C.c_uint32),
+        ("tile_qubits", C.c_int32),
+        ("sync", C.c_int32),
+        ("reserved", C.c_int32 * 3),
+    ]
+
+
+class BFError(RuntimeError):
+    """An error status returned by the engine, with its message."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(msg)
+        self.code = code
+
+
+_lib = None
+
+# (name, argtypes) of every exported entry point; the CPU test checks that
+# the shared library exports exactly these.
+SIGNATURES = {
+    "bf_exec_opts_init": [C.POINTER(bf_exec_opts)],
+    "bf_version": [C.POINTER(C.c_int32)],
+    "bf_last_error": [C.c_char_p, C.c_size_t],
+    "bf_state_create": [C.c_int32, C.c_int32, C.POINTER(C.c_void_p)],
+    "bf_state_destroy": [C.c_void_p],
+    "bf_state_info": [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)],
+    "bf_state_set_basis": [C.c_void_p, C.c_uint64],
+    "bf_state_upload_soa": [C.c_void_p, C.c_void_p, C.c_void_p],
+    "bf_state_download_soa": [C.c_void_p, C.c_void_p, C.c_void_p],
+    "bf_state_download_range": [C.c_void_p, C.c_uint64, C.c_uint64, C.c_void_p, C.c_void_p],
+    "bf_state_sync": [C.c_void_p],
+    "bf_state_stream": [C.c_void_p, C.POINTER(C.c_void_p)],
+    "bf_execute": [C.c_void_p, C.POINTER(bf_op), C.c_int64, C.POINTER(bf_exec_opts)],
+    "bf_state_launch_count": [C.c_void_p, C.POINTER(C.c_uint64), C.c_int32],
+    "bf_norm2": [C.c_void_p, C.POINTER(C.c_double)],
+    "bf_validate": [C.c_int32, C.POINTER(bf_op), C.c_int64],
+    "bf_plan_stats": [C.c_int32, C.POINTER(bf_op), C.c_int64, C.POINTER(bf_exec_opts), C.POINTER(C.c_int64),
+                      C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_double)],
+}
+
+
+def lib() -> C.CDLL:
+    """Loads libbfgpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+        L = C.CDLL(str(LIB_PATH))
+        for name, argtypes in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = argtypes
+            fn.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def last_error() -> str:
+    buf = C.create_string_buffer(1024)
+    lib().bf_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(rc: int) -> None:
+    if rc != BF_OK:
+        raise BFError(rc, last_error())

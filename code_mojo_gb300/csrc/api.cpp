@@ -1,0 +1,603 @@
+// api.cpp — the C ABI (include/bfgpu.h): state lifecycle, boundary copies,
+// and bf_execute, the GPU counterpart of execute_with_handlers
+// (butterfly/core/executors.mojo:268-319).
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "bf_internal.h"
+
+namespace bf {
+
+static thread_local std::string g_last_error;
+
+template <class F>
+static int guarded(F&& f) {
+  try {
+    f();
+    return BF_OK;
+  } catch (const Error& e) {
+    g_last_error = e.msg;
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    g_last_error = "host allocation failed";
+    return BF_ENOMEM;
+  } catch (...) {
+    g_last_error = "unexpected internal error";
+    return BF_ECUDA;
+  }
+}
+
+static int default_tile_qubits(const State& st) {
+  // 2^11 amplitudes (32 KiB at complex128) per CTA: six resident CTAs per SM.
+  (void)st;
+  return 11;
+}
+
+static int env_int(const char* name, int dflt) {
+  const char* v = std::getenv(name);
+  return (v && *v) ? std::atoi(v) : dflt;
+}
+
+// ---- program buffer for tile ops ---------------------------------------------
+static void upload_program(State& st, const std::vector<TileOp>& prog) {
+  if (prog.empty()) return;
+  if (st.prog_event_live) BF_CUDA(cudaEventSynchronize(st.prog_event));
+  if (prog.size() > st.prog_cap) {
+    size_t cap = std::max(prog.size(), st.prog_cap * 2);
+    if (st.d_prog) {
+      BF_CUDA(cudaStreamSynchronize(st.stream));
+      cudaFree(st.d_prog);
+      st.d_prog = nullptr;
+    }
+    if (st.h_prog) {
+      cudaFreeHost(st.h_prog);
+      st.h_prog = nullptr;
+    }
+    st.prog_cap = 0;
+    if (cudaMalloc(&st.d_prog, cap * sizeof(TileOp)) != cudaSuccess ||
+        cudaHostAlloc(&st.h_prog, cap * sizeof(TileOp), cudaHostAllocDefault) != cudaSuccess) {
+      cudaGetLastError();
+      fail(BF_ENOMEM, "cannot allocate the tile program buffer (%zu ops)", cap);
+    }
+    st.prog_cap = cap;
+  }
+  std::memcpy(st.h_prog, prog.data(), prog.size() * sizeof(TileOp));
+  BF_CUDA(cudaMemcpyAsync(st.d_prog, st.h_prog, prog.size() * sizeof(TileOp), cudaMemcpyHostToDevice, st.stream));
+  BF_CUDA(cudaEventRecord(st.prog_event, st.stream));
+  st.prog_event_live = true;
+}
+
+// ---- execution -------------------------------------------------------------
+// A step is one launch (or a launch group) in op order.
+struct Step {
+  enum Kind { GATE, TILE, BITREV, PERMUTE, SWAPBITS, UNITARY } kind;
+  GateInstr gate;
+  TilePass tile;            // ops moved into the program; tile.ops emptied
+  size_t prog_off = 0;
+  int nprog = 0;
+  std::vector<int32_t> src_of;
+  int a = 0, b = 0;
+  std::vector<double> u;
+  int ut = 0, um = 0, uc = -1;
+};
+
+static bool is_h(const bf_op& o) { return o.ncontrols == 0 && o.gate == BF_GATE_H; }
+static bool is_p(const bf_op& o) { return o.ncontrols == 0 && o.gate == BF_GATE_P; }
+static bool is_cp(const bf_op& o) { return o.ncontrols == 1 && o.gate == BF_GATE_P; }
+
+// 4x4 composition of a FusedPairTransformation that matches none of the sparse
+// kernels (transformations_fusion.mojo:277-310): m = M1 * M0 on (q_low, q_low+1).
+static void fused_pair_matrix(const bf_op& t0, const bf_op& t1, int& q_low, std::vector<double>& out) {
+  auto gm = [](const bf_op& o, double* m) {
+    GateInstr g = lower_gate(o, 0);
+    std::memcpy(m, g.m, 8 * sizeof(double));
+  };
+  auto ctz = [](uint64_t v) { return v ? __builtin_ctzll(v) : 0; };
+  int c0 = t0.ncontrols == 1 ? ctz(t0.controls) : 0;
+  int c1 = t1.ncontrols == 1 ? ctz(t1.controls) : 0;
+  q_low = t0.target;
+  if (t0.ncontrols == 1) q_low = std::min(q_low, c0);
+  q_low = std::min(q_low, t1.target);
+  if (t1.ncontrols == 1) q_low = std::min(q_low, c1);
+  auto to4 = [&](const bf_op& o, int ctl, double* M) {  // 16 complex, row-major
+    double g[8];
+    gm(o, g);
+    for (int i = 0; i < 32; ++i) M[i] = 0;
+    auto G = [&](int r, int c, int part) { return g[2 * (2 * r + c) + part]; };
+    if (o.ncontrols == 1) {
+      for (int b0 = 0; b0 < 2; ++b0)
+        for (int b1 = 0; b1 < 2; ++b1) {
+          int in = b0 + 2 * b1;
+          int cb = ctl == q_low ? b0 : b1;
+          int tb = o.target == q_low ? b0 : b1;
+          if (cb == 0) {
+            M[2 * (in * 4 + in)] = 1;
+          } else {
+            for (int ot = 0; ot < 2; ++ot) {
+              int ob0 = b0, ob1 = b1;
+              if (o.target == q_low) ob0 = ot; else ob1 = ot;
+              int oi = ob0 + 2 * ob1;
+              M[2 * (oi * 4 + in)] = G(ot, tb, 0);
+              M[2 * (oi * 4 + in) + 1] = G(ot, tb, 1);
+            }
+          }
+        }
+    } else if (o.target == q_low) {
+      for (int b1 = 0; b1 < 2; ++b1)
+        for (int r0 = 0; r0 < 2; ++r0)
+          for (int c0_ = 0; c0_ < 2; ++c0_) {
+            int idx = (r0 + 2 * b1) * 4 + c0_ + 2 * b1;
+            M[2 * idx] = G(r0, c0_, 0);
+            M[2 * idx + 1] = G(r0, c0_, 1);
+          }
+    } else {
+      for (int b0 = 0; b0 < 2; ++b0)
+        for (int r1 = 0; r1 < 2; ++r1)
+          for (int c1_ = 0; c1_ < 2; ++c1_) {
+            int idx = (b0 + 2 * r1) * 4 + b0 + 2 * c1_;
+            M[2 * idx] = G(r1, c1_, 0);
+            M[2 * idx + 1] = G(r1, c1_, 1);
+          }
+    }
+  };
+  double m0[32], m1[32];
+  to4(t0, c0, m0);
+  to4(t1, c1, m1);
+  out.assign(32, 0.0);
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 4; ++c) {
+      double sr = 0, si = 0;
+      for (int k = 0; k < 4; ++k) {
+        double ar = m1[2 * (r * 4 + k)], ai = m1[2 * (r * 4 + k) + 1];
+        double br = m0[2 * (k * 4 + c)], bi = m0[2 * (k * 4 + c) + 1];
+        sr = sr + (ar * br - ai * bi);
+        si = si + (ar * bi + ai * br);
+      }
+      out[2 * (r * 4 + c)] = sr;
+      out[2 * (r * 4 + c) + 1] = si;
+    }
+}
+
+static void build_steps(int n, const bf_op* ops, int64_t nops, const bf_exec_opts& o, std::vector<Step>& steps,
+                        std::vector<TileOp>& prog) {
+  const bool fused = o.strategy == BF_STRATEGY_GPU_FUSED;
+  const int K = o.tile_qubits > 0 ? o.tile_qubits : 11;
+  std::vector<GateInstr> run;
+  auto flush = [&]() {
+    if (run.empty()) return;
+    for (auto& ps : plan_gates(n, run, K)) {
+      Step s;
+      if (ps.is_tile) {
+        s.kind = Step::TILE;
+        s.tile = ps.tile;
+        s.prog_off = prog.size();
+        s.nprog = (int)ps.tile.ops.size();
+        prog.insert(prog.end(), ps.tile.ops.begin(), ps.tile.ops.end());
+        s.tile.ops.clear();
+      } else {
+        s.kind = Step::GATE;
+        s.gate = ps.gate;
+      }
+      steps.push_back(std::move(s));
+    }
+    run.clear();
+  };
+  auto emit_gate = [&](const GateInstr& g) {
+    if (fused) {
+      run.push_back(g);
+    } else {
+      Step s;
+      s.kind = Step::GATE;
+      s.gate = g;
+      steps.push_back(std::move(s));
+    }
+  };
+  auto emit_perm = [&](const std::vector<int32_t>& src_of) {
+    flush();
+    bool full = true;
+    for (int p = 0; p < n; ++p) full &= (src_of[p] == n - 1 - p);
+    Step s;
+    s.kind = full ? Step::BITREV : Step::PERMUTE;
+    s.src_of = src_of;
+    steps.push_back(std::move(s));
+  };
+  auto emit_unitary = [&](const double* data, int t, int m, int ctl) {
+    if (m <= 0) return;
+    if (m == 1) {  // a 2x2: the gate kernels (and tile passes) take it
+      bf_op g;
+      std::memset(&g, 0, sizeof g);
+      g.kind = BF_OP_GATE;
+      g.gate = BF_GATE_CUSTOM;
+      g.target = t;
+      if (ctl >= 0) {
+        g.controls = 1ull << ctl;
+        g.ncontrols = 1;
+      }
+      std::memcpy(g.mat, data, 8 * sizeof(double));
+      emit_gate(lower_gate(g, o.specialized));
+      return;
+    }
+    flush();
+    Step s;
+    s.kind = Step::UNITARY;
+    s.u.assign(data, data + 2 * ((size_t)1 << (2 * m)));
+    s.ut = t;
+    s.um = m;
+    s.uc = ctl;
+    steps.push_back(std::move(s));
+  };
+
+  for (int64_t i = 0; i < nops; ++i) {
+    const bf_op& op = ops[i];
+    switch (op.kind) {
+      case BF_OP_GATE: {
+        if ((op.flags & BF_OPF_FUSE_WITH_NEXT) && i + 1 < nops) {
+          // FusedPairTransformation (apply_fused_pair, transformations_fusion.mojo:221-310)
+          const bf_op& t1 = ops[i + 1];
+          bool special = (is_cp(op) && is_cp(t1) && op.controls == t1.controls && op.target != t1.target) ||
+                         (is_h(op) && is_h(t1) && op.target != t1.target) ||
+                         (is_p(op) && is_p(t1) && op.target != t1.target) ||
+                         (is_h(op) && is_p(t1) && op.target != t1.target) ||
+                         (is_p(op) && is_h(t1) && op.target != t1.target);
+          if (special) {
+            // one pass for both gates: a two-gate run through the tile planner
+            std::vector<GateInstr> pair = {lower_gate(op, o.specialized), lower_gate(t1, o.specialized)};
+            if (fused) {
+              run.insert(run.end(), pair.begin(), pair.end());
+            } else {
+              std::vector<GateInstr> saved;
+              saved.swap(run);
+              run = pair;
+              flush();
+              run.swap(saved);
+            }
+          } else {
+            int q_low = 0;
+            std::vector<double> m;
+            fused_pair_matrix(op, t1, q_low, m);
+            if (q_low + 2 > n) fail(BF_EINVAL, "Target range out of bounds");
+            emit_unitary(m.data(), q_low, 2, -1);
+          }
+          ++i;
+        } else {
+          emit_gate(lower_gate(op, o.specialized));
+        }
+        break;
+      }
+      case BF_OP_SWAP:   // apply_swap_with_cx (executors.mojo:231-241): three CX = one exchange
+      case BF_OP_CSWAP:  // apply_swap (state.mojo:434-444)
+        if (op.target != op.target2) {
+          flush();
+          Step s;
+          s.kind = Step::SWAPBITS;
+          s.a = op.target;
+          s.b = op.target2;
+          steps.push_back(std::move(s));
+        }
+        break;
+      case BF_OP_QREV: {  // apply_qubit_reversal_with_cx (executors.mojo:244-265)
+        std::vector<int> t;
+        if (op.nqubits == 0) for (int q = 0; q < n; ++q) t.push_back(q);
+        else t.assign(op.qubits, op.qubits + op.nqubits);
+        std::sort(t.begin(), t.end());
+        std::vector<int32_t> src_of(n);
+        for (int p = 0; p < n; ++p) src_of[p] = p;
+        for (size_t k = 0; k < t.size() / 2; ++k) std::swap(src_of[t[k]], src_of[t[t.size() - 1 - k]]);
+        emit_perm(src_of);
+        break;
+      }
+      case BF_OP_BITREV: {  // apply_bit_reverse (state.mojo:383-390)
+        std::vector<int32_t> src_of(n);
+        for (int p = 0; p < n; ++p) src_of[p] = p;
+        if (op.nqubits == 0) {
+          for (int p = 0; p < n; ++p) src_of[p] = n - 1 - p;
+        } else if (op.nqubits > 1) {
+          std::vector<int> t(op.qubits, op.qubits + op.nqubits);
+          std::sort(t.begin(), t.end());
+          int k = (int)t.size();
+          for (int b = 0; b < k; ++b) src_of[t[b]] = t[k - 1 - b];
+        }
+        emit_perm(src_of);
+        break;
+      }
+      case BF_OP_PERMUTE: {  // apply_permute_qubits (state.mojo:393-431)
+        if (op.nqubits == 0) break;
+        std::vector<int32_t> src_of(op.qubits, op.qubits + op.nqubits);
+        emit_perm(src_of);
+        break;
+      }
+      case BF_OP_UNITARY:
+        emit_unitary(op.data, op.target, op.target2, -1);
+        break;
+      case BF_OP_CUNITARY:
+        emit_unitary(op.data, op.target, op.target2, __builtin_ctzll(op.controls));
+        break;
+      default:
+        fail(BF_EINVAL, "Unknown transformation type: %d", op.kind);
+    }
+  }
+  flush();
+}
+
+static void run_steps(State& st, std::vector<Step>& steps, const std::vector<TileOp>& prog) {
+  upload_program(st, prog);
+  for (auto& s : steps) {
+    switch (s.kind) {
+      case Step::GATE: launch_gate(st, s.gate); break;
+      case Step::TILE: launch_tile_pass(st, st.d_prog + s.prog_off, s.nprog, s.tile); break;
+      case Step::BITREV: launch_bitrev_full(st); break;
+      case Step::PERMUTE: launch_permute(st, s.src_of.data()); break;
+      case Step::SWAPBITS: launch_swap_bits(st, s.a, s.b); break;
+      case Step::UNITARY: launch_unitary(st, s.u.data(), s.ut, s.um, s.uc); break;
+    }
+  }
+}
+
+static void free_state(State* st) {
+  if (!st) return;
+  if (st->stream) cudaStreamSynchronize(st->stream);
+  if (st->amp) cudaFree(st->amp);
+  if (st->scratch) cudaFree(st->scratch);
+  if (st->d_prog) cudaFree(st->d_prog);
+  if (st->h_prog) cudaFreeHost(st->h_prog);
+  if (st->d_stage) cudaFree(st->d_stage);
+  if (st->d_partial) cudaFree(st->d_partial);
+  if (st->h_partial) cudaFreeHost(st->h_partial);
+  if (st->d_umat) cudaFree(st->d_umat);
+  if (st->prog_event) cudaEventDestroy(st->prog_event);
+  if (st->stream) cudaStreamDestroy(st->stream);
+  delete st;
+}
+
+static constexpr uint64_t kStageElems = 1ull << 23;  // 8 Mi amplitudes per chunk
+
+static void ensure_stage(State& st) {
+  size_t want = (size_t)std::min<uint64_t>(st.N, kStageElems) * 2 * sizeof(double);
+  if (st.stage_bytes >= want) return;
+  if (st.d_stage) cudaFree(st.d_stage);
+  st.d_stage = nullptr;
+  st.stage_bytes = 0;
+  if (cudaMalloc(&st.d_stage, want) != cudaSuccess) {
+    cudaGetLastError();
+    fail(BF_ENOMEM, "cannot allocate %zu bytes of boundary staging", want);
+  }
+  st.stage_bytes = want;
+}
+
+}  // namespace bf
+
+using namespace bf;
+
+static inline State* S_(bf_state* h) { return reinterpret_cast<State*>(h); }
+static inline const State* S_(const bf_state* h) { return reinterpret_cast<const State*>(h); }
+
+extern "C" {
+
+int bf_exec_opts_init(bf_exec_opts* o) {
+  if (!o) return BF_EINVAL;
+  std::memset(o, 0, sizeof *o);
+  o->strategy = BF_STRATEGY_GPU_FUSED;
+  o->validate = 1;
+  o->specialized = BF_SPEC_ALL;
+  o->tile_qubits = 0;
+  o->sync = 0;
+  return BF_OK;
+}
+
+int bf_version(int32_t* v) {
+  if (!v) return BF_EINVAL;
+  *v = BFGPU_ABI_VERSION;
+  return BF_OK;
+}
+
+int bf_last_error(char* buf, size_t len) {
+  if (!buf || len == 0) return BF_EINVAL;
+  size_t k = std::min(len - 1, g_last_error.size());
+  std::memcpy(buf, g_last_error.data(), k);
+  buf[k] = 0;
+  return BF_OK;
+}
+
+int bf_state_create(int32_t n, int32_t dtype, bf_state** out) {
+  return guarded([&]() {
+    if (!out) fail(BF_EINVAL, "out is null");
+    *out = nullptr;
+    if (n < 1 || n > 40) fail(BF_EINVAL, "num_qubits must be in [1, 40], got %d", n);
+    if (dtype != BF_C128 && dtype != BF_C64) fail(BF_EINVAL, "unknown dtype %d", dtype);
+    State* st = new State();
+    try {
+      st->n = n;
+      st->dtype = dtype;
+      st->N = 1ull << n;
+      // complex128 computes in double-float unless BFGPU_C128_MATH=f64
+      const char* math = std::getenv("BFGPU_C128_MATH");
+      if (dtype == BF_C64) st->prec = PREC_F32;
+      else st->prec = (math && std::strcmp(math, "f64") == 0) ? PREC_F64 : PREC_DF;
+      BF_CUDA(cudaGetDevice(&st->device));
+      BF_CUDA(cudaDeviceGetAttribute(&st->num_sms, cudaDevAttrMultiProcessorCount, st->device));
+      BF_CUDA(cudaStreamCreateWithFlags(&st->stream, cudaStreamNonBlocking));
+      BF_CUDA(cudaEventCreateWithFlags(&st->prog_event, cudaEventDisableTiming));
+      if (cudaMalloc(&st->amp, st->bytes()) != cudaSuccess) {
+        cudaGetLastError();
+        st->amp = nullptr;
+        fail(BF_ENOMEM, "cannot allocate %zu bytes for a %d-qubit state", st->bytes(), n);
+      }
+      launch_set_basis(*st, 0);
+    } catch (...) {
+      free_state(st);
+      throw;
+    }
+    *out = reinterpret_cast<bf_state*>(st);
+  });
+}
+
+int bf_state_destroy(bf_state* hst) {
+  State* st = S_(hst);
+  return guarded([&]() { free_state(st); });
+}
+
+int bf_state_info(const bf_state* hst, int32_t* n, int32_t* dtype) {
+  const State* st = S_(hst);
+  return guarded([&]() {
+    if (!st) fail(BF_EINVAL, "state is null");
+    if (n) *n = st->n;
+    if (dtype) *dtype = st->dtype;
+  });
+}
+
+int bf_state_set_basis(bf_state* hst, uint64_t idx) {
+  State* st = S_(hst);
+  return guarded([&]() {
+    if (!st) fail(BF_EINVAL, "state is null");
+    if (idx >= st->N) fail(BF_EINVAL, "basis index %llu out of range", (unsigned long long)idx);
+    launch_set_basis(*st, idx);
+  });
+}
+
+int bf_state_upload_soa(bf_state* hst, const double* re, const double* im) {
+  State* st = S_(hst);
+  return guarded([&]() {
+    if (!st || !re || !im) fail(BF_EINVAL, "null argument");
+    ensure_stage(*st);
+    double* d_re = static_cast<double*>(st->d_stage);
+    uint64_t chunk = std::min<uint64_t>(st->N, kStageElems);
+    double* d_im = d_re + chunk;
+    for (uint64_t off = 0; off < st->N; off += chunk) {
+      uint64_t cnt = std::min(chunk, st->N - off);
+      BF_CUDA(cudaMemcpyAsync(d_re, re + off, cnt * sizeof(double), cudaMemcpyHostToDevice, st->stream));
+      BF_CUDA(cudaMemcpyAsync(d_im, im + off, cnt * sizeof(double), cudaMemcpyHostToDevice, st->stream));
+      launch_interleave(*st, d_re, d_im, off, cnt);
+    }
+  });
+}
+
+int bf_state_download_range(bf_state* hst, uint64_t offset, uint64_t count, double* re, double* im) {
+  State* st = S_(hst);
+  return guarded([&]() {
+    if (!st || (count && (!re || !im))) fail(BF_EINVAL, "null argument");
+    if (offset > st->N || count > st->N - offset) fail(BF_EINVAL, "range out of bounds");
+    ensure_stage(*st);
+    double* d_re = static_cast<double*>(st->d_stage);
+    uint64_t chunk = std::min<uint64_t>(st->N, kStageElems);
+    double* d_im = d_re + chunk;
+    for (uint64_t done = 0; done < count; done += chunk) {
+      uint64_t cnt = std::min(chunk, count - done);
+      launch_deinterleave(*st, d_re, d_im, offset + done, cnt);
+      BF_CUDA(cudaMemcpyAsync(re + done, d_re, cnt * sizeof(double), cudaMemcpyDeviceToHost, st->stream));
+      BF_CUDA(cudaMemcpyAsync(im + done, d_im, cnt * sizeof(double), cudaMemcpyDeviceToHost, st->stream));
+    }
+    BF_CUDA(cudaStreamSynchronize(st->stream));
+  });
+}
+
+int bf_state_download_soa(bf_state* hst, double* re, double* im) {
+  State* st = S_(hst);
+  if (!st) {
+    g_last_error = "state is null";
+    return BF_EINVAL;
+  }
+  return bf_state_download_range(hst, 0, st->N, re, im);
+}
+
+int bf_state_sync(bf_state* hst) {
+  State* st = S_(hst);
+  return guarded([&]() {
+    if (!st) fail(BF_EINVAL, "state is null");
+    BF_CUDA(cudaStreamSynchronize(st->stream));
+  });
+}
+
+int bf_state_stream(bf_state* hst, void** stream) {
+  State* st = S_(hst);
+  return guarded([&]() {
+    if (!st || !stream) fail(BF_EINVAL, "null argument");
+    *stream = (void*)st->stream;
+  });
+}
+
+int bf_state_launch_count(const bf_state* hst, uint64_t* launches, int32_t reset) {
+  const State* st = S_(hst);
+  return guarded([&]() {
+    if (!st || !launches) fail(BF_EINVAL, "null argument");
+    *launches = st->launches;
+    if (reset) const_cast<State*>(st)->launches = 0;
+  });
+}
+
+int bf_execute(bf_state* hst, const bf_op* ops, int64_t nops, const bf_exec_opts* opts) {
+  State* st = S_(hst);
+  return guarded([&]() {
+    if (!st) fail(BF_EINVAL, "state is null");
+    bf_exec_opts o;
+    if (opts) o = *opts;
+    else bf_exec_opts_init(&o);
+    if (o.strategy >= 0 && o.strategy <= 7)
+      fail(BF_EUNSUPPORTED, "Execution strategy %d is a CPU strategy; use BF_STRATEGY_GPU(_FUSED)", o.strategy);
+    if (o.strategy != BF_STRATEGY_GPU && o.strategy != BF_STRATEGY_GPU_FUSED)
+      fail(BF_EINVAL, "Unknown execution strategy: %d", o.strategy);
+    if (o.tile_qubits < 0 || o.tile_qubits > kMaxTileQubits)
+      fail(BF_EINVAL, "tile_qubits must be in [0, %d]", kMaxTileQubits);
+    if (o.tile_qubits == 0) o.tile_qubits = env_int("BFGPU_TILE_QUBITS", default_tile_qubits(*st));
+    if (o.validate) validate_ops(st->n, ops, nops);
+    std::vector<Step> steps;
+    std::vector<TileOp> prog;
+    build_steps(st->n, ops, nops, o, steps, prog);
+    run_steps(*st, steps, prog);
+    if (o.sync) BF_CUDA(cudaStreamSynchronize(st->stream));
+  });
+}
+
+int bf_norm2(bf_state* hst, double* out) {
+  State* st = S_(hst);
+  return guarded([&]() {
+    if (!st || !out) fail(BF_EINVAL, "null argument");
+    *out = reduce_norm2(*st);
+  });
+}
+
+// Host-only: validates and plans ops for a state of n qubits without a
+// device, reporting how many tile passes, per-gate kernels and other passes
+// bf_execute would launch and the algorithmic bytes they move (units of S).
+int bf_plan_stats(int32_t n, const bf_op* ops, int64_t nops, const bf_exec_opts* opts, int64_t* tile_passes,
+                  int64_t* gate_kernels, int64_t* other_passes, double* bytes_in_S) {
+  return guarded([&]() {
+    if (n < 1 || n > 40) fail(BF_EINVAL, "num_qubits must be in [1, 40], got %d", n);
+    bf_exec_opts o;
+    if (opts) o = *opts;
+    else bf_exec_opts_init(&o);
+    if (o.tile_qubits <= 0) o.tile_qubits = 11;
+    if (o.validate) validate_ops(n, ops, nops);
+    std::vector<Step> steps;
+    std::vector<TileOp> prog;
+    build_steps(n, ops, nops, o, steps, prog);
+    int64_t t = 0, g = 0, x = 0;
+    double bytes = 0;
+    for (auto& s : steps) {
+      if (s.kind == Step::TILE) {
+        ++t;
+        bytes += 2.0;
+      } else if (s.kind == Step::GATE) {
+        ++g;
+        bytes += gate_bytes_fraction(s.gate);
+      } else {
+        ++x;
+        bytes += (s.kind == Step::SWAPBITS) ? 1.0 : 2.0;
+      }
+    }
+    if (tile_passes) *tile_passes = t;
+    if (gate_kernels) *gate_kernels = g;
+    if (other_passes) *other_passes = x;
+    if (bytes_in_S) *bytes_in_S = bytes;
+  });
+}
+
+// Host-only validation (validate_circuit, executors.mojo:129-185).
+int bf_validate(int32_t n, const bf_op* ops, int64_t nops) {
+  return guarded([&]() { validate_ops(n, ops, nops); });
+}
+
+}  // extern "C"

@@ -1,0 +1,143 @@
+// bf_internal.h — shared declarations of the bfgpu engine (host + device).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/bfgpu.h"
+
+namespace bf {
+
+// ---------------------------------------------------------------------------
+// Errors: host code throws bf::Error; the C ABI converts it to a status code
+// and a thread-local message.
+struct Error {
+  int code;
+  std::string msg;
+};
+[[noreturn]] void fail(int code, const char* fmt, ...);
+void check_cuda(cudaError_t e, const char* what);
+#define BF_CUDA(call) ::bf::check_cuda((call), #call)
+
+// ---------------------------------------------------------------------------
+// Compute precision of a state.
+//   F64 : complex128 storage, FP64 arithmetic (DFMA).
+//   DF  : complex128 storage, double-float arithmetic (FP32 hi+lo pairs, the
+//         error-free transformations of Dekker 1971 / Knuth TAOCP vol. 2) with
+//         the FP64 <-> pair conversions done in integer arithmetic.
+//   F32 : complex64 storage, FP32 arithmetic.
+enum Prec { PREC_F64 = 0, PREC_DF = 1, PREC_F32 = 2 };
+
+// ---------------------------------------------------------------------------
+// A lowered single-target gate (after kind/arg -> matrix on the host).
+enum GKind : int32_t {
+  GK_DENSE = 0,  // full 2x2 complex matrix m
+  GK_H = 1,      // Hadamard: (u+v)*s, (u-v)*s with s = 0.7071067811865476
+  GK_SWAP = 2,   // X: exchange the pair
+  GK_PHASE = 3,  // diag(1, e^{i theta}): m[6], m[7] = cos, sin (P, Z, CP, CZ, MCP)
+  GK_DIAG = 4,   // diag(d0, d1): m[0..1] = d0, m[6..7] = d1 (RZ)
+  GK_RY = 5      // real rotation [[c,-s],[s,c]]: m[0] = c, m[4] = s
+};
+
+struct GateInstr {
+  int32_t kind;     // GKind
+  int32_t target;
+  uint64_t cmask;   // control qubits (all must be 1)
+  double m[8];      // re00 im00 re01 im01 re10 im10 re11 im11
+  float mhl[16];    // the same eight values as (hi, lo) FP32 pairs
+};
+
+inline bool gk_is_diagonal(int k) { return k == GK_PHASE || k == GK_DIAG; }
+
+// Per-gate algorithmic bytes of one pass (read + write of every amplitude the
+// gate must touch), in units of the state's byte size S.
+double gate_bytes_fraction(const GateInstr& g);
+
+// ---------------------------------------------------------------------------
+// Tile pass: one shared-memory resident block of 2^K amplitudes per CTA,
+// indexed by the tile qubits q[0..K) (ascending, q[j] = j for j < low).
+constexpr int kMaxTileQubits = 13;
+constexpr int kTileLowQubits = 5;
+
+struct TileOp {
+  int32_t kind;       // GKind
+  int32_t tloc;       // local bit of the target, or -1 (diagonal gate whose
+                      // target lies outside the tile)
+  int32_t tglob;      // global target qubit
+  uint32_t cmask_loc; // control bits inside the tile (local positions)
+  uint64_t cmask_out; // control bits outside the tile (global positions)
+  double m[8];
+  float mhl[16];
+};
+
+struct TilePass {
+  int32_t K;
+  int32_t q[kMaxTileQubits];
+  std::vector<TileOp> ops;
+};
+
+// ---------------------------------------------------------------------------
+// The device state.
+struct State {
+  int32_t n = 0;
+  int32_t dtype = BF_C128;
+  int32_t prec = PREC_F64;
+  uint64_t N = 0;
+  void* amp = nullptr;        // interleaved complex, 16 B (C128) or 8 B (C64)
+  void* scratch = nullptr;    // second state-sized buffer, lazily allocated
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  int num_sms = 0;
+  uint64_t launches = 0;
+  // program buffer for tile ops (device) and its pinned host staging
+  TileOp* d_prog = nullptr;
+  TileOp* h_prog = nullptr;
+  size_t prog_cap = 0;
+  cudaEvent_t prog_event = nullptr;
+  bool prog_event_live = false;
+  // staging for SoA <-> interleaved conversion
+  void* d_stage = nullptr;
+  size_t stage_bytes = 0;
+  // dense unitary matrix (device copy of the current op's matrix)
+  double* d_umat = nullptr;
+  // reduction partials
+  double* d_partial = nullptr;
+  double* h_partial = nullptr;
+  size_t partial_cap = 0;
+
+  size_t amp_bytes() const { return dtype == BF_C128 ? 16 : 8; }
+  size_t bytes() const { return (size_t)N * amp_bytes(); }
+};
+
+// ---------------------------------------------------------------------------
+// Kernel launchers (device code lives in the .cu files).
+void launch_gate(State& s, const GateInstr& g);
+void launch_tile_pass(State& s, const TileOp* d_ops, int nops, const TilePass& p);
+void launch_bitrev_full(State& s);
+void launch_permute(State& s, const int32_t* src_bit_of_dst);  // dst bit j <- src bit perm[j]
+void launch_swap_bits(State& s, int a, int b);
+void launch_unitary(State& s, const double* h_u, int target, int m, int control);
+void launch_set_basis(State& s, uint64_t idx);
+void launch_interleave(State& s, const double* d_re, const double* d_im, uint64_t off, uint64_t cnt);
+void launch_deinterleave(State& s, double* d_re, double* d_im, uint64_t off, uint64_t cnt);
+double reduce_norm2(State& s);
+
+int tile_max_qubits(const State& s);
+
+// ---------------------------------------------------------------------------
+// Host planner and lowering.
+GateInstr lower_gate(const bf_op& o, uint32_t specialized);
+void validate_ops(int n, const bf_op* ops, int64_t nops);
+// Groups a run of gates into tile passes (tile width K); gates for which a
+// per-gate kernel moves fewer bytes than a tile pass stay single.
+struct PlanStep {
+  bool is_tile;
+  GateInstr gate;  // when !is_tile
+  TilePass tile;   // when is_tile
+};
+std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int K);
+
+}  // namespace bf

@@ -1,0 +1,138 @@
+// perm.cu — qubit permutations as data movement (bit-exact by construction).
+//
+//  * Full bit reversal (bit_reverse_state, state.mojo:131-204) in place as a
+//    tiled shared-memory transpose: with the index split as
+//    [h: top 5 bits][m: middle n-10 bits][l: low 5 bits], rev(i) =
+//    [rev l][rev m][rev h], so the 32x32 tile at middle value m exchanges
+//    with the transposed, bit-reversed tile at rev(m).  One CTA owns the
+//    pair (m, rev m); every global access is a 512 B run (complex128).
+//  * Any other permutation of qubit positions (partial reversal,
+//    permute_qubits, qubit reversal of a subset) as an out-of-place gather
+//    dst[j] = src[map(j)] into the scratch buffer; the two buffers are then
+//    swapped.  map(j) is assembled from a per-CTA shared-memory table of
+//    8-bit chunks.
+#include <algorithm>
+#include <utility>
+
+#include "amp_math.cuh"
+#include "bf_internal.h"
+
+namespace bf {
+
+constexpr int kRevT = 5;             // tile edge bits
+constexpr int kRevW = 1 << kRevT;    // 32
+constexpr int kRevPitch = kRevW + 1; // padded row (bank spread for the transpose)
+
+__device__ __forceinline__ uint32_t rev_bits_u32(uint32_t x, int nbits) {
+  return nbits == 0 ? 0u : (__brev(x) >> (32 - nbits));
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_bitrev_tiles(T* __restrict__ s, int n) {
+  __shared__ T ta[kRevW * kRevPitch];
+  __shared__ T tb[kRevW * kRevPitch];
+  const int M = n - 2 * kRevT;
+  const uint32_t m = blockIdx.x;
+  const uint32_t mr = rev_bits_u32(m, M);
+  if (mr < m) return;  // the partner CTA owns this pair (CTA-uniform exit)
+  const int hshift = n - kRevT;
+  const bool self = (mr == m);
+  for (int e = threadIdx.x; e < kRevW * kRevW; e += blockDim.x) {
+    int h = e >> kRevT, l = e & (kRevW - 1);
+    uint64_t ia = ((uint64_t)h << hshift) | ((uint64_t)m << kRevT) | (uint64_t)l;
+    ta[h * kRevPitch + l] = s[ia];
+    if (!self) {
+      uint64_t ib = ((uint64_t)h << hshift) | ((uint64_t)mr << kRevT) | (uint64_t)l;
+      tb[h * kRevPitch + l] = s[ib];
+    }
+  }
+  __syncthreads();
+  const T* src_for_a = self ? ta : tb;
+  for (int e = threadIdx.x; e < kRevW * kRevW; e += blockDim.x) {
+    int h = e >> kRevT, l = e & (kRevW - 1);
+    int rl = (int)rev_bits_u32((uint32_t)l, kRevT), rh = (int)rev_bits_u32((uint32_t)h, kRevT);
+    uint64_t ia = ((uint64_t)h << hshift) | ((uint64_t)m << kRevT) | (uint64_t)l;
+    s[ia] = src_for_a[rl * kRevPitch + rh];
+    if (!self) {
+      uint64_t ib = ((uint64_t)h << hshift) | ((uint64_t)mr << kRevT) | (uint64_t)l;
+      s[ib] = ta[rl * kRevPitch + rh];
+    }
+  }
+}
+
+struct PermArgs {
+  int32_t n;
+  int32_t src_of[64];  // destination bit p takes source bit src_of[p]
+};
+
+template <class T>
+__global__ void __launch_bounds__(256) k_permute(const T* __restrict__ src, T* __restrict__ dst, uint64_t N,
+                                                 const PermArgs a) {
+  __shared__ uint64_t lut[5][256];
+  const int nchunks = (a.n + 7) / 8;
+  for (int e = threadIdx.x; e < nchunks * 256; e += blockDim.x) {
+    int c = e >> 8, v = e & 255;
+    uint64_t off = 0;
+    for (int b = 0; b < 8; ++b) {
+      int p = c * 8 + b;
+      if (p < a.n && ((v >> b) & 1)) off |= 1ull << a.src_of[p];
+    }
+    lut[c][v] = off;
+  }
+  __syncthreads();
+  const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < N; j += step) {
+    uint64_t i = 0;
+    for (int c = 0; c < nchunks; ++c) i |= lut[c][(j >> (8 * c)) & 255];
+    dst[j] = src[i];
+  }
+}
+
+void ensure_scratch(State& st) {
+  if (st.scratch) return;
+  cudaError_t e = cudaMalloc(&st.scratch, st.bytes());
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    st.scratch = nullptr;
+    fail(BF_ENOMEM, "cannot allocate %zu bytes of permutation scratch", st.bytes());
+  }
+}
+
+void launch_bitrev_full(State& st) {
+  if (st.n < 2 * kRevT) {
+    int32_t src_of[64];
+    for (int p = 0; p < st.n; ++p) src_of[p] = st.n - 1 - p;
+    launch_permute(st, src_of);
+    return;
+  }
+  unsigned blocks = 1u << (st.n - 2 * kRevT);
+  if (st.dtype == BF_C128)
+    k_bitrev_tiles<double2><<<blocks, 256, 0, st.stream>>>(static_cast<double2*>(st.amp), st.n);
+  else
+    k_bitrev_tiles<float2><<<blocks, 256, 0, st.stream>>>(static_cast<float2*>(st.amp), st.n);
+  BF_CUDA(cudaGetLastError());
+  st.launches++;
+}
+
+void launch_permute(State& st, const int32_t* src_of) {
+  bool identity = true;
+  for (int p = 0; p < st.n; ++p) identity &= (src_of[p] == p);
+  if (identity) return;
+  if (st.n > 40) fail(BF_EUNSUPPORTED, "permutation of more than 40 qubits");
+  ensure_scratch(st);
+  PermArgs a;
+  a.n = st.n;
+  for (int p = 0; p < 64; ++p) a.src_of[p] = p < st.n ? src_of[p] : 0;
+  uint64_t blocks = std::min<uint64_t>((st.N + 255) / 256, (uint64_t)st.num_sms * 16);
+  if (st.dtype == BF_C128)
+    k_permute<double2><<<(unsigned)blocks, 256, 0, st.stream>>>(static_cast<const double2*>(st.amp),
+                                                                static_cast<double2*>(st.scratch), st.N, a);
+  else
+    k_permute<float2><<<(unsigned)blocks, 256, 0, st.stream>>>(static_cast<const float2*>(st.amp),
+                                                               static_cast<float2*>(st.scratch), st.N, a);
+  BF_CUDA(cudaGetLastError());
+  st.launches++;
+  std::swap(st.amp, st.scratch);
+}
+
+}  // namespace bf

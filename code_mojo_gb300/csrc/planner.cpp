@@ -1,0 +1,259 @@
+// planner.cpp — host-side lowering, validation and tile-pass planning.
+// No device code: everything here runs (and is tested) without a GPU.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+
+#include "bf_internal.h"
+
+namespace bf {
+
+void fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  throw Error{code, buf};
+}
+
+void check_cuda(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    fail(e == cudaErrorMemoryAllocation ? BF_ENOMEM : BF_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+  }
+}
+
+// ---- validation: validate_circuit (executors.mojo:78-185) ----------------
+static void check_qubit(int idx, int n, const char* label) {
+  if (idx < 0 || idx >= n) fail(BF_EINVAL, "%s out of bounds: %d", label, idx);
+}
+
+void validate_ops(int n, const bf_op* ops, int64_t nops) {
+  if (nops < 0) fail(BF_EINVAL, "negative op count");
+  if (nops > 0 && ops == nullptr) fail(BF_EINVAL, "ops is null");
+  for (int64_t i = 0; i < nops; ++i) {
+    const bf_op& o = ops[i];
+    switch (o.kind) {
+      case BF_OP_GATE: {
+        check_qubit(o.target, n, "Target");
+        if (o.gate < 0 || o.gate > BF_GATE_CUSTOM) fail(BF_EINVAL, "Unknown gate kind: %d", o.gate);
+        if (n < 64 && (o.controls >> n)) fail(BF_EINVAL, "Control out of bounds: %d", 63 - __builtin_clzll(o.controls));
+        if (o.ncontrols < 0 || __builtin_popcountll(o.controls) != o.ncontrols)
+          fail(BF_EINVAL, "Gate control kind mismatch: expected %d controls, mask holds %d", o.ncontrols,
+               __builtin_popcountll(o.controls));
+        if (o.flags & BF_OPF_FUSE_WITH_NEXT) {
+          if (i + 1 >= nops || ops[i + 1].kind != BF_OP_GATE)
+            fail(BF_EINVAL, "fused pair: the gate flagged FUSE_WITH_NEXT must be followed by a gate");
+        }
+        break;
+      }
+      case BF_OP_SWAP:
+      case BF_OP_CSWAP:
+        check_qubit(o.target, n, "Target");
+        check_qubit(o.target2, n, "Target");
+        break;
+      case BF_OP_QREV:
+      case BF_OP_BITREV:
+      case BF_OP_PERMUTE: {
+        if (o.nqubits < 0 || (o.nqubits > 0 && o.qubits == nullptr)) fail(BF_EINVAL, "qubit list is null");
+        for (int64_t k = 0; k < o.nqubits; ++k) check_qubit(o.qubits[k], n, "Target");
+        if (o.kind == BF_OP_BITREV) {
+          uint64_t seen = 0;
+          for (int64_t k = 0; k < o.nqubits; ++k) {
+            if ((seen >> o.qubits[k]) & 1) fail(BF_EINVAL, "Duplicate target: %d", o.qubits[k]);
+            seen |= 1ull << o.qubits[k];
+          }
+        }
+        if (o.kind == BF_OP_PERMUTE && o.nqubits != 0) {
+          if (o.nqubits != n) fail(BF_EINVAL, "Permutation size mismatch: %lld", (long long)o.nqubits);
+          uint64_t seen = 0;
+          for (int64_t k = 0; k < o.nqubits; ++k) {
+            if ((seen >> o.qubits[k]) & 1) fail(BF_EINVAL, "Duplicate permutation value: %d", o.qubits[k]);
+            seen |= 1ull << o.qubits[k];
+          }
+        }
+        break;
+      }
+      case BF_OP_UNITARY:
+      case BF_OP_CUNITARY: {
+        int m = o.target2;
+        if (m > 0 && (o.target < 0 || o.target + m > n)) fail(BF_EINVAL, "Target range out of bounds");
+        if (o.kind == BF_OP_CUNITARY) {
+          if (o.ncontrols != 1 || __builtin_popcountll(o.controls) != 1)
+            fail(BF_EINVAL, "Controlled unitary expects exactly one control");
+          int c = __builtin_ctzll(o.controls);
+          check_qubit(c, n, "Control");
+          if (m > 0 && c >= o.target && c < o.target + m) fail(BF_EINVAL, "Control overlaps target range");
+        }
+        if (m > 0 && o.data == nullptr) fail(BF_EINVAL, "Unitary data is null");
+        break;
+      }
+      default:
+        fail(BF_EINVAL, "Unknown transformation type: %d", o.kind);
+    }
+  }
+}
+
+// ---- lowering: GateInfo kind/arg -> matrix (gates.mojo:5-61) ---------------
+static void gate_matrix(int kind, double a, const double* mat, double* m) {
+  const double s = std::sqrt(0.5);
+  auto set = [&](double a0, double a1, double a2, double a3, double a4, double a5, double a6, double a7) {
+    m[0] = a0; m[1] = a1; m[2] = a2; m[3] = a3; m[4] = a4; m[5] = a5; m[6] = a6; m[7] = a7;
+  };
+  switch (kind) {
+    case BF_GATE_H: set(s, 0, s, 0, s, 0, -s, 0); break;
+    case BF_GATE_P: set(1, 0, 0, 0, 0, 0, std::cos(a), std::sin(a)); break;
+    case BF_GATE_X: set(0, 0, 1, 0, 1, 0, 0, 0); break;
+    case BF_GATE_Y: set(0, 0, 0, -1, 0, 1, 0, 0); break;
+    case BF_GATE_Z: set(1, 0, 0, 0, 0, 0, -1, 0); break;
+    case BF_GATE_RX: set(std::cos(a / 2), 0, 0, -std::sin(a / 2), 0, -std::sin(a / 2), std::cos(a / 2), 0); break;
+    case BF_GATE_RY: set(std::cos(a / 2), 0, -std::sin(a / 2), 0, std::sin(a / 2), 0, std::cos(a / 2), 0); break;
+    case BF_GATE_RZ: set(std::cos(a / 2), -std::sin(a / 2), 0, 0, 0, 0, std::cos(a / 2), std::sin(a / 2)); break;
+    default: std::memcpy(m, mat, 8 * sizeof(double)); break;
+  }
+}
+
+static void split_pairs(GateInstr& g) {
+  for (int i = 0; i < 8; ++i) {
+    float hi = (float)g.m[i];
+    g.mhl[2 * i] = hi;
+    g.mhl[2 * i + 1] = (float)(g.m[i] - (double)hi);
+  }
+}
+
+// Chooses the cheapest kernel form that computes the same matrix: the
+// reference's specialised H/P/X/RY/CP/CX/CRY kernels (transformations_scalar.mojo
+// :178-566) plus diagonal and permutation detection for any other kind.
+GateInstr lower_gate(const bf_op& o, uint32_t spec) {
+  GateInstr g;
+  std::memset(&g, 0, sizeof g);
+  g.target = o.target;
+  g.cmask = o.controls;
+  gate_matrix(o.gate, o.arg, o.mat, g.m);
+  const double* m = g.m;
+  const bool ctl0 = o.ncontrols == 0, ctl1 = o.ncontrols == 1;
+  bool off_zero = m[2] == 0 && m[3] == 0 && m[4] == 0 && m[5] == 0;
+  bool diag_zero = m[0] == 0 && m[1] == 0 && m[6] == 0 && m[7] == 0;
+  if (o.gate == BF_GATE_H && ctl0 && (spec & BF_SPEC_H)) {
+    g.kind = GK_H;
+  } else if (diag_zero && m[2] == 1 && m[3] == 0 && m[4] == 1 && m[5] == 0) {
+    g.kind = GK_SWAP;  // X, CX, CCX, MCX (and a CUSTOM X)
+  } else if (off_zero && m[0] == 1 && m[1] == 0) {
+    g.kind = GK_PHASE;  // P, Z, CP, CZ, MCP
+  } else if (off_zero) {
+    g.kind = GK_DIAG;  // RZ and other diagonals
+  } else if ((o.gate == BF_GATE_RY && ((ctl0 && (spec & BF_SPEC_RY)) || (ctl1 && (spec & BF_SPEC_CRY)))) ||
+             (m[1] == 0 && m[3] == 0 && m[5] == 0 && m[7] == 0 && m[0] == m[6] && m[2] == -m[4])) {
+    g.kind = GK_RY;  // real rotation [[c, -s], [s, c]]
+  } else {
+    g.kind = GK_DENSE;
+  }
+  split_pairs(g);
+  return g;
+}
+
+double gate_bytes_fraction(const GateInstr& g) {
+  int c = __builtin_popcountll(g.cmask);
+  double f = (g.kind == GK_PHASE) ? 1.0 : 2.0;  // P touches half the amplitudes
+  return f / std::ldexp(1.0, c);
+}
+
+// ---- tile-pass planning -----------------------------------------------------
+// Greedy, order-respecting grouping.  Scanning the remaining gates in order,
+// a gate joins the current pass if it commutes with every gate deferred so
+// far and its target is (or can become) a tile qubit; otherwise it is
+// deferred.  Two gates commute when, on every qubit they share, both act
+// diagonally (controls always do; a diagonal gate does on its target).
+static TileOp to_tile_op(const GateInstr& g, const int* loc_of) {
+  TileOp t;
+  std::memset(&t, 0, sizeof t);
+  t.kind = g.kind;
+  t.tglob = g.target;
+  t.tloc = loc_of[g.target];
+  for (int b = 0; b < 64; ++b) {
+    if (!((g.cmask >> b) & 1)) continue;
+    if (loc_of[b] >= 0) t.cmask_loc |= 1u << loc_of[b];
+    else t.cmask_out |= 1ull << b;
+  }
+  std::memcpy(t.m, g.m, sizeof t.m);
+  std::memcpy(t.mhl, g.mhl, sizeof t.mhl);
+  return t;
+}
+
+std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int K) {
+  std::vector<PlanStep> steps;
+  if (gates.empty()) return steps;
+  K = std::max(1, std::min(K, std::min(n, kMaxTileQubits)));
+  const int L = std::min(K, kTileLowQubits);
+  std::vector<const GateInstr*> remaining;
+  for (auto& g : gates) remaining.push_back(&g);
+  while (!remaining.empty()) {
+    uint64_t inQ = (L >= 64) ? ~0ull : ((1ull << L) - 1);
+    int nQ = L;
+    std::vector<const GateInstr*> taken, deferred;
+    uint64_t blockedX = 0, blockedAll = 0;
+    for (const GateInstr* g : remaining) {
+      bool diag = gk_is_diagonal(g->kind);
+      uint64_t tb = 1ull << g->target;
+      uint64_t Xg = diag ? 0 : tb;
+      uint64_t Ag = g->cmask | tb;
+      bool commutes = !(Xg & blockedAll) && !(Ag & blockedX);
+      bool fits = false;
+      if (commutes) {
+        if ((Xg & ~inQ) == 0) {
+          fits = true;
+        } else if (nQ + 1 <= K) {
+          inQ |= Xg;
+          nQ += 1;
+          fits = true;
+        }
+      }
+      if (fits) {
+        taken.push_back(g);
+      } else {
+        deferred.push_back(g);
+        blockedX |= Xg;
+        blockedAll |= Ag;
+      }
+    }
+    double single_bytes = 0;
+    for (const GateInstr* g : taken) single_bytes += gate_bytes_fraction(*g);
+    if (single_bytes <= 2.0) {
+      // a tile pass moves 2S; the gates on their own move no more
+      for (const GateInstr* g : taken) {
+        PlanStep st;
+        st.is_tile = false;
+        st.gate = *g;
+        steps.push_back(st);
+      }
+    } else {
+      // pad the tile with the lowest unused qubits up to K
+      for (int q = 0; q < n && nQ < K; ++q)
+        if (!((inQ >> q) & 1)) {
+          inQ |= 1ull << q;
+          nQ++;
+        }
+      PlanStep st;
+      st.is_tile = true;
+      st.tile.K = nQ;
+      int loc_of[64];
+      for (int q = 0; q < 64; ++q) loc_of[q] = -1;
+      int j = 0;
+      for (int q = 0; q < n; ++q)
+        if ((inQ >> q) & 1) {
+          st.tile.q[j] = q;
+          loc_of[q] = j;
+          ++j;
+        }
+      for (const GateInstr* g : taken) st.tile.ops.push_back(to_tile_op(*g, loc_of));
+      steps.push_back(std::move(st));
+    }
+    remaining.swap(deferred);
+  }
+  return steps;
+}
+
+}  // namespace bf

@@ -1,0 +1,119 @@
+"""Circuit builders for the benchmarked workloads.
+
+  * iqft_circuit / build_iqft_circuit / encode_value_circuit restate
+    butterfly/algos/value_encoding_circuit.mojo:5-29;
+  * qft_circuit is iqft_circuit(...).inverse() plus the final bit reversal,
+    the 20-qubit QFT workload (H on each qubit, n(n-1)/2 controlled phases
+    CP(pi/2^k), then the bit-reversal permutation);
+  * random_layered_circuit is the 30-qubit random layered workload: per layer
+    a U3(theta, phi, lambda) on every qubit with angles uniform in [0, 2pi)
+    and a CX on each pair of a seeded random perfect matching;
+  * grover_circuit follows butterfly/algos/grover.mojo:45-94 (oracle as an
+    X-conjugated multi-controlled phase, then the diffuser).
+All randomness comes from numpy's seeded PCG64 generator.
+"""
+from __future__ import annotations
+
+import math
+from typing import Sequence
+
+import numpy as np
+
+from .butterfly import QuantumCircuit, bit_reverse
+
+
+def iqft_circuit(qc: QuantumCircuit, targets: Sequence[int], swap: bool = False) -> None:
+    """value_encoding_circuit.mojo:5-12 (MSB-first inverse QFT)."""
+    for j in reversed(range(len(targets))):
+        qc.h(targets[j])
+        for k in reversed(range(j)):
+            qc.cp(targets[j], targets[k], -math.pi / 2 ** (j - k))
+    if swap:
+        bit_reverse(qc, list(targets))
+
+
+def build_iqft_circuit(n: int, swap: bool = False) -> QuantumCircuit:
+    qc = QuantumCircuit(n)
+    iqft_circuit(qc, [n - 1 - j for j in range(n)], swap=swap)
+    return qc
+
+
+def encode_value_circuit(n: int, v: float) -> QuantumCircuit:
+    """value_encoding_circuit.mojo:19-29: H on all qubits, P(2*pi*v/2^(j+1))
+    on qubit j, then the MSB-first IQFT without swap."""
+    qc = QuantumCircuit(n)
+    for j in range(n):
+        qc.h(j)
+    for j in range(n):
+        qc.p(j, 2 * math.pi / 2 ** (j + 1) * v)
+    iqft_circuit(qc, [n - 1 - j for j in range(n)])
+    return qc
+
+
+def qft_circuit(n: int, with_bit_reversal: bool = True) -> QuantumCircuit:
+    """QFT as iqft_circuit(...).inverse() (tests/test_qft_classical.mojo:40-56),
+    followed by the full bit reversal."""
+    qc = QuantumCircuit(n)
+    iqft_circuit(qc, [n - 1 - j for j in range(n)], swap=False)
+    q = qc.inverse()
+    if with_bit_reversal:
+        bit_reverse(q)
+    return q
+
+
+def random_layered_circuit(n: int, layers: int, seed: int = 0) -> QuantumCircuit:
+    """Per layer: U3 on every qubit (angles uniform in [0, 2pi)), then CX on a
+    random perfect matching (seeded shuffle, paired consecutively)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    qc = QuantumCircuit(n)
+    for _ in range(layers):
+        ang = rng.uniform(0.0, 2 * math.pi, size=(n, 3))
+        for q in range(n):
+            qc.u3(q, float(ang[q, 0]), float(ang[q, 1]), float(ang[q, 2]))
+        perm = rng.permutation(n)
+        for k in range(0, n - 1, 2):
+            qc.cx(int(perm[k]), int(perm[k + 1]))
+    return qc
+
+
+def grover_iterations(n: int) -> int:
+    return int(math.floor(math.pi / 4 * math.sqrt(2 ** n)))
+
+
+def grover_circuit(n: int, marked: int, iterations: int | None = None) -> QuantumCircuit:
+    """H^n, then `iterations` x (phase oracle for `marked`, diffuser)
+    (grover.mojo:45-94): the oracle flips the phase of |marked> with X gates
+    around an (n-1)-controlled P(pi); the diffuser is H^n, inversion about
+    |0> (X^n, MCP(pi), X^n), H^n."""
+    it = grover_iterations(n) if iterations is None else iterations
+    qc = QuantumCircuit(n)
+    for q in range(n):
+        qc.h(q)
+    ctrls = list(range(n - 1))
+    for _ in range(it):
+        flips = [q for q in range(n) if not (marked >> q) & 1]
+        for q in flips:
+            qc.x(q)
+        qc.mcp(ctrls, n - 1, math.pi)
+        for q in flips:
+            qc.x(q)
+        for q in range(n):
+            qc.h(q)
+        for q in range(n):
+            qc.x(q)
+        qc.mcp(ctrls, n - 1, math.pi)
+        for q in range(n):
+            qc.x(q)
+        for q in range(n):
+            qc.h(q)
+    return qc
+
+
+def random_normal_state(n: int, seed: int = 0) -> tuple[np.ndarray, np.ndarray]:
+    """Amplitudes with re, im i.i.d. N(0, 1) from a seed, normalised to unit
+    norm in FP64 (the QFT workload's initial state)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    re = rng.standard_normal(1 << n)
+    im = rng.standard_normal(1 << n)
+    s = math.sqrt(float(np.sum(re * re) + np.sum(im * im)))
+    return re / s, im / s

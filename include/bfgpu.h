@@ -1,0 +1,202 @@
+/*
+ * bfgpu.h — C ABI of the GB300 (sm_103a) statevector engine for Butterfly's
+ * gate-application hot path.
+ *
+ * The reference (Butterfly, Mojo) has no FFI on this path; its seam is
+ *   fn execute(mut state: QuantumState, circuit: QuantumCircuit,
+ *              ctx: ExecContext = ExecContext()) raises
+ * (butterfly/core/executors.mojo:723-730), dispatched through the
+ * function-pointer registry ExecutorFn / ExecutorEntry
+ * (butterfly/core/executors.mojo:611-712) on ctx.execution_strategy
+ * (butterfly/utils/context.mojo:33-40).  The entry points below are what a
+ * GPU ExecutorFn binds: the state moves to the device once, the circuit is
+ * flattened into an array of bf_op records, and bf_execute replaces the
+ * per-transformation dispatch of execute_with_handlers
+ * (butterfly/core/executors.mojo:268-319).
+ *
+ * Conventions
+ *  - Every function returns an int status: BF_OK (0) or a negative BF_E* code.
+ *    The message of the last failure on the calling thread is returned by
+ *    bf_last_error().  No C++ exception crosses this boundary.
+ *  - Qubit q is bit q of the amplitude index (little-endian), exactly as in
+ *    the reference (transformations_scalar.mojo:87, stride = 1 << target).
+ *  - The caller owns host arrays; the library owns device memory.
+ *  - Each state owns one CUDA stream. Work on one state is stream-ordered;
+ *    different states may run concurrently.  bf_execute only enqueues unless
+ *    opts->sync is non-zero; bf_state_download_soa / bf_state_sync block.
+ *  - Sizes are in elements unless stated otherwise.
+ */
+#ifndef BFGPU_H
+#define BFGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BFGPU_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  BF_OK = 0,
+  BF_EINVAL = -1,        /* invalid argument / circuit fails validation   */
+  BF_ENOMEM = -2,        /* device or pinned allocation failed            */
+  BF_ECUDA = -3,         /* CUDA runtime error (message has the details)  */
+  BF_EUNSUPPORTED = -4,  /* valid request this build does not handle      */
+  BF_ETIMEDOUT = -5,     /* bounded wait expired (serving loop)           */
+  BF_EBUSY = -6          /* admission refused: not enough free HBM/slots  */
+};
+
+/* ---- state element types ----------------------------------------------- */
+enum {
+  BF_C128 = 0,   /* complex128: interleaved (re, im) FP64 pairs, FP64 math  */
+  BF_C64 = 1     /* complex64:  interleaved (re, im) FP32 pairs, FP32 math  */
+};
+
+/* ---- gate kinds: values mirror GateKind (butterfly/core/gates.mojo:63-92) */
+enum {
+  BF_GATE_H = 0,
+  BF_GATE_P = 1,
+  BF_GATE_X = 2,
+  BF_GATE_Y = 3,
+  BF_GATE_Z = 4,
+  BF_GATE_RX = 5,
+  BF_GATE_RY = 6,
+  BF_GATE_RZ = 7,
+  BF_GATE_CUSTOM = 8   /* explicit 2x2 matrix in bf_op.mat                 */
+};
+
+/* ---- op kinds: one per Transformation variant (circuit.mojo:230-239) ---- */
+enum {
+  BF_OP_GATE = 0,      /* GateTransformation: controls + target + gate       */
+  BF_OP_SWAP = 1,      /* SwapTransformation(a=target, b=target2)            */
+  BF_OP_QREV = 2,      /* QubitReversalTransformation(targets; none = all)   */
+  BF_OP_UNITARY = 3,   /* UnitaryTransformation(u, target, m=target2)        */
+  BF_OP_CUNITARY = 4,  /* ControlledUnitaryTransformation(u, control, target, m) */
+  BF_OP_BITREV = 5,    /* classical bit_reverse_tr(targets; none = all)      */
+  BF_OP_PERMUTE = 6,   /* classical permute_qubits_tr(order)                 */
+  BF_OP_CSWAP = 7      /* classical swap_tr(a, b) (apply_swap)               */
+};
+
+/* bf_op.flags */
+#define BF_OPF_FUSE_WITH_NEXT 1u  /* this gate and the next one form a
+                                     FusedPairTransformation (circuit.mojo:70-88) */
+
+/*
+ * One transformation.  Layout is fixed (128 bytes, 8-byte aligned) so that a
+ * Mojo / ctypes / cgo caller can build the array without this header.
+ *   GATE:      gate, target, controls (bitmask; ncontrols = its popcount and
+ *              mirrors ControlKind), arg (angle for P/RX/RY/RZ), mat (CUSTOM).
+ *   SWAP/CSWAP: target = a, target2 = b.
+ *   QREV/BITREV/PERMUTE: qubits[0..nqubits) (nqubits = 0 means "all" for
+ *              QREV/BITREV).
+ *   UNITARY:   target, target2 = m, data = 2^m x 2^m complex row-major as
+ *              interleaved (re, im) doubles.
+ *   CUNITARY:  as UNITARY plus controls = 1 << control, ncontrols = 1.
+ */
+typedef struct bf_op {
+  int32_t kind;
+  int32_t gate;
+  int32_t target;
+  int32_t target2;
+  uint64_t controls;
+  int32_t ncontrols;
+  uint32_t flags;
+  double arg;
+  double mat[8];            /* re00 im00 re01 im01 re10 im10 re11 im11 */
+  const double* data;
+  const int32_t* qubits;
+  int64_t nqubits;
+} bf_op;
+
+/* ---- execution strategies ------------------------------------------------
+ * Values 0..7 are the reference's ExecutionStrategy (context.mojo:33-40) and
+ * are accepted only to be rejected with BF_EUNSUPPORTED (they are CPU paths).
+ * BF_STRATEGY_GPU runs one kernel per transformation (the per-gate path);
+ * BF_STRATEGY_GPU_FUSED groups consecutive gates into shared-memory tile
+ * passes (the fused-grid path).                                              */
+enum {
+  BF_STRATEGY_GPU = 8,
+  BF_STRATEGY_GPU_FUSED = 9
+};
+
+/* specialised-kernel switches, mirroring ExecContext.simd_use_specialized_*
+ * (context.mojo:79-85). */
+#define BF_SPEC_H   1u
+#define BF_SPEC_P   2u
+#define BF_SPEC_CP  4u
+#define BF_SPEC_X   8u
+#define BF_SPEC_CX  16u
+#define BF_SPEC_RY  32u
+#define BF_SPEC_CRY 64u
+#define BF_SPEC_ALL 127u
+
+typedef struct bf_exec_opts {
+  int32_t strategy;          /* BF_STRATEGY_GPU or BF_STRATEGY_GPU_FUSED       */
+  int32_t validate;          /* mirrors ExecContext.validate_circuit (default 1) */
+  uint32_t specialized;      /* BF_SPEC_* mask (default BF_SPEC_ALL)           */
+  int32_t tile_qubits;       /* fusion width of a tile pass; 0 = autotuned     */
+  int32_t sync;              /* non-zero: block until the work has finished    */
+  int32_t reserved[3];
+} bf_exec_opts;
+
+/* Fills *opts with the defaults above (strategy GPU_FUSED). */
+int bf_exec_opts_init(bf_exec_opts* opts);
+
+/* ---- library ------------------------------------------------------------- */
+int bf_version(int32_t* abi_version);
+/* Copies the last error message of the calling thread (NUL-terminated). */
+int bf_last_error(char* buf, size_t len);
+
+/* ---- state lifecycle (QuantumState, butterfly/core/state.mojo:19-98) ------ */
+typedef struct bf_state bf_state;
+
+/* Allocates 2^num_qubits amplitudes on the current device, set to |0...0>
+ * like State(n) (state.mojo:26-33). */
+int bf_state_create(int32_t num_qubits, int32_t dtype, bf_state** out);
+int bf_state_destroy(bf_state* st);
+int bf_state_info(const bf_state* st, int32_t* num_qubits, int32_t* dtype);
+/* |idx> basis state. */
+int bf_state_set_basis(bf_state* st, uint64_t idx);
+/* Host SoA arrays re[2^n], im[2^n] (the reference's layout, state.mojo:20-21)
+ * to and from the device's interleaved layout.  Download blocks. */
+int bf_state_upload_soa(bf_state* st, const double* re, const double* im);
+int bf_state_download_soa(bf_state* st, double* re, double* im);
+/* Copies amplitudes [offset, offset+count) to host SoA arrays (blocks). */
+int bf_state_download_range(bf_state* st, uint64_t offset, uint64_t count,
+                            double* re, double* im);
+int bf_state_sync(bf_state* st);
+/* The state's cudaStream_t, for callers that order their own work on it. */
+int bf_state_stream(bf_state* st, void** stream);
+
+/* ---- execution (execute, butterfly/core/executors.mojo:723-730) ---------- */
+int bf_execute(bf_state* st, const bf_op* ops, int64_t nops,
+               const bf_exec_opts* opts);
+
+/* Number of kernel launches bf_execute issued on this state since creation
+ * (or since the last reset), for launch accounting. */
+int bf_state_launch_count(const bf_state* st, uint64_t* launches, int32_t reset);
+
+/* ---- reductions ---------------------------------------------------------- */
+/* sum |amp|^2, accumulated in FP64 (state.mojo:482-501 accumulates in the
+ * state's type). */
+int bf_norm2(bf_state* st, double* out);
+
+/* ---- host-only entry points (no device needed) --------------------------- */
+/* validate_circuit (butterfly/core/executors.mojo:129-185) for a state of
+ * num_qubits qubits. */
+int bf_validate(int32_t num_qubits, const bf_op* ops, int64_t nops);
+/* Plans ops as bf_execute would and reports the launches it would issue and
+ * the algorithmic bytes they move, in units of the state's size S. */
+int bf_plan_stats(int32_t num_qubits, const bf_op* ops, int64_t nops,
+                  const bf_exec_opts* opts, int64_t* tile_passes,
+                  int64_t* gate_kernels, int64_t* other_passes,
+                  double* bytes_in_S);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BFGPU_H */

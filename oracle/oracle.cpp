@@ -1,0 +1,822 @@
+// oracle.cpp — CPU restatement of Butterfly's SCALAR strategy and a chunked
+// multi-threaded port of its SIMD_PARALLEL strategy.
+//
+// TEST INFRASTRUCTURE ONLY: loaded by tests/, __graft_entry__.smoke() and
+// bench.py's CPU legs as the checker / timed baseline, never by the engine.
+// Built with -ffp-contract=off so that every expression rounds exactly as
+// written, on x86-64 and on aarch64 alike.
+//
+// Each function names the reference code (paths inside learnqc/code_mojo)
+// whose loop order and arithmetic it restates.
+
+#include "oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+namespace {
+
+struct Cplx {
+  double re, im;
+};
+typedef Cplx Gate2[2][2];
+
+struct OrError {
+  std::string msg;
+  int code;
+};
+
+[[noreturn]] void fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  throw OrError{buf, code};
+}
+
+struct St {
+  int n;
+  size_t N;
+  double* re;
+  double* im;
+};
+
+struct Ctx {
+  uint32_t spec;   // BF_SPEC_* (ExecContext.simd_use_specialized_*)
+  int threads;     // worker threads of the parallel port
+  int chunks;      // work items per gate (get_num_chunks)
+  int strategy;
+};
+
+// ---- gates (butterfly/core/gates.mojo:5-61, cis utils/common.mojo:8-9) ----
+Cplx cis(double t) { return Cplx{cos(t), sin(t)}; }
+
+void gate_matrix(int kind, double a, const double* mat, Gate2 g) {
+  const double s = sqrt(0.5);  // sq_half_re, types.mojo:23
+  auto set = [&](Cplx a00, Cplx a01, Cplx a10, Cplx a11) {
+    g[0][0] = a00; g[0][1] = a01; g[1][0] = a10; g[1][1] = a11;
+  };
+  switch (kind) {
+    case BF_GATE_H: set({s, 0}, {s, 0}, {s, 0}, {-s, 0}); break;
+    case BF_GATE_P: set({1, 0}, {0, 0}, {0, 0}, cis(a)); break;
+    case BF_GATE_X: set({0, 0}, {1, 0}, {1, 0}, {0, 0}); break;
+    case BF_GATE_Y: set({0, 0}, {0, -1}, {0, 1}, {0, 0}); break;
+    case BF_GATE_Z: set({1, 0}, {0, 0}, {0, 0}, {-1, 0}); break;
+    case BF_GATE_RX:
+      set({cos(a / 2), 0}, {0, -sin(a / 2)}, {0, -sin(a / 2)}, {cos(a / 2), 0});
+      break;
+    case BF_GATE_RY:
+      set({cos(a / 2), 0}, {-sin(a / 2), 0}, {sin(a / 2), 0}, {cos(a / 2), 0});
+      break;
+    case BF_GATE_RZ:
+      set({cos(a / 2), -sin(a / 2)}, {0, 0}, {0, 0}, {cos(a / 2), sin(a / 2)});
+      break;
+    case BF_GATE_CUSTOM:
+      set({mat[0], mat[1]}, {mat[2], mat[3]}, {mat[4], mat[5]}, {mat[6], mat[7]});
+      break;
+    default: fail(BF_EINVAL, "Unknown gate kind: %d", kind);
+  }
+}
+
+// ---- parallel helper: the chunking of transformations_simd_parallel.mojo:
+// min(chunks, blocks) workers, each owning contiguous blocks (:13-37). -------
+template <class F>
+void for_blocks(const Ctx& c, size_t total_blocks, F&& body) {
+  if (total_blocks == 0) return;
+  if (c.strategy != OR_SIMD_PARALLEL) {
+    body(0, total_blocks);
+    return;
+  }
+  size_t items = (size_t)std::max(1, c.chunks);
+  size_t workers = std::min(items, total_blocks);
+  size_t per = std::max<size_t>(1, total_blocks / items);
+  if (workers <= 1) {
+    body(0, total_blocks);
+    return;
+  }
+  std::vector<std::thread> pool;
+  size_t nthreads = std::min<size_t>(workers, (size_t)std::max(1, c.threads));
+  // items are distributed round-robin over the threads (parallelize's pool)
+  for (size_t t = 0; t < nthreads; ++t) {
+    pool.emplace_back([&, t]() {
+      for (size_t w = t; w < workers; w += nthreads) {
+        size_t b0 = w * per;
+        size_t b1 = (w == workers - 1) ? total_blocks : (w + 1) * per;
+        body(b0, b1);
+      }
+    });
+  }
+  for (auto& th : pool) th.join();
+}
+
+// ---- process_pair_scalar (transformations_scalar.mojo:10-40) -------------
+inline void process_pair(St& s, const Gate2 g, size_t k0, size_t k1) {
+  double u_re = s.re[k0], u_im = s.im[k0], v_re = s.re[k1], v_im = s.im[k1];
+  s.re[k0] = u_re * g[0][0].re - u_im * g[0][0].im + v_re * g[0][1].re - v_im * g[0][1].im;
+  s.im[k0] = u_re * g[0][0].im + u_im * g[0][0].re + v_re * g[0][1].im + v_im * g[0][1].re;
+  s.re[k1] = u_re * g[1][0].re - u_im * g[1][0].im + v_re * g[1][1].re - v_im * g[1][1].im;
+  s.im[k1] = u_re * g[1][0].im + u_im * g[1][0].re + v_re * g[1][1].im + v_im * g[1][1].re;
+}
+
+// Pair enumeration.  SCALAR walks j in [0, N/2) with idx = 2j - r, r wrapping
+// at stride (transformations_scalar.mojo:111-117); the parallel port walks
+// contiguous 2*stride blocks (transformations_simd_parallel.mojo:341-357).
+// Both visit every pair base (bit `target` clear) exactly once.
+template <class F>
+void for_pairs(St& s, const Ctx& c, int target, F&& f) {
+  size_t stride = (size_t)1 << target;
+  if (c.strategy == OR_SCALAR) {
+    size_t r = 0;
+    for (size_t j = 0; j < s.N / 2; ++j) {
+      size_t idx = 2 * j - r;
+      f(idx, idx + stride);
+      r += 1;
+      if (r == stride) r = 0;
+    }
+    return;
+  }
+  for_blocks(c, s.N / (2 * stride), [&](size_t b0, size_t b1) {
+    for (size_t b = b0; b < b1; ++b) {
+      size_t k = b * 2 * stride;
+      for (size_t m = 0; m < stride; ++m) f(k + m, k + m + stride);
+    }
+  });
+}
+
+inline bool bit_set(size_t m, int k) { return (m >> k) & 1; }
+
+// transform_h_scalar (:233-286)
+void transform_h(St& s, const Ctx& c, int t) {
+  const double sq_half = 0.7071067811865476;
+  for_pairs(s, c, t, [&](size_t i, size_t j) {
+    double u_re = s.re[i], u_im = s.im[i], v_re = s.re[j], v_im = s.im[j];
+    s.re[i] = (u_re + v_re) * sq_half;
+    s.im[i] = (u_im + v_im) * sq_half;
+    s.re[j] = (u_re - v_re) * sq_half;
+    s.im[j] = (u_im - v_im) * sq_half;
+  });
+}
+
+// transform_p_scalar (:289-336)
+void transform_p(St& s, const Ctx& c, int t, double theta) {
+  double cs = cos(theta), sn = sin(theta);
+  for_pairs(s, c, t, [&](size_t, size_t j) {
+    double v_re = s.re[j], v_im = s.im[j];
+    s.re[j] = v_re * cs - v_im * sn;
+    s.im[j] = v_re * sn + v_im * cs;
+  });
+}
+
+// transform_x_scalar (:178-230)
+void transform_x(St& s, const Ctx& c, int t) {
+  for_pairs(s, c, t, [&](size_t i, size_t j) {
+    std::swap(s.re[i], s.re[j]);
+    std::swap(s.im[i], s.im[j]);
+  });
+}
+
+// transform_ry_scalar (:339-394)
+void transform_ry(St& s, const Ctx& c, int t, double theta) {
+  double cs = cos(theta / 2), sn = sin(theta / 2);
+  for_pairs(s, c, t, [&](size_t i, size_t j) {
+    double u_re = s.re[i], u_im = s.im[i], v_re = s.re[j], v_im = s.im[j];
+    s.re[i] = u_re * cs - v_re * sn;
+    s.im[i] = u_im * cs - v_im * sn;
+    s.re[j] = u_re * sn + v_re * cs;
+    s.im[j] = u_im * sn + v_im * cs;
+  });
+}
+
+// transform_scalar (:63-117): specialised dispatch, else the generic pair.
+void transform(St& s, const Ctx& c, int t, const Gate2 g, int kind, double arg) {
+  if (kind == BF_GATE_H && (c.spec & BF_SPEC_H)) return transform_h(s, c, t);
+  if (kind == BF_GATE_P && (c.spec & BF_SPEC_P)) return transform_p(s, c, t, arg);
+  if (kind == BF_GATE_X && (c.spec & BF_SPEC_X)) return transform_x(s, c, t);
+  if (kind == BF_GATE_RY && (c.spec & BF_SPEC_RY)) return transform_ry(s, c, t, arg);
+  for_pairs(s, c, t, [&](size_t i, size_t j) { process_pair(s, g, i, j); });
+}
+
+// c_transform_scalar (:120-175) and its specialised CP/CX/CRY (:397-566)
+void c_transform(St& s, const Ctx& c, int ctl, int t, const Gate2 g, int kind,
+                 double arg) {
+  if (kind == BF_GATE_P && (c.spec & BF_SPEC_CP)) {
+    double cs = cos(arg), sn = sin(arg);
+    for_pairs(s, c, t, [&](size_t i, size_t j) {
+      if (!bit_set(i, ctl)) return;
+      double v_re = s.re[j], v_im = s.im[j];
+      s.re[j] = v_re * cs - v_im * sn;
+      s.im[j] = v_re * sn + v_im * cs;
+    });
+    return;
+  }
+  if (kind == BF_GATE_X && (c.spec & BF_SPEC_CX)) {
+    for_pairs(s, c, t, [&](size_t i, size_t j) {
+      if (!bit_set(i, ctl)) return;
+      std::swap(s.re[i], s.re[j]);
+      std::swap(s.im[i], s.im[j]);
+    });
+    return;
+  }
+  if (kind == BF_GATE_RY && (c.spec & BF_SPEC_CRY)) {
+    double cs = cos(arg / 2), sn = sin(arg / 2);
+    for_pairs(s, c, t, [&](size_t i, size_t j) {
+      if (!bit_set(i, ctl)) return;
+      double u_re = s.re[i], u_im = s.im[i], v_re = s.re[j], v_im = s.im[j];
+      s.re[i] = u_re * cs - v_re * sn;
+      s.im[i] = u_im * cs - v_im * sn;
+      s.re[j] = u_re * sn + v_re * cs;
+      s.im[j] = u_im * sn + v_im * cs;
+    });
+    return;
+  }
+  for_pairs(s, c, t, [&](size_t i, size_t j) {
+    if (bit_set(i, ctl)) process_pair(s, g, i, j);
+  });
+}
+
+// mc_transform_scalar (:569-594): generic pair under a control mask.
+void mc_transform(St& s, const Ctx& c, uint64_t mask, int t, const Gate2 g) {
+  for_pairs(s, c, t, [&](size_t i, size_t j) {
+    if ((i & mask) == mask) process_pair(s, g, i, j);
+  });
+}
+
+// ---- dense m-qubit unitaries (transformations_unitary.mojo:22-139) --------
+void apply_unitary(St& s, const double* u, int target, int m, int control) {
+  if (m <= 0) return;
+  size_t dim = (size_t)1 << m;
+  size_t stride = (size_t)1 << target;
+  size_t block = (size_t)1 << (target + m);
+  std::vector<double> tr(dim), ti(dim), orr(dim), oi(dim);
+  for (size_t high = 0; high < s.N; high += block) {
+    for (size_t low = 0; low < stride; ++low) {
+      size_t base = high + low;
+      if (control >= 0 && (base & ((size_t)1 << control)) == 0) continue;
+      for (size_t k = 0; k < dim; ++k) {
+        size_t idx = base + (k << target);
+        tr[k] = s.re[idx];
+        ti[k] = s.im[idx];
+      }
+      for (size_t row = 0; row < dim; ++row) {
+        double sr = 0, si = 0;
+        for (size_t col = 0; col < dim; ++col) {
+          double ur = u[2 * (row * dim + col)], ui = u[2 * (row * dim + col) + 1];
+          sr += ur * tr[col] - ui * ti[col];
+          si += ur * ti[col] + ui * tr[col];
+        }
+        orr[row] = sr;
+        oi[row] = si;
+      }
+      for (size_t k = 0; k < dim; ++k) {
+        size_t idx = base + (k << target);
+        s.re[idx] = orr[k];
+        s.im[idx] = oi[k];
+      }
+    }
+  }
+}
+
+// ---- fused pair kernels (fused_kernels_sparse_global.mojo:8-250) ----------
+inline size_t insert_zero_bit(size_t x, int pos) {  // utils/bit_utils.mojo:5-10
+  size_t mask = ((size_t)1 << pos) - 1;
+  return ((x & ~mask) << 1) | (x & mask);
+}
+
+void fused_hh(St& s, int t1, int t2) {
+  int hi = std::max(t1, t2), lo = std::min(t1, t2);
+  size_t sl = (size_t)1 << lo, sh = (size_t)1 << hi;
+  const double scale = 0.5;
+  for (size_t k = 0; k < (s.N >> 2); ++k) {
+    size_t i0 = insert_zero_bit(insert_zero_bit(k, lo), hi);
+    size_t i1 = i0 + sl, i2 = i0 + sh, i3 = i1 + sh;
+    double r0 = s.re[i0], m0 = s.im[i0], r1 = s.re[i1], m1 = s.im[i1];
+    double r2 = s.re[i2], m2 = s.im[i2], r3 = s.re[i3], m3 = s.im[i3];
+    double s01r = r0 + r1, s01i = m0 + m1, d01r = r0 - r1, d01i = m0 - m1;
+    double s23r = r2 + r3, s23i = m2 + m3, d23r = r2 - r3, d23i = m2 - m3;
+    s.re[i0] = (s01r + s23r) * scale; s.im[i0] = (s01i + s23i) * scale;
+    s.re[i1] = (d01r + d23r) * scale; s.im[i1] = (d01i + d23i) * scale;
+    s.re[i2] = (s01r - s23r) * scale; s.im[i2] = (s01i - s23i) * scale;
+    s.re[i3] = (d01r - d23r) * scale; s.im[i3] = (d01i - d23i) * scale;
+  }
+}
+
+void fused_hp(St& s, int th, int tp, double theta) {
+  size_t sh = (size_t)1 << th, sp = (size_t)1 << tp;
+  int lo = std::min(th, tp), hi = std::max(th, tp);
+  const double sq_half = 0.7071067811865476;
+  double cs = cos(theta), sn = sin(theta);
+  for (size_t k = 0; k < (s.N >> 2); ++k) {
+    size_t i0 = insert_zero_bit(insert_zero_bit(k, lo), hi);
+    size_t ih = i0 | sh, ip = i0 | sp, ihp = i0 | sh | sp;
+    double r0 = s.re[i0], m0 = s.im[i0], rh = s.re[ih], mh = s.im[ih];
+    double rp = s.re[ip], mp = s.im[ip], rhp = s.re[ihp], mhp = s.im[ihp];
+    double n_r0 = (r0 + rh) * sq_half, n_i0 = (m0 + mh) * sq_half;
+    double n_rh = (r0 - rh) * sq_half, n_ih = (m0 - mh) * sq_half;
+    double n_rp = (rp + rhp) * sq_half, n_ip = (mp + mhp) * sq_half;
+    double n_rhp = (rp - rhp) * sq_half, n_ihp = (mp - mhp) * sq_half;
+    s.re[i0] = n_r0; s.im[i0] = n_i0;
+    s.re[ih] = n_rh; s.im[ih] = n_ih;
+    s.re[ip] = n_rp * cs - n_ip * sn; s.im[ip] = n_rp * sn + n_ip * cs;
+    s.re[ihp] = n_rhp * cs - n_ihp * sn; s.im[ihp] = n_rhp * sn + n_ihp * cs;
+  }
+}
+
+void fused_pp(St& s, int t1, int t2, double th1, double th2) {
+  int hi = t1, lo = t2;
+  if (t2 > t1) { hi = t2; lo = t1; std::swap(th1, th2); }
+  size_t sl = (size_t)1 << lo, sh = (size_t)1 << hi;
+  double c1 = cos(th1), s1 = sin(th1), c2 = cos(th2), s2 = sin(th2);
+  double c12 = cos(th1 + th2), s12 = sin(th1 + th2);
+  for (size_t k = 0; k < (s.N >> 2); ++k) {
+    size_t i0 = insert_zero_bit(insert_zero_bit(k, lo), hi);
+    size_t i1 = i0 | sl, i2 = i0 | sh, i3 = i1 | sh;
+    double r1 = s.re[i1], m1 = s.im[i1];
+    s.re[i1] = r1 * c2 - m1 * s2; s.im[i1] = r1 * s2 + m1 * c2;
+    double r2 = s.re[i2], m2 = s.im[i2];
+    s.re[i2] = r2 * c1 - m2 * s1; s.im[i2] = r2 * s1 + m2 * c1;
+    double r3 = s.re[i3], m3 = s.im[i3];
+    s.re[i3] = r3 * c12 - m3 * s12; s.im[i3] = r3 * s12 + m3 * c12;
+  }
+}
+
+void fused_shared_c_pp(St& s, int ctl, int t1, int t2, double th1, double th2) {
+  int b[3] = {ctl, t1, t2};
+  std::sort(b, b + 3);
+  size_t sc = (size_t)1 << ctl, s1 = (size_t)1 << t1, s2 = (size_t)1 << t2;
+  double c1 = cos(th1), n1 = sin(th1), c2 = cos(th2), n2 = sin(th2);
+  double c12 = cos(th1 + th2), n12 = sin(th1 + th2);
+  for (size_t k = 0; k < (s.N >> 3); ++k) {
+    size_t i0 = insert_zero_bit(insert_zero_bit(insert_zero_bit(k, b[0]), b[1]), b[2]);
+    size_t cb = i0 | sc;
+    size_t a = cb | s1;
+    double r = s.re[a], m = s.im[a];
+    s.re[a] = r * c1 - m * n1; s.im[a] = r * n1 + m * c1;
+    a = cb | s2;
+    r = s.re[a]; m = s.im[a];
+    s.re[a] = r * c2 - m * n2; s.im[a] = r * n2 + m * c2;
+    a = cb | s1 | s2;
+    r = s.re[a]; m = s.im[a];
+    s.re[a] = r * c12 - m * n12; s.im[a] = r * n12 + m * c12;
+  }
+}
+
+// 4x4 helpers of transformations_fusion.mojo:51-103 (complex products as
+// (a.re*b.re - a.im*b.im, a.re*b.im + a.im*b.re)).
+void gate_to_4x4(const Gate2 g, int q_low, int target, Cplx* m) {
+  for (int i = 0; i < 16; ++i) m[i] = Cplx{0, 0};
+  if (target == q_low) {
+    for (int b1 = 0; b1 < 2; ++b1)
+      for (int r0 = 0; r0 < 2; ++r0)
+        for (int c0 = 0; c0 < 2; ++c0) m[(r0 + 2 * b1) * 4 + c0 + 2 * b1] = g[r0][c0];
+  } else {
+    for (int b0 = 0; b0 < 2; ++b0)
+      for (int r1 = 0; r1 < 2; ++r1)
+        for (int c1 = 0; c1 < 2; ++c1) m[(b0 + 2 * r1) * 4 + b0 + 2 * c1] = g[r1][c1];
+  }
+}
+
+void cgate_to_4x4(const Gate2 g, int q_low, int control, int target, Cplx* m) {
+  for (int i = 0; i < 16; ++i) m[i] = Cplx{0, 0};
+  for (int b0 = 0; b0 < 2; ++b0)
+    for (int b1 = 0; b1 < 2; ++b1) {
+      int in = b0 + 2 * b1;
+      int cb = control == q_low ? b0 : b1;
+      int tb = target == q_low ? b0 : b1;
+      if (cb == 0) {
+        m[in * 4 + in] = Cplx{1, 0};
+      } else {
+        for (int ot = 0; ot < 2; ++ot) {
+          int ob0 = b0, ob1 = b1;
+          if (target == q_low) ob0 = ot; else ob1 = ot;
+          m[(ob0 + 2 * ob1) * 4 + in] = g[ot][tb];
+        }
+      }
+    }
+}
+
+void matmul4(const Cplx* a, const Cplx* b, Cplx* out) {
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 4; ++c) {
+      Cplx sum{0, 0};
+      for (int k = 0; k < 4; ++k) {
+        Cplx x = a[r * 4 + k], y = b[k * 4 + c];
+        sum.re = sum.re + (x.re * y.re - x.im * y.im);
+        sum.im = sum.im + (x.re * y.im + x.im * y.re);
+      }
+      out[r * 4 + c] = sum;
+    }
+}
+
+bool is_h(const bf_op& o) { return o.ncontrols == 0 && o.gate == BF_GATE_H; }
+bool is_p(const bf_op& o) { return o.ncontrols == 0 && o.gate == BF_GATE_P; }
+bool is_cp(const bf_op& o) { return o.ncontrols == 1 && o.gate == BF_GATE_P; }
+int lowest_bit(uint64_t m) { return m ? __builtin_ctzll(m) : 0; }
+
+// apply_fused_pair (transformations_fusion.mojo:221-310)
+void apply_fused_pair(St& s, const bf_op& t0, const bf_op& t1) {
+  if (is_cp(t0) && is_cp(t1) && t0.controls == t1.controls) {
+    int ctl = lowest_bit(t0.controls);
+    if (t0.target > t1.target)
+      fused_shared_c_pp(s, ctl, t0.target, t1.target, t0.arg, t1.arg);
+    else
+      fused_shared_c_pp(s, ctl, t1.target, t0.target, t1.arg, t0.arg);
+    return;
+  }
+  if (is_h(t0) && is_h(t1)) return fused_hh(s, t0.target, t1.target);
+  if (is_p(t0) && is_p(t1)) {
+    if (t0.target > t1.target) fused_pp(s, t0.target, t1.target, t0.arg, t1.arg);
+    else fused_pp(s, t1.target, t0.target, t1.arg, t0.arg);
+    return;
+  }
+  if (is_h(t0) && is_p(t1)) return fused_hp(s, t0.target, t1.target, t1.arg);
+  if (is_p(t0) && is_h(t1)) return fused_hp(s, t1.target, t0.target, t0.arg);
+  int c0 = t0.ncontrols == 1 ? lowest_bit(t0.controls) : 0;
+  int c1 = t1.ncontrols == 1 ? lowest_bit(t1.controls) : 0;
+  int q_low = t0.target;
+  if (t0.ncontrols == 1) q_low = std::min(q_low, c0);
+  q_low = std::min(q_low, t1.target);
+  if (t1.ncontrols == 1) q_low = std::min(q_low, c1);
+  Gate2 g0, g1;
+  gate_matrix(t0.gate, t0.arg, t0.mat, g0);
+  gate_matrix(t1.gate, t1.arg, t1.mat, g1);
+  Cplx m0[16], m1[16], m[16];
+  if (t0.ncontrols == 1) cgate_to_4x4(g0, q_low, c0, t0.target, m0);
+  else gate_to_4x4(g0, q_low, t0.target, m0);
+  if (t1.ncontrols == 1) cgate_to_4x4(g1, q_low, c1, t1.target, m1);
+  else gate_to_4x4(g1, q_low, t1.target, m1);
+  matmul4(m1, m0, m);
+  double u[32];
+  for (int i = 0; i < 16; ++i) { u[2 * i] = m[i].re; u[2 * i + 1] = m[i].im; }
+  apply_unitary(s, u, q_low, 2, -1);
+}
+
+// ---- permutations (state.mojo:131-445, utils/common.mojo:12-19) ---------
+size_t rev_bits(size_t i, int n) {
+  size_t r = 0;
+  for (int b = 0; b < n; ++b) r |= ((i >> b) & 1) << (n - 1 - b);
+  return r;
+}
+
+// bit_reverse_state (:131-204): out[i] = in[rev(i)] into fresh arrays.
+void bit_reverse_full(St& s) {
+  std::vector<double> nr(s.N), ni(s.N);
+  for (size_t i = 0; i < s.N; ++i) {
+    size_t r = rev_bits(i, s.n);
+    nr[i] = s.re[r];
+    ni[i] = s.im[r];
+  }
+  memcpy(s.re, nr.data(), s.N * sizeof(double));
+  memcpy(s.im, ni.data(), s.N * sizeof(double));
+}
+
+// partial_bit_reverse_state (:252-301)
+void bit_reverse_partial(St& s, std::vector<int> t) {
+  int k = (int)t.size();
+  if (k <= 1) return;
+  std::sort(t.begin(), t.end());
+  for (size_t il = 0; il < s.N; ++il) {
+    size_t is = 0;
+    for (int b = 0; b < k; ++b)
+      if ((il >> t[b]) & 1) is |= (size_t)1 << b;
+    size_t js = 0;
+    for (int b = 0; b < k; ++b)
+      if ((is >> b) & 1) js |= (size_t)1 << (k - 1 - b);
+    if (is < js) {
+      size_t jl = il;
+      for (int b = 0; b < k; ++b) {
+        if ((js >> b) & 1) jl |= (size_t)1 << t[b];
+        else jl &= ~((size_t)1 << t[b]);
+      }
+      std::swap(s.re[il], s.re[jl]);
+      std::swap(s.im[il], s.im[jl]);
+    }
+  }
+}
+
+// swap_bits_state (:304-317) with swap_bits_index (common.mojo:12-19)
+void swap_bits(St& s, int a, int b) {
+  if (a == b) return;
+  for (size_t i = 0; i < s.N; ++i) {
+    size_t x = ((i >> a) ^ (i >> b)) & 1;
+    size_t j = i ^ ((x << a) | (x << b));
+    if (j > i) {
+      std::swap(s.re[i], s.re[j]);
+      std::swap(s.im[i], s.im[j]);
+    }
+  }
+}
+
+// apply_permute_qubits (:393-431)
+void permute_qubits(St& s, const int32_t* order, int64_t cnt) {
+  if (cnt == 0) return;
+  if (cnt != s.n) fail(BF_EINVAL, "Permutation size mismatch: %lld", (long long)cnt);
+  std::vector<bool> seen(s.n, false);
+  for (int i = 0; i < s.n; ++i) {
+    int v = order[i];
+    if (v < 0 || v >= s.n) fail(BF_EINVAL, "Invalid permutation value: %d", v);
+    if (seen[v]) fail(BF_EINVAL, "Duplicate permutation value: %d", v);
+    seen[v] = true;
+  }
+  std::vector<int> perm(s.n);
+  for (int i = 0; i < s.n; ++i) perm[i] = i;
+  for (int i = 0; i < s.n; ++i) {
+    if (perm[i] == order[i]) continue;
+    int j = i + 1;
+    while (j < s.n && perm[j] != order[i]) ++j;
+    if (j >= s.n) fail(BF_EINVAL, "Invalid permutation order");
+    swap_bits(s, i, j);
+    std::swap(perm[i], perm[j]);
+  }
+}
+
+// ---- validation (executors.mojo:78-185) -----------------------------------
+void check_qubit(int idx, int n, const char* label) {
+  if (idx < 0 || idx >= n) fail(BF_EINVAL, "%s out of bounds: %d", label, idx);
+}
+
+void validate(const St& s, const bf_op* ops, int64_t nops) {
+  int n = s.n;
+  for (int64_t i = 0; i < nops; ++i) {
+    const bf_op& o = ops[i];
+    switch (o.kind) {
+      case BF_OP_GATE: {
+        check_qubit(o.target, n, "Target");
+        if (o.ncontrols < 0 || __builtin_popcountll(o.controls) != o.ncontrols)
+          fail(BF_EINVAL, "Gate control kind mismatch: %d controls in a mask of %d",
+               o.ncontrols, __builtin_popcountll(o.controls));
+        if (n < 64 && (o.controls >> n))
+          fail(BF_EINVAL, "Control out of bounds: %d", 63 - __builtin_clzll(o.controls));
+        if (o.gate < 0 || o.gate > BF_GATE_CUSTOM) fail(BF_EINVAL, "Unknown gate kind: %d", o.gate);
+        break;
+      }
+      case BF_OP_SWAP:
+      case BF_OP_CSWAP:
+        check_qubit(o.target, n, "Target");
+        check_qubit(o.target2, n, "Target");
+        break;
+      case BF_OP_QREV:
+      case BF_OP_BITREV:
+      case BF_OP_PERMUTE:
+        for (int64_t k = 0; k < o.nqubits; ++k) check_qubit(o.qubits[k], n, "Target");
+        break;
+      case BF_OP_UNITARY:
+      case BF_OP_CUNITARY: {
+        int m = o.target2;
+        if (m > 0 && (o.target < 0 || o.target + m > n)) fail(BF_EINVAL, "Target range out of bounds");
+        if (o.kind == BF_OP_CUNITARY) {
+          if (o.ncontrols != 1 || __builtin_popcountll(o.controls) != 1)
+            fail(BF_EINVAL, "Controlled unitary expects exactly one control");
+          int c = lowest_bit(o.controls);
+          check_qubit(c, n, "Control");
+          if (m > 0 && c >= o.target && c < o.target + m) fail(BF_EINVAL, "Control overlaps target range");
+        }
+        if (m > 0 && o.data == nullptr) fail(BF_EINVAL, "Unitary data is null");
+        break;
+      }
+      default: fail(BF_EINVAL, "Unknown transformation type: %d", o.kind);
+    }
+  }
+}
+
+// ---- executor (execute_with_handlers, executors.mojo:268-319) -------------
+void cx(St& s, const Ctx& c, int ctl, int t) {  // handle_cx_scalar (:368-372)
+  Gate2 g;
+  gate_matrix(BF_GATE_X, 0, nullptr, g);
+  if (c.strategy == OR_SCALAR) c_transform(s, c, ctl, t, g, BF_GATE_X, 0);
+  else mc_transform(s, c, (uint64_t)1 << ctl, t, g);  // handle_cx_simd_parallel
+}
+
+void gate_op(St& s, const Ctx& c, const bf_op& o) {
+  Gate2 g;
+  gate_matrix(o.gate, o.arg, o.mat, g);
+  if (o.ncontrols == 0) {
+    // handle_gate_scalar / handle_gate_simd_parallel share this dispatch for
+    // the specialised kinds, then the generic pair kernel.
+    transform(s, c, o.target, g, o.gate, o.arg);
+  } else if (o.ncontrols == 1) {
+    int ctl = lowest_bit(o.controls);
+    if (c.strategy == OR_SCALAR) {
+      c_transform(s, c, ctl, o.target, g, o.gate, o.arg);
+    } else {
+      bool spec = (o.gate == BF_GATE_P && (c.spec & BF_SPEC_CP)) ||
+                  (o.gate == BF_GATE_X && (c.spec & BF_SPEC_CX)) ||
+                  (o.gate == BF_GATE_RY && (c.spec & BF_SPEC_CRY));
+      if (spec) c_transform(s, c, ctl, o.target, g, o.gate, o.arg);
+      else mc_transform(s, c, o.controls, o.target, g);
+    }
+  } else {
+    mc_transform(s, c, o.controls, o.target, g);
+  }
+}
+
+void run(St& s, const Ctx& c, const bf_op* ops, int64_t nops, bool do_validate) {
+  if (do_validate) validate(s, ops, nops);
+  for (int64_t i = 0; i < nops; ++i) {
+    const bf_op& o = ops[i];
+    switch (o.kind) {
+      case BF_OP_GATE:
+        if ((o.flags & BF_OPF_FUSE_WITH_NEXT) && i + 1 < nops && ops[i + 1].kind == BF_OP_GATE) {
+          apply_fused_pair(s, o, ops[i + 1]);
+          ++i;
+        } else {
+          gate_op(s, c, o);
+        }
+        break;
+      case BF_OP_SWAP:  // apply_swap_with_cx (:231-241)
+        if (o.target != o.target2) {
+          cx(s, c, o.target, o.target2);
+          cx(s, c, o.target2, o.target);
+          cx(s, c, o.target, o.target2);
+        }
+        break;
+      case BF_OP_QREV: {  // apply_qubit_reversal_with_cx (:244-265)
+        std::vector<int> t;
+        if (o.nqubits == 0) for (int q = 0; q < s.n; ++q) t.push_back(q);
+        else t.assign(o.qubits, o.qubits + o.nqubits);
+        std::sort(t.begin(), t.end());
+        size_t half = t.size() / 2;
+        for (size_t k = 0; k < half; ++k) {
+          int a = t[k], b = t[t.size() - 1 - k];
+          if (a == b) continue;
+          cx(s, c, a, b);
+          cx(s, c, b, a);
+          cx(s, c, a, b);
+        }
+        break;
+      }
+      case BF_OP_UNITARY:
+        apply_unitary(s, o.data, o.target, o.target2, -1);
+        break;
+      case BF_OP_CUNITARY:
+        apply_unitary(s, o.data, o.target, o.target2, lowest_bit(o.controls));
+        break;
+      case BF_OP_BITREV:  // apply_bit_reverse (:383-390)
+        if (o.nqubits == 0) bit_reverse_full(s);
+        else bit_reverse_partial(s, std::vector<int>(o.qubits, o.qubits + o.nqubits));
+        break;
+      case BF_OP_PERMUTE:
+        permute_qubits(s, o.qubits, o.nqubits);
+        break;
+      case BF_OP_CSWAP:  // apply_swap (:434-444)
+        swap_bits(s, o.target, o.target2);
+        break;
+      default:
+        fail(BF_EINVAL, "Unknown transformation type: %d", o.kind);
+    }
+  }
+}
+
+void set_err(char* err, size_t len, const std::string& m) {
+  if (err && len) {
+    size_t k = std::min(len - 1, m.size());
+    memcpy(err, m.data(), k);
+    err[k] = 0;
+  }
+}
+
+// ---- classical QFT (butterfly/algos/qft_classical.mojo) -------------------
+void fft_in_place(std::vector<double>& re, std::vector<double>& im, bool inverse) {
+  size_t n = re.size();
+  if (n <= 1) return;
+  int log_n = 0;
+  while (((size_t)1 << log_n) < n) ++log_n;
+  for (size_t i = 0; i < n; ++i) {  // _bit_reverse_in_place (:51-75)
+    size_t j = rev_bits(i, log_n);
+    if (i < j) { std::swap(re[i], re[j]); std::swap(im[i], im[j]); }
+  }
+  double sign = inverse ? -1.0 : 1.0;
+  const double two_pi = 2.0 * M_PI;
+  for (size_t step = 2; step <= n; step *= 2) {  // _fft_in_place (:78-119)
+    size_t half = step / 2;
+    double theta = sign * two_pi / (double)step;
+    double wmr = cos(theta), wmi = sin(theta);
+    for (size_t k = 0; k < n; k += step) {
+      double wr = 1, wi = 0;
+      for (size_t j = 0; j < half; ++j) {
+        double tr = wr * re[k + j + half] - wi * im[k + j + half];
+        double ti = wr * im[k + j + half] + wi * re[k + j + half];
+        double ur = re[k + j], ui = im[k + j];
+        re[k + j] = ur + tr; im[k + j] = ui + ti;
+        re[k + j + half] = ur - tr; im[k + j + half] = ui - ti;
+        double nwr = wr * wmr - wi * wmi;
+        double nwi = wr * wmi + wi * wmr;
+        wr = nwr; wi = nwi;
+      }
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int or_execute(int32_t n, double* re, double* im, const bf_op* ops, int64_t nops,
+               int32_t strategy, int32_t threads, int32_t chunks, uint32_t specialized,
+               int32_t validate_flag, char* err, size_t errlen) {
+  try {
+    if (n < 0 || n > 40) fail(BF_EINVAL, "State size must be a power of two");
+    if (strategy != OR_SCALAR && strategy != OR_SIMD_PARALLEL)
+      fail(BF_EUNSUPPORTED, "Unknown execution strategy: %d", strategy);
+    St s{n, (size_t)1 << n, re, im};
+    Ctx c;
+    c.spec = specialized;
+    c.strategy = strategy;
+    c.threads = threads > 0 ? threads : or_num_cores();
+    c.chunks = chunks > 0 ? chunks : c.threads;
+    run(s, c, ops, nops, validate_flag != 0);
+    return BF_OK;
+  } catch (const OrError& e) {
+    set_err(err, errlen, e.msg);
+    return e.code;
+  }
+}
+
+// _apply_qft_like (qft_classical.mojo:122-210)
+int or_qft_classical(int32_t n, double* re, double* im, const int32_t* targets,
+                     int32_t ntargets, int32_t inverse, int32_t swap, char* err,
+                     size_t errlen) {
+  try {
+    St s{n, (size_t)1 << n, re, im};
+    std::vector<int> t;
+    if (ntargets == 0) for (int q = 0; q < n; ++q) t.push_back(q);
+    else {
+      std::vector<bool> seen(n, false);
+      for (int i = 0; i < ntargets; ++i) {
+        int q = targets[i];
+        if (q < 0 || q >= n) fail(BF_EINVAL, "Target out of bounds: %d", q);
+        if (seen[q]) fail(BF_EINVAL, "Duplicate target: %d", q);
+        seen[q] = true;
+        t.push_back(q);
+      }
+    }
+    if (t.empty()) return BF_OK;
+    bool lsb_first = true;
+    for (size_t i = 1; i < t.size(); ++i)
+      if (t[i] <= t[i - 1]) { lsb_first = false; break; }
+    bool pre = false, post = false;
+    if (inverse) {
+      if (lsb_first) post = !swap;
+      else { pre = true; post = swap; }
+    } else {
+      if (lsb_first) pre = !swap;
+      else { pre = swap; post = true; }
+    }
+    auto bitrev = [&]() {
+      if ((int)t.size() == n) bit_reverse_full(s);
+      else bit_reverse_partial(s, t);
+    };
+    if (pre) bitrev();
+    std::vector<bool> is_t(n, false);
+    for (int q : t) is_t[q] = true;
+    std::vector<int> other;
+    for (int q = 0; q < n; ++q) if (!is_t[q]) other.push_back(q);
+    size_t nt = t.size(), bs = (size_t)1 << nt;
+    double scale = 1.0 / sqrt((double)bs);
+    std::vector<double> tr(bs), ti(bs);
+    for (size_t blk = 0; blk < ((size_t)1 << other.size()); ++blk) {
+      size_t base = 0;
+      for (size_t i = 0; i < other.size(); ++i)
+        if ((blk >> i) & 1) base |= (size_t)1 << other[i];
+      auto idx_of = [&](size_t tm) {
+        size_t idx = base;
+        for (size_t j = 0; j < nt; ++j)
+          if ((tm >> j) & 1) idx |= (size_t)1 << (lsb_first ? t[j] : t[nt - 1 - j]);
+        return idx;
+      };
+      for (size_t tm = 0; tm < bs; ++tm) { size_t i = idx_of(tm); tr[tm] = re[i]; ti[tm] = im[i]; }
+      fft_in_place(tr, ti, inverse != 0);
+      for (size_t tm = 0; tm < bs; ++tm) { size_t i = idx_of(tm); re[i] = tr[tm] * scale; im[i] = ti[tm] * scale; }
+    }
+    if (post) bitrev();
+    return BF_OK;
+  } catch (const OrError& e) {
+    set_err(err, errlen, e.msg);
+    return e.code;
+  }
+}
+
+void or_bit_reverse_indices(int32_t n, uint64_t* out_index) {
+  size_t N = (size_t)1 << n;
+  for (size_t i = 0; i < N; ++i) out_index[i] = rev_bits(i, n);
+}
+
+double or_norm2(int32_t n, const double* re, const double* im) {
+  size_t N = (size_t)1 << n;
+  double acc = 0;
+  for (size_t i = 0; i < N; ++i) acc += re[i] * re[i] + im[i] * im[i];
+  return acc;
+}
+
+int32_t or_num_cores(void) {
+  unsigned c = std::thread::hardware_concurrency();
+  return c ? (int32_t)c : 1;
+}
+
+}  // extern "C"

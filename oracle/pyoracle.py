@@ -1,0 +1,108 @@
+"""ctypes loader of the CPU oracle (oracle/_build/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU legs of bench.py.  The engine never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent.parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+from code_mojo_gb300 import _ffi as F  # noqa: E402  (bf_op layout only; no engine calls)
+
+LIB_PATH = Path(__file__).resolve().parent / "_build" / "liboracle.so"
+OR_SCALAR, OR_SIMD_PARALLEL = 0, 3
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} missing: run `make -C oracle`")
+        L = C.CDLL(str(LIB_PATH))
+        L.or_execute.argtypes = [C.c_int32, C.c_void_p, C.c_void_p, C.POINTER(F.bf_op), C.c_int64, C.c_int32,
+                                 C.c_int32, C.c_int32, C.c_uint32, C.c_int32, C.c_char_p, C.c_size_t]
+        L.or_execute.restype = C.c_int
+        L.or_qft_classical.argtypes = [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32,
+                                       C.c_int32, C.c_char_p, C.c_size_t]
+        L.or_qft_classical.restype = C.c_int
+        L.or_bit_reverse_indices.argtypes = [C.c_int32, C.c_void_p]
+        L.or_bit_reverse_indices.restype = None
+        L.or_norm2.argtypes = [C.c_int32, C.c_void_p, C.c_void_p]
+        L.or_norm2.restype = C.c_double
+        L.or_num_cores.argtypes = []
+        L.or_num_cores.restype = C.c_int32
+        _lib = L
+    return _lib
+
+
+class OracleError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(msg)
+        self.code = code
+
+
+def run(circuit, re: np.ndarray, im: np.ndarray, strategy: int = OR_SCALAR, threads: int = 0, chunks: int = 0,
+        specialized: int = 127, validate: bool = True) -> tuple[np.ndarray, np.ndarray]:
+    """Runs `circuit` (a butterfly.QuantumCircuit) on copies of (re, im)."""
+    re = np.array(re, dtype=np.float64, copy=True)
+    im = np.array(im, dtype=np.float64, copy=True)
+    n = int(re.size).bit_length() - 1
+    arr, cnt, keep = circuit.to_ops()
+    err = C.create_string_buffer(512)
+    rc = lib().or_execute(n, re.ctypes.data, im.ctypes.data, arr, cnt, strategy, threads, chunks, specialized,
+                          1 if validate else 0, err, len(err))
+    del keep
+    if rc != 0:
+        raise OracleError(rc, err.value.decode())
+    return re, im
+
+
+def run_inplace(circuit, re: np.ndarray, im: np.ndarray, strategy: int = OR_SCALAR, threads: int = 0,
+                chunks: int = 0) -> None:
+    n = int(re.size).bit_length() - 1
+    arr, cnt, keep = circuit.to_ops()
+    err = C.create_string_buffer(512)
+    rc = lib().or_execute(n, re.ctypes.data, im.ctypes.data, arr, cnt, strategy, threads, chunks, 127, 1, err,
+                          len(err))
+    del keep
+    if rc != 0:
+        raise OracleError(rc, err.value.decode())
+
+
+def basis(n: int, idx: int = 0) -> tuple[np.ndarray, np.ndarray]:
+    re = np.zeros(1 << n)
+    im = np.zeros(1 << n)
+    re[idx] = 1.0
+    return re, im
+
+
+def qft_classical(re, im, targets=(), inverse=False, swap=False):
+    re = np.array(re, dtype=np.float64, copy=True)
+    im = np.array(im, dtype=np.float64, copy=True)
+    n = int(re.size).bit_length() - 1
+    t = (C.c_int32 * max(1, len(targets)))(*targets)
+    err = C.create_string_buffer(512)
+    rc = lib().or_qft_classical(n, re.ctypes.data, im.ctypes.data, t, len(targets), int(inverse), int(swap), err,
+                                len(err))
+    if rc != 0:
+        raise OracleError(rc, err.value.decode())
+    return re, im
+
+
+def bit_reverse_indices(n: int) -> np.ndarray:
+    out = np.empty(1 << n, dtype=np.uint64)
+    lib().or_bit_reverse_indices(n, out.ctypes.data)
+    return out
+
+
+def num_cores() -> int:
+    return int(lib().or_num_cores())

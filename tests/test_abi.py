@@ -1,0 +1,147 @@
+"""CPU tests of the C ABI: the library loads, exports exactly what
+include/bfgpu.h declares, and its host-only logic (validation, planning)
+behaves like the reference's validate_circuit.  No kernel is launched."""
+import ctypes as C
+import math
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from code_mojo_gb300 import _ffi as F
+from code_mojo_gb300 import butterfly as bfy
+from code_mojo_gb300 import workloads as W
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def header_functions():
+    text = (ROOT / "include" / "bfgpu.h").read_text()
+    return set(re.findall(r"^int (bf_\w+)\(", text, flags=re.M))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = F.lib()
+    declared = header_functions()
+    assert declared, "no declarations parsed"
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert declared == set(F.SIGNATURES), declared ^ set(F.SIGNATURES)
+
+
+def test_library_exports_nothing_undeclared():
+    out = subprocess.run(["nm", "-D", "--defined-only", str(F.LIB_PATH)], capture_output=True, text=True)
+    if out.returncode != 0:
+        pytest.skip("nm unavailable")
+    exported = {l.split()[-1] for l in out.stdout.splitlines() if re.search(r" T bf_", l)}
+    assert exported == header_functions()
+
+
+def test_struct_layouts():
+    assert C.sizeof(F.bf_op) == 128
+    assert C.sizeof(F.bf_exec_opts) == 32
+    v = C.c_int32()
+    F.check(F.lib().bf_version(C.byref(v)))
+    assert v.value == 1
+
+
+def test_exec_opts_defaults():
+    o = F.bf_exec_opts()
+    F.check(F.lib().bf_exec_opts_init(C.byref(o)))
+    assert (o.strategy, o.validate, o.specialized, o.tile_qubits, o.sync) == (9, 1, 127, 0, 0)
+
+
+def test_state_create_rejects_bad_arguments_without_device():
+    h = C.c_void_p()
+    assert F.lib().bf_state_create(0, 0, C.byref(h)) == F.BF_EINVAL
+    assert "num_qubits" in F.last_error()
+    assert F.lib().bf_state_create(10, 7, C.byref(h)) == F.BF_EINVAL
+    assert "dtype" in F.last_error()
+
+
+# ---- validate_circuit (executors.mojo:90-185) --------------------------------
+@pytest.mark.parametrize("build,msg", [
+    (lambda qc: qc.h(9), "Target out of bounds: 9"),
+    (lambda qc: qc.h(-1), "Target out of bounds: -1"),
+    (lambda qc: qc.cx(7, 1), "Control out of bounds: 7"),
+    (lambda qc: qc.unitary(np.eye(4), 3, 2), "Target range out of bounds"),
+    (lambda qc: qc.c_unitary(np.eye(4), 1, 0, 2), "Control overlaps target range"),
+    (lambda qc: qc.swap(0, 4), "Target out of bounds: 4"),
+    (lambda qc: qc.qubit_reversal([1, 5]), "Target out of bounds: 5"),
+    (lambda qc: bfy.permute_qubits(qc, [0, 1, 2]), "Permutation size mismatch: 3"),
+    (lambda qc: bfy.permute_qubits(qc, [0, 1, 1, 2]), "Duplicate permutation value: 1"),
+    (lambda qc: bfy.bit_reverse(qc, [1, 1]), "Duplicate target: 1"),
+])
+def test_validation_messages(build, msg):
+    qc = bfy.QuantumCircuit(4)
+    build(qc)
+    with pytest.raises(F.BFError, match=msg) as e:
+        bfy.validate(qc)
+    assert e.value.code == F.BF_EINVAL
+
+
+def test_validation_accepts_valid_circuits():
+    for qc in (W.qft_circuit(8), W.random_layered_circuit(9, 3, 1), W.grover_circuit(5, 3, 1),
+               W.encode_value_circuit(7, 4.7)):
+        bfy.validate(qc)
+
+
+def test_control_kind_mismatch_is_rejected():
+    qc = bfy.QuantumCircuit(4)
+    qc.cx(1, 2)
+    arr, n, keep = qc.to_ops()
+    arr[0].ncontrols = 2
+    assert F.lib().bf_validate(4, arr, n) == F.BF_EINVAL
+    assert "control kind mismatch" in F.last_error()
+
+
+# ---- planner ------------------------------------------------------------------
+def stats(qc, strategy=bfy.ExecutionStrategy.GPU_FUSED, K=11):
+    ctx = bfy.ExecContext()
+    ctx.execution_strategy = strategy
+    ctx.gpu_tile_qubits = K
+    return bfy.plan_stats(qc, ctx)
+
+
+def test_per_gate_plan_launches_one_kernel_per_gate():
+    qc = W.random_layered_circuit(12, 2, 0)
+    s = stats(qc, bfy.ExecutionStrategy.GPU)
+    assert s["tile_passes"] == 0 and s["gate_kernels"] == len(qc.transformations)
+    # 24 dense U3 (2S each) + 12 CX (S each)
+    assert math.isclose(s["bytes_in_S"], 24 * 2 + 12 * 1)
+
+
+def test_qft20_fuses_to_few_passes():
+    qc = W.qft_circuit(20)
+    s = stats(qc, K=11)
+    # 20 H spread over the qubits: 6 free tile slots beside the 5 low qubits
+    assert s["tile_passes"] <= 4 and s["gate_kernels"] == 0 and s["other_passes"] == 1
+    unfused = stats(qc, bfy.ExecutionStrategy.GPU)
+    assert unfused["bytes_in_S"] == pytest.approx(20 * 2 + 190 * 0.5 + 2)
+
+
+@pytest.mark.parametrize("K", [6, 8, 10, 11, 12, 13])
+def test_random_layered_pass_count_shrinks_with_width(K):
+    qc = W.random_layered_circuit(30, 40, 0)
+    s = stats(qc, K=K)
+    total = s["tile_passes"] + s["gate_kernels"]
+    assert 0 < total < 1800
+    assert s["bytes_in_S"] < 3000
+
+
+def test_wider_tiles_move_fewer_bytes():
+    qc = W.random_layered_circuit(30, 10, 0)
+    b = [stats(qc, K=K)["bytes_in_S"] for K in (7, 9, 11, 13)]
+    assert b == sorted(b, reverse=True)
+
+
+def test_diagonal_gates_never_constrain_tiles():
+    qc = bfy.QuantumCircuit(24)
+    for q in range(24):
+        qc.h(q % 5)
+        qc.cp(23 - q, q, 0.1 * q)
+        qc.p(q, 0.2)
+    s = stats(qc, K=6)
+    assert s["tile_passes"] == 1 and s["gate_kernels"] == 0
