@@ -75,6 +75,7 @@ struct TileOp {
 
 struct TilePass {
   int32_t K;
+  int32_t L;   // q[j] = j for j < L (the always-resident low qubits)
   int32_t q[kMaxTileQubits];
   std::vector<TileOp> ops;
 };

@@ -187,7 +187,9 @@ std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int
   std::vector<PlanStep> steps;
   if (gates.empty()) return steps;
   K = std::max(1, std::min(K, std::min(n, kMaxTileQubits)));
-  const int L = std::min(K, kTileLowQubits);
+  // Low qubits always in the tile; when the tile is narrower than the state
+  // at least one slot stays free, so every pass can take the next gate.
+  const int L = (K >= n) ? std::min(K, kTileLowQubits) : std::min(K - 1, kTileLowQubits);
   std::vector<const GateInstr*> remaining;
   for (auto& g : gates) remaining.push_back(&g);
   while (!remaining.empty()) {
@@ -219,6 +221,7 @@ std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int
         blockedAll |= Ag;
       }
     }
+    if (taken.empty()) fail(BF_EINVAL, "internal: tile planner made no progress (K=%d, n=%d)", K, n);
     double single_bytes = 0;
     for (const GateInstr* g : taken) single_bytes += gate_bytes_fraction(*g);
     if (single_bytes <= 2.0) {
@@ -239,6 +242,7 @@ std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int
       PlanStep st;
       st.is_tile = true;
       st.tile.K = nQ;
+      st.tile.L = L;
       int loc_of[64];
       for (int q = 0; q < 64; ++q) loc_of[q] = -1;
       int j = 0;

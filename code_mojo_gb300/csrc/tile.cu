@@ -116,8 +116,7 @@ __global__ void __launch_bounds__(kTileThreads) k_tile(typename P::Glob* __restr
 }
 
 template <class P>
-static size_t tile_smem_bytes(int K) {
-  int L = std::min(K, kTileLowQubits);
+static size_t tile_smem_bytes(int K, int L) {
   return ((size_t)1 << K) * sizeof(typename P::Smem) + ((size_t)1 << (K - L)) * sizeof(uint64_t);
 }
 
@@ -125,16 +124,17 @@ template <class P>
 static void launch_tile_p(State& st, const TileOp* d_ops, int nops, const TilePass& p) {
   TileGeom geo;
   geo.K = p.K;
-  geo.L = std::min(p.K, kTileLowQubits);
+  geo.L = p.L;
+  if (geo.L < 0 || geo.L > std::min(p.K, kTileLowQubits)) fail(BF_EINVAL, "internal: bad tile low width %d", geo.L);
   for (int j = 0; j < p.K; ++j) geo.q[j] = p.q[j];
   for (int j = 0; j < geo.L; ++j)
     if (geo.q[j] != j) fail(BF_EINVAL, "internal: tile qubits must start with 0..%d", geo.L - 1);
-  size_t smem = tile_smem_bytes<P>(p.K);
+  size_t smem = tile_smem_bytes<P>(p.K, geo.L);
   static int configured[3] = {0, 0, 0};
   int idx = st.prec;
   if (!configured[idx]) {
     BF_CUDA(cudaFuncSetAttribute(k_tile<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)tile_smem_bytes<P>(kMaxTileQubits)));
+                                 (int)tile_smem_bytes<P>(kMaxTileQubits, 0)));
     configured[idx] = 1;
   }
   uint64_t blocks = st.N >> p.K;

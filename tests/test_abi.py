@@ -122,13 +122,21 @@ def test_qft20_fuses_to_few_passes():
     assert unfused["bytes_in_S"] == pytest.approx(20 * 2 + 190 * 0.5 + 2)
 
 
-@pytest.mark.parametrize("K", [6, 8, 10, 11, 12, 13])
+@pytest.mark.parametrize("K", [1, 2, 3, 4, 5, 6, 8, 10, 11, 12, 13])
 def test_random_layered_pass_count_shrinks_with_width(K):
     qc = W.random_layered_circuit(30, 40, 0)
     s = stats(qc, K=K)
     total = s["tile_passes"] + s["gate_kernels"]
     assert 0 < total < 1800
     assert s["bytes_in_S"] < 3000
+
+
+@pytest.mark.parametrize("n,K", [(15, 5), (15, 1), (4, 13), (5, 5), (6, 5), (3, 2)])
+def test_planner_always_progresses(n, K):
+    qc = W.random_layered_circuit(n, 4, 1)
+    qc.transformations += W.qft_circuit(n).transformations
+    s = stats(qc, K=K)
+    assert s["tile_passes"] + s["gate_kernels"] > 0
 
 
 def test_wider_tiles_move_fewer_bytes():
