@@ -104,10 +104,11 @@ __device__ __forceinline__ dfl df_dot2(dfl a0, dfl b0, dfl a1, dfl b1) {
 }
 
 // FP64 bits -> (hi, lo).  hi keeps the leading 24 significant bits
-// (truncated), lo the next 23 (truncated): |x - hi - lo| < 2^-47 |x|.
-// |x| below 2^-126 is flushed to zero (absolute error < 1.2e-38); the lo part
-// of |x| below 2^-80 is dropped (absolute error < 2^-104).  Inf/NaN map to
-// NaN so that they stay visible.
+// (truncated); lo is the remaining 29 bits rounded to the nearest 23
+// (|x - hi - lo| <= 2^-47 |x|, unbiased, so errors do not drift over many
+// passes).  |x| below 2^-126 is flushed to zero (absolute error < 1.2e-38);
+// the lo part of |x| below 2^-80 is dropped (absolute error < 2^-103).
+// Inf/NaN map to NaN so that they stay visible.
 __device__ __forceinline__ dfl df_from_double(double x) {
   unsigned long long b = (unsigned long long)__double_as_longlong(x);
   unsigned hw = (unsigned)(b >> 32), lw = (unsigned)b;
@@ -127,7 +128,9 @@ __device__ __forceinline__ dfl df_from_double(double x) {
     return r;
   }
   r.hi = __int_as_float((int)(sign | ((unsigned)ef << 23) | mant23));
-  unsigned r23 = (lw & 0x1fffffffu) >> 6;
+  // rounded top 23 of the 29 remainder bits; a carry to 2^23 still decodes
+  // correctly below (0x4B800000 - 2^23 = 2^23)
+  unsigned r23 = ((lw & 0x1fffffffu) + 32u) >> 6;
   int es = e - 942;  // FP32 biased exponent of 2^(e - 1069)
   float lo = 0.f;
   if (es >= 1) {
@@ -138,31 +141,38 @@ __device__ __forceinline__ dfl df_from_double(double x) {
   return r;
 }
 
-// (hi, lo) -> FP64 bits, exact up to truncation of lo bits more than 29
-// places below hi's leading bit (relative error < 2^-52).
+// (hi, lo) -> FP64, rounded to nearest (ties away from zero) in integer
+// arithmetic: M = hi's 24-bit significand << 29 plus lo aligned to it.
 __device__ __forceinline__ double df_to_double(dfl v) {
   unsigned hb = (unsigned)__float_as_int(v.hi), lb = (unsigned)__float_as_int(v.lo);
   int eh = (int)((hb >> 23) & 0xffu);
   if (eh == 0) return 0.0;  // hi is zero (or FP32-subnormal): value below 2^-126
   if (eh == 0xff) return __longlong_as_double(0x7ff8000000000000ll);
-  long long M = (long long)((hb & 0x7fffffu) | 0x800000u) << 29;  // 53-bit
+  // 2 guard bits below the FP64 significand: M has 55 bits at scale 2^-2
+  long long M = (long long)((hb & 0x7fffffu) | 0x800000u) << 31;
   int el = (int)((lb >> 23) & 0xffu);
   if (el != 0) {
     long long ml = (long long)((lb & 0x7fffffu) | 0x800000u);
     int sh = eh - el;  // >= 0 for a normalised pair
     long long L;
-    if (sh <= 29) L = ml << (29 - sh);
-    else if (sh < 29 + 24) L = ml >> (sh - 29);
+    if (sh <= 31) L = ml << (31 - sh);
+    else if (sh < 31 + 25) L = (ml + (1ll << (sh - 32))) >> (sh - 31);
     else L = 0;
     if ((hb ^ lb) & 0x80000000u) M -= L; else M += L;
   }
-  int E = eh + 896;  // FP64 biased exponent for M in [2^52, 2^53)
-  if (M >= (1ll << 53)) {
+  int E = eh + 896;  // FP64 biased exponent for M in [2^54, 2^55)
+  int drop = 2;
+  if (M >= (1ll << 55)) {
+    drop = 3;
+    E += 1;
+  } else if (M < (1ll << 54)) {
+    drop = 1;
+    E -= 1;
+  }
+  M = (M + (1ll << (drop - 1))) >> drop;
+  if (M >= (1ll << 53)) {  // rounding carried into a new bit
     M >>= 1;
     E += 1;
-  } else if (M < (1ll << 52)) {
-    M <<= 1;
-    E -= 1;
   }
   unsigned long long bits = ((unsigned long long)(hb & 0x80000000u) << 32) |
                             ((unsigned long long)E << 52) |

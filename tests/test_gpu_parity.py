@@ -269,6 +269,25 @@ def test_cross_row_fusion_cases(second):
         assert maxdiff(run_gpu(qc, re, im, s), oracle(qc, re, im)) <= TOL128
 
 
+def test_double_float_round_trip_is_unbiased(monkeypatch):
+    """P(0) on every qubit, one pass per gate: each pass converts FP64 -> pair
+    -> FP64.  The error per element stays below 2^-46 relative and does not
+    drift in one direction (the conversions round, they do not truncate)."""
+    monkeypatch.delenv("BFGPU_C128_MATH", raising=False)
+    n = 14
+    re, im = W.random_normal_state(n, 12)
+    qc = bfy.QuantumCircuit(n)
+    for _ in range(20):
+        for q in range(n):
+            qc.p(q, 0.0)
+    got = run_gpu(qc, re, im, bfy.ExecutionStrategy.GPU)
+    z = re + 1j * im
+    rel = np.abs(got - z) / np.abs(z)
+    assert float(np.max(rel)) < 2.0 ** -40
+    bias = np.mean((got.real - z.real) / np.abs(z))
+    assert abs(bias) < 2.0 ** -50
+
+
 # ---- reductions, complex64, errors -------------------------------------------
 def test_norm2():
     n = 18
