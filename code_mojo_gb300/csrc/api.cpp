@@ -559,6 +559,10 @@ int bf_norm2(bf_state* hst, double* out) {
   });
 }
 
+int bf_norm2_noalloc(const void* d_amps, uint64_t num_amps, int32_t dtype, double* d_out, void* stream) {
+  return guarded([&]() { norm2_noalloc(d_amps, num_amps, dtype, d_out, static_cast<cudaStream_t>(stream)); });
+}
+
 // Host-only: validates and plans ops for a state of n qubits without a
 // device, reporting how many tile passes, per-gate kernels and other passes
 // bf_execute would launch and the algorithmic bytes they move (units of S).

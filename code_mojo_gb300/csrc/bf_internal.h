@@ -125,6 +125,8 @@ void launch_set_basis(State& s, uint64_t idx);
 void launch_interleave(State& s, const double* d_re, const double* d_im, uint64_t off, uint64_t cnt);
 void launch_deinterleave(State& s, double* d_re, double* d_im, uint64_t off, uint64_t cnt);
 double reduce_norm2(State& s);
+// sum |amp|^2 of caller memory with the library's static scratch (noalloc.cu)
+void norm2_noalloc(const void* d_amps, uint64_t num_amps, int32_t dtype, double* d_out, cudaStream_t stream);
 
 int tile_max_qubits(const State& s);
 

@@ -184,6 +184,23 @@ int bf_state_launch_count(const bf_state* st, uint64_t* launches, int32_t reset)
  * state's type). */
 int bf_norm2(bf_state* st, double* out);
 
+/* ---- sum |amp|^2 without allocating ---------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory: code running while its stream is captured into a CUDA graph, a
+ * plugin inside a host framework whose allocator owns all device memory, or a
+ * real-time path that cannot take cudaMalloc's implicit synchronisation.
+ * d_amps: num_amps interleaved amplitudes (dtype BF_C128 or BF_C64) in the
+ * caller's device memory; d_out: one double in the caller's device memory,
+ * written with sum |amp|^2 (double-float accumulation), stream-ordered on
+ * `stream` (a cudaStream_t; NULL = the default stream).  Nothing is
+ * allocated: the partial sums use a 512 KiB array built into the library
+ * (held by every GPU that loads it), which limits num_amps to 2^31; larger
+ * inputs are rejected with BF_EINVAL.  The first call on a device resolves
+ * that array's address; make it before capturing a stream.  All calls share
+ * the array, so calls that overlap on the GPU race: serialise them. */
+int bf_norm2_noalloc(const void* d_amps, uint64_t num_amps, int32_t dtype,
+                     double* d_out, void* stream);
+
 /* ---- host-only entry points (no device needed) --------------------------- */
 /* validate_circuit (butterfly/core/executors.mojo:129-185) for a state of
  * num_qubits qubits. */
