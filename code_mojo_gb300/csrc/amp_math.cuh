@@ -186,6 +186,7 @@ __device__ __forceinline__ double df_to_double(dfl v) {
 struct PolF64 {
   using Glob = double2;
   using Smem = double2;
+  using E = double;
   struct R {
     double re, im;
   };
@@ -234,8 +235,8 @@ struct PolF64 {
     return R{acc.re + (a.re * b.re - a.im * b.im), acc.im + (a.re * b.im + a.im * b.re)};
   }
   // multiply by the complex coefficient (v[k], v[k+1])
-  __device__ static __forceinline__ void cmul(R& x, const Coef& g, int k) {
-    double c = g.v[k], s = g.v[k + 1];
+  __device__ static __forceinline__ void cmul(R& x, const Coef& g, int k) { cmul_by(x, g.v[k], g.v[k + 1]); }
+  __device__ static __forceinline__ void cmul_by(R& x, E c, E s) {
     R a = x;
     x.re = a.re * c - a.im * s;
     x.im = a.re * s + a.im * c;
@@ -245,6 +246,7 @@ struct PolF64 {
 struct PolDF {
   using Glob = double2;
   using Smem = float4;  // (re.hi, re.lo, im.hi, im.lo)
+  using E = dfl;
   struct R {
     dfl re, im;
   };
@@ -300,8 +302,8 @@ struct PolDF {
     return R{df_add(acc.re, df_dot2(a.re, b.re, df_neg(a.im), b.im)),
              df_add(acc.im, df_dot2(a.re, b.im, a.im, b.re))};
   }
-  __device__ static __forceinline__ void cmul(R& x, const Coef& g, int k) {
-    dfl c = g.v[k], s = g.v[k + 1];
+  __device__ static __forceinline__ void cmul(R& x, const Coef& g, int k) { cmul_by(x, g.v[k], g.v[k + 1]); }
+  __device__ static __forceinline__ void cmul_by(R& x, E c, E s) {
     R a = x;
     x.re = df_dot2(a.re, c, df_neg(a.im), s);
     x.im = df_dot2(a.re, s, a.im, c);
@@ -311,6 +313,7 @@ struct PolDF {
 struct PolF32 {
   using Glob = float2;
   using Smem = float2;
+  using E = float;
   struct R {
     float re, im;
   };
@@ -357,8 +360,8 @@ struct PolF32 {
   __device__ static __forceinline__ R fma(R a, R b, R acc) {
     return R{acc.re + (a.re * b.re - a.im * b.im), acc.im + (a.re * b.im + a.im * b.re)};
   }
-  __device__ static __forceinline__ void cmul(R& x, const Coef& g, int k) {
-    float c = g.v[k], s = g.v[k + 1];
+  __device__ static __forceinline__ void cmul(R& x, const Coef& g, int k) { cmul_by(x, g.v[k], g.v[k + 1]); }
+  __device__ static __forceinline__ void cmul_by(R& x, E c, E s) {
     R a = x;
     x.re = a.re * c - a.im * s;
     x.im = a.re * s + a.im * c;
