@@ -241,6 +241,18 @@ class ClassicalTransformation:
         self.targets = list(targets)
 
 
+class MeasurementTransformation:
+    """MeasurementTransformation (circuit.mojo:200-227): apply_measure on
+    `targets`; values[k] None = free, True/False = post-selected."""
+
+    def __init__(self, targets: Sequence[int], values=None, seed: Optional[int] = None):
+        self.targets = list(targets)
+        self.values = list(values) if values else [None] * len(self.targets)
+        if len(self.values) != len(self.targets):
+            raise ValueError("Measurement values length mismatch")
+        self.seed = seed
+
+
 class Register:
     def __init__(self, name: str, length: int, start: int = 0):
         self.name, self.length, self.start = name, length, start
@@ -352,6 +364,13 @@ class QuantumCircuit:
                 ops.append(_unitary_op(F.BF_OP_UNITARY, tr.u, tr.target, tr.m, None, keep))
             elif isinstance(tr, ControlledUnitaryTransformation):
                 ops.append(_unitary_op(F.BF_OP_CUNITARY, tr.u, tr.target, tr.m, tr.control, keep))
+            elif isinstance(tr, MeasurementTransformation):
+                vals = np.array([-1.0 if v is None else float(bool(v)) for v in tr.values], dtype=np.float64)
+                keep.append(vals)
+                o = _list_op(F.BF_OP_MEASURE, tr.targets, keep)
+                o.data = vals.ctypes.data_as(C.POINTER(C.c_double))
+                o.arg = float(-1 if tr.seed is None else tr.seed)
+                ops.append(o)
             elif isinstance(tr, ClassicalTransformation):
                 if tr.name == "BITREV":
                     ops.append(_list_op(F.BF_OP_BITREV, tr.targets, keep))
@@ -419,6 +438,8 @@ def _invert_gate(gt: GateTransformation) -> GateTransformation:
 
 
 def _invert(tr):
+    if isinstance(tr, MeasurementTransformation):
+        raise ValueError("Cannot invert circuit containing measurements")
     if isinstance(tr, GateTransformation):
         return _invert_gate(tr)
     if isinstance(tr, FusedPairTransformation):
@@ -445,6 +466,11 @@ def bit_reverse(circuit: QuantumCircuit, targets: Optional[Sequence[int]] = None
 
 def permute_qubits(circuit: QuantumCircuit, order: Sequence[int]) -> None:
     circuit.transformations.append(ClassicalTransformation("PERMUTE", list(order)))
+
+
+def measure(circuit: QuantumCircuit, targets: Sequence[int], values=None, seed: Optional[int] = None) -> None:
+    """quantum_circuit.mojo:139-182."""
+    circuit.transformations.append(MeasurementTransformation(targets, values, seed))
 
 
 def swap_tr(a: int, b: int) -> ClassicalTransformation:
@@ -520,6 +546,39 @@ class QuantumState:
 
     def sync(self) -> None:
         F.check(F.lib().bf_state_sync(self.handle))
+
+    @staticmethod
+    def _values(values, n):
+        if values is None:
+            return None
+        arr = (C.c_int8 * max(1, n))(*[(-1 if v is None else int(bool(v))) for v in values])
+        return arr
+
+    def probabilities(self, qubits: Sequence[int], values=None) -> np.ndarray:
+        """Outcome probabilities of the free qubits among `qubits` (bit j of
+        the outcome index = j-th free qubit); values fix the others."""
+        q = (C.c_int32 * max(1, len(qubits)))(*qubits)
+        v = self._values(values, len(qubits))
+        nfree = len(qubits) if values is None else sum(1 for x in values if x is None)
+        out = np.empty(1 << nfree, dtype=np.float64)
+        F.check(F.lib().bf_probabilities(self.handle, q, v, len(qubits), out.ctypes.data))
+        return out
+
+    def measure(self, targets: Sequence[int], values=None, seed: Optional[int] = None) -> tuple[int, float]:
+        """apply_measure (state.mojo:447-553): returns (outcome, probability)
+        and collapses the state."""
+        q = (C.c_int32 * max(1, len(targets)))(*targets)
+        v = self._values(values, len(targets))
+        oc, pr = C.c_uint64(), C.c_double()
+        F.check(F.lib().bf_measure(self.handle, q, v, len(targets), -1 if seed is None else int(seed), C.byref(oc),
+                                   C.byref(pr)))
+        return oc.value, pr.value
+
+    def topk(self, k: int = 16) -> tuple[np.ndarray, np.ndarray]:
+        idx = np.empty(k, dtype=np.uint64)
+        pr = np.empty(k, dtype=np.float64)
+        F.check(F.lib().bf_probs_topk(self.handle, k, idx.ctypes.data, pr.ctypes.data))
+        return idx, pr
 
     def stream_ptr(self) -> int:
         p = C.c_void_p()

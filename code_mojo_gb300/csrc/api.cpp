@@ -74,7 +74,7 @@ static void upload_program(State& st, const std::vector<TileOp>& prog) {
 // ---- execution -------------------------------------------------------------
 // A step is one launch (or a launch group) in op order.
 struct Step {
-  enum Kind { GATE, TILE, BITREV, PERMUTE, SWAPBITS, UNITARY } kind;
+  enum Kind { GATE, TILE, BITREV, PERMUTE, SWAPBITS, UNITARY, MEASURE } kind;
   GateInstr gate;
   TilePass tile;            // ops moved into the program; tile.ops emptied
   size_t prog_off = 0;
@@ -83,6 +83,9 @@ struct Step {
   int a = 0, b = 0;
   std::vector<double> u;
   int ut = 0, um = 0, uc = -1;
+  std::vector<int32_t> mq;   // measured qubits
+  std::vector<int8_t> mv;    // their values (-1 free)
+  int64_t seed = -1;
 };
 
 static bool is_h(const bf_op& o) { return o.ncontrols == 0 && o.gate == BF_GATE_H; }
@@ -310,6 +313,16 @@ static void build_steps(int n, const bf_op* ops, int64_t nops, const bf_exec_opt
         emit_perm(src_of);
         break;
       }
+      case BF_OP_MEASURE: {  // MeasurementTransformation -> apply_measure (state.mojo:447-553)
+        flush();
+        Step s;
+        s.kind = Step::MEASURE;
+        s.mq.assign(op.qubits, op.qubits + op.nqubits);
+        for (int64_t k = 0; k < op.nqubits; ++k) s.mv.push_back(op.data ? (int8_t)op.data[k] : (int8_t)-1);
+        s.seed = (int64_t)op.arg;
+        steps.push_back(std::move(s));
+        break;
+      }
       case BF_OP_UNITARY:
         emit_unitary(op.data, op.target, op.target2, -1);
         break;
@@ -333,6 +346,9 @@ static void run_steps(State& st, std::vector<Step>& steps, const std::vector<Til
       case Step::PERMUTE: launch_permute(st, s.src_of.data()); break;
       case Step::SWAPBITS: launch_swap_bits(st, s.a, s.b); break;
       case Step::UNITARY: launch_unitary(st, s.u.data(), s.ut, s.um, s.uc); break;
+      case Step::MEASURE:
+        measure(st, s.mq.data(), s.mv.data(), (int32_t)s.mq.size(), s.seed, nullptr, nullptr);
+        break;
     }
   }
 }
@@ -556,6 +572,33 @@ int bf_norm2(bf_state* hst, double* out) {
   return guarded([&]() {
     if (!st || !out) fail(BF_EINVAL, "null argument");
     *out = reduce_norm2(*st);
+  });
+}
+
+int bf_probabilities(bf_state* hst, const int32_t* qubits, const int8_t* values, int32_t nq, double* out) {
+  State* st = S_(hst);
+  return guarded([&]() {
+    if (!st || !out) fail(BF_EINVAL, "null argument");
+    std::vector<double> p;
+    marginal_probs(*st, qubits, values, nq, p);
+    std::memcpy(out, p.data(), p.size() * sizeof(double));
+  });
+}
+
+int bf_measure(bf_state* hst, const int32_t* targets, const int8_t* values, int32_t ntargets, int64_t seed,
+               uint64_t* outcome, double* probability) {
+  State* st = S_(hst);
+  return guarded([&]() {
+    if (!st) fail(BF_EINVAL, "state is null");
+    measure(*st, targets, values, ntargets, seed, outcome, probability);
+  });
+}
+
+int bf_probs_topk(bf_state* hst, int32_t k, uint64_t* indices, double* probs) {
+  State* st = S_(hst);
+  return guarded([&]() {
+    if (!st || !indices || !probs) fail(BF_EINVAL, "null argument");
+    probs_topk(*st, k, indices, probs);
   });
 }
 

@@ -77,6 +77,18 @@ void validate_ops(int n, const bf_op* ops, int64_t nops) {
         }
         break;
       }
+      case BF_OP_MEASURE: {
+        if (o.nqubits < 0 || (o.nqubits > 0 && o.qubits == nullptr)) fail(BF_EINVAL, "qubit list is null");
+        uint64_t seen = 0;
+        for (int64_t k = 0; k < o.nqubits; ++k) {
+          check_qubit(o.qubits[k], n, "Target");
+          if ((seen >> o.qubits[k]) & 1) fail(BF_EINVAL, "Duplicate target: %d", o.qubits[k]);
+          seen |= 1ull << o.qubits[k];
+          if (o.data && !(o.data[k] == -1.0 || o.data[k] == 0.0 || o.data[k] == 1.0))
+            fail(BF_EINVAL, "Measurement values must be -1 (free), 0 or 1");
+        }
+        break;
+      }
       case BF_OP_UNITARY:
       case BF_OP_CUNITARY: {
         int m = o.target2;

@@ -98,11 +98,11 @@ __global__ void __launch_bounds__(kTileThreads) k_tile(typename P::Glob* __restr
       const int tg = __ldg(&op->tglob);
       const int bit = (int)((obase >> tg) & 1);
       if (kind == GK_PHASE && bit == 0) continue;  // CTA-uniform
-      const int ci = bit ? 6 : 0;
+      const typename P::E c = bit ? g.v[6] : g.v[0], sn = bit ? g.v[7] : g.v[1];
       for (int e = tid; e < TS; e += kTileThreads) {
         if ((e & cml) != cml) continue;
         R x = P::from_smem(amp[e]);
-        P::cmul(x, g, ci);
+        P::cmul_by(x, c, sn);
         amp[e] = P::to_smem(x);
       }
     }

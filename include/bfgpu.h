@@ -77,7 +77,10 @@ enum {
   BF_OP_CUNITARY = 4,  /* ControlledUnitaryTransformation(u, control, target, m) */
   BF_OP_BITREV = 5,    /* classical bit_reverse_tr(targets; none = all)      */
   BF_OP_PERMUTE = 6,   /* classical permute_qubits_tr(order)                 */
-  BF_OP_CSWAP = 7      /* classical swap_tr(a, b) (apply_swap)               */
+  BF_OP_CSWAP = 7,     /* classical swap_tr(a, b) (apply_swap)               */
+  BF_OP_MEASURE = 8    /* MeasurementTransformation (apply_measure): qubits =
+                          targets, data = per-target values as doubles (-1 free,
+                          0, 1) or NULL (all free), arg = seed (< 0: clock)   */
 };
 
 /* bf_op.flags */
@@ -183,6 +186,26 @@ int bf_state_launch_count(const bf_state* st, uint64_t* launches, int32_t reset)
 /* sum |amp|^2, accumulated in FP64 (state.mojo:482-501 accumulates in the
  * state's type). */
 int bf_norm2(bf_state* st, double* out);
+
+/* ---- measurement and readout (apply_measure, state.mojo:447-553) ---------- */
+/* Outcome probabilities over `qubits`: values[k] = 0 or 1 restricts to
+ * amplitudes whose qubit k reads that value, -1 leaves it free (values may be
+ * NULL: all free).  out[o] for the 2^f outcomes of the f free qubits, bit j of
+ * o = the j-th free qubit in list order; f <= 20.  Blocks. */
+int bf_probabilities(bf_state* st, const int32_t* qubits, const int8_t* values,
+                     int32_t nqubits, double* out);
+/* apply_measure: draws an outcome of the free targets with the reference's
+ * generator (seed mod 2^31-1, times 48271 mod 2^31-1, scaled by the total
+ * probability; a negative seed draws from the clock), collapses the state
+ * onto it and renormalises by 1/sqrt(p).  Returns the outcome (bit j = j-th
+ * free target) and its probability p.  Errors as the reference:
+ * "Measurement probability is zero".  Blocks. */
+int bf_measure(bf_state* st, const int32_t* targets, const int8_t* values,
+               int32_t ntargets, int64_t seed, uint64_t* outcome,
+               double* probability);
+/* The k (1..64) most probable basis states, by descending |amp|^2, ties by
+ * ascending index.  Blocks. */
+int bf_probs_topk(bf_state* st, int32_t k, uint64_t* indices, double* probs);
 
 /* ---- sum |amp|^2 without allocating ---------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device

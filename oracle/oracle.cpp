@@ -566,6 +566,9 @@ void validate(const St& s, const bf_op* ops, int64_t nops) {
       case BF_OP_PERMUTE:
         for (int64_t k = 0; k < o.nqubits; ++k) check_qubit(o.qubits[k], n, "Target");
         break;
+      case BF_OP_MEASURE:
+        for (int64_t k = 0; k < o.nqubits; ++k) check_qubit(o.qubits[k], n, "Target");
+        break;
       case BF_OP_UNITARY:
       case BF_OP_CUNITARY: {
         int m = o.target2;
@@ -800,6 +803,79 @@ int or_qft_classical(int32_t n, double* re, double* im, const int32_t* targets,
     set_err(err, errlen, e.msg);
     return e.code;
   }
+}
+
+// apply_measure (state.mojo:447-553), the sequential loops as written.
+// values[k]: -1 free, 0/1 fixed.  Returns the chosen outcome and its
+// probability; collapses (re, im) in place.
+int or_measure(int32_t n, double* re, double* im, const int32_t* targets, const int8_t* values,
+               int32_t nt, int64_t seed, uint64_t* outcome, double* prob, char* err, size_t errlen) {
+  try {
+    size_t N = (size_t)1 << n;
+    for (int j = 0; j < nt; ++j)
+      if (targets[j] < 0 || targets[j] >= n) fail(BF_EINVAL, "Target out of bounds: %d", targets[j]);
+    std::vector<int> free_t, free_pos(nt);
+    for (int j = 0; j < nt; ++j) {
+      if (values && values[j] >= 0) free_pos[j] = -1;
+      else { free_pos[j] = (int)free_t.size(); free_t.push_back(targets[j]); }
+    }
+    size_t oc = (size_t)1 << free_t.size();
+    std::vector<double> op(oc, 0.0);
+    double total = 0;
+    for (size_t i = 0; i < N; ++i) {
+      bool match = true;
+      for (int j = 0; j < nt; ++j)
+        if (values && values[j] >= 0 && (int)((i >> targets[j]) & 1) != values[j]) { match = false; break; }
+      if (!match) continue;
+      size_t o = 0;
+      for (size_t k = 0; k < free_t.size(); ++k)
+        if ((i >> free_t[k]) & 1) o |= (size_t)1 << k;
+      double p = re[i] * re[i] + im[i] * im[i];
+      op[o] = op[o] + p;
+      total += p;
+    }
+    if (total <= 0) fail(BF_EINVAL, "Measurement probability is zero");
+    int64_t rng = seed % 2147483647;
+    rng = (rng * 48271) % 2147483647;
+    double r = (double)rng / (double)2147483647 * total;
+    size_t chosen = 0;
+    double acc = 0;
+    for (size_t i = 0; i < oc; ++i) {
+      acc += op[i];
+      if (r <= acc) { chosen = i; break; }
+    }
+    double cp = op[chosen];
+    if (cp <= 0) fail(BF_EINVAL, "Measurement outcome probability is zero");
+    double inv = 1.0 / sqrt(cp);
+    for (size_t i = 0; i < N; ++i) {
+      bool match = true;
+      for (int j = 0; j < nt; ++j) {
+        int bit = (int)((i >> targets[j]) & 1);
+        int want = (values && values[j] >= 0) ? values[j] : (int)((chosen >> free_pos[j]) & 1);
+        if (bit != want) { match = false; break; }
+      }
+      if (match) { re[i] = re[i] * inv; im[i] = im[i] * inv; }
+      else { re[i] = 0.0; im[i] = 0.0; }
+    }
+    if (outcome) *outcome = chosen;
+    if (prob) *prob = cp;
+    return BF_OK;
+  } catch (const OrError& e) {
+    set_err(err, errlen, e.msg);
+    return e.code;
+  }
+}
+
+// The k most probable indices, by descending re^2 + im^2, ties by index.
+void or_topk(int32_t n, const double* re, const double* im, int32_t k, uint64_t* idx, double* prob) {
+  size_t N = (size_t)1 << n;
+  std::vector<std::pair<double, uint64_t>> v(N);
+  for (size_t i = 0; i < N; ++i) v[i] = {re[i] * re[i] + im[i] * im[i], i};
+  std::partial_sort(v.begin(), v.begin() + k, v.end(), [](const auto& a, const auto& b) {
+    if (a.first != b.first) return a.first > b.first;
+    return a.second < b.second;
+  });
+  for (int i = 0; i < k; ++i) { idx[i] = v[i].second; prob[i] = v[i].first; }
 }
 
 void or_bit_reverse_indices(int32_t n, uint64_t* out_index) {

@@ -54,6 +54,15 @@ int or_qft_classical(int32_t n, double* re, double* im, const int32_t* targets,
  * out_index[i] = rev_n(i).  Used to check permutations bit-exactly. */
 void or_bit_reverse_indices(int32_t n, uint64_t* out_index);
 
+/* apply_measure (state.mojo:447-553): values[k] -1 = free, 0/1 = fixed. */
+int or_measure(int32_t n, double* re, double* im, const int32_t* targets,
+               const int8_t* values, int32_t ntargets, int64_t seed,
+               uint64_t* outcome, double* prob, char* err, size_t errlen);
+
+/* The k most probable basis states (descending probability, ties by index). */
+void or_topk(int32_t n, const double* re, const double* im, int32_t k,
+             uint64_t* idx, double* prob);
+
 /* sum |amp|^2 in FP64. */
 double or_norm2(int32_t n, const double* re, const double* im);
 

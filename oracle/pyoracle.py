@@ -38,6 +38,11 @@ def lib() -> C.CDLL:
         L.or_bit_reverse_indices.restype = None
         L.or_norm2.argtypes = [C.c_int32, C.c_void_p, C.c_void_p]
         L.or_norm2.restype = C.c_double
+        L.or_measure.argtypes = [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int64,
+                                 C.POINTER(C.c_uint64), C.POINTER(C.c_double), C.c_char_p, C.c_size_t]
+        L.or_measure.restype = C.c_int
+        L.or_topk.argtypes = [C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]
+        L.or_topk.restype = None
         L.or_num_cores.argtypes = []
         L.or_num_cores.restype = C.c_int32
         _lib = L
@@ -96,6 +101,33 @@ def qft_classical(re, im, targets=(), inverse=False, swap=False):
     if rc != 0:
         raise OracleError(rc, err.value.decode())
     return re, im
+
+
+def measure(re, im, targets, values=None, seed=0):
+    """apply_measure on copies: returns (outcome, prob, re, im)."""
+    re = np.array(re, dtype=np.float64, copy=True)
+    im = np.array(im, dtype=np.float64, copy=True)
+    n = int(re.size).bit_length() - 1
+    t = (C.c_int32 * max(1, len(targets)))(*targets)
+    v = None
+    if values is not None:
+        v = (C.c_int8 * max(1, len(values)))(*[(-1 if x is None else int(x)) for x in values])
+    oc, pr = C.c_uint64(), C.c_double()
+    err = C.create_string_buffer(512)
+    rc = lib().or_measure(n, re.ctypes.data, im.ctypes.data, t, v, len(targets), seed, C.byref(oc), C.byref(pr),
+                          err, len(err))
+    if rc != 0:
+        raise OracleError(rc, err.value.decode())
+    return oc.value, pr.value, re, im
+
+
+def topk(re, im, k):
+    n = int(re.size).bit_length() - 1
+    idx = np.empty(k, dtype=np.uint64)
+    pr = np.empty(k, dtype=np.float64)
+    lib().or_topk(n, np.ascontiguousarray(re).ctypes.data, np.ascontiguousarray(im).ctypes.data, k, idx.ctypes.data,
+                  pr.ctypes.data)
+    return idx, pr
 
 
 def bit_reverse_indices(n: int) -> np.ndarray:

@@ -360,3 +360,77 @@ def test_random_layered_30q_round_trip():
     re[0] = 0.0
     assert float(np.max(np.abs(re))) <= 1e-12 and float(np.max(np.abs(im))) <= 1e-12
     st.close()
+
+
+# ---- measurement and readout (apply_measure, state.mojo:447-553) --------------
+@pytest.mark.parametrize("dtype", ["c128", "c64"])
+@pytest.mark.parametrize("qubits,values", [([0, 1, 2], None), ([13, 2, 7], None), ([5], None),
+                                           ([3, 9, 11, 0], [None, 1, None, 0]), ([], None),
+                                           (list(range(12)), None)])
+def test_probabilities(dtype, qubits, values):
+    n = 14
+    re, im = W.random_normal_state(n, 31)
+    st = bfy.QuantumState.from_soa(re, im, dtype)
+    got = st.probabilities(qubits, values)
+    st.close()
+    p = re ** 2 + im ** 2
+    idx = np.arange(1 << n)
+    free = [q for k, q in enumerate(qubits) if values is None or values[k] is None]
+    mask = np.ones(1 << n, dtype=bool)
+    for k, q in enumerate(qubits):
+        if values is not None and values[k] is not None:
+            mask &= ((idx >> q) & 1) == values[k]
+    outcome = np.zeros(1 << n, dtype=np.int64)
+    for j, q in enumerate(free):
+        outcome |= ((idx >> q) & 1) << j
+    exp = np.bincount(outcome[mask], weights=p[mask], minlength=1 << len(free))
+    tol = 1e-14 if dtype == "c128" else 1e-6
+    assert np.max(np.abs(got - exp)) <= tol
+
+
+@pytest.mark.parametrize("targets,values", [([0, 3, 7], None), ([12, 1], [None, True]), (list(range(15)), None),
+                                            ([4], None)])
+@pytest.mark.parametrize("seed", [1, 77, 2 ** 33 + 5])
+def test_measure_matches_oracle(targets, values, seed, c128_math):
+    n = 15
+    re, im = W.random_normal_state(n, 5)
+    st = bfy.QuantumState.from_soa(re, im)
+    oc, pr = st.measure(targets, values, seed)
+    got = st.to_complex()
+    st.close()
+    eo, ep, er, ei = O.measure(re, im, targets, values, seed)
+    assert oc == eo
+    assert abs(pr - ep) <= 1e-14
+    assert maxdiff(got, er + 1j * ei) <= TOL128
+
+
+def test_measure_inside_a_circuit():
+    n = 12
+    qc = W.random_layered_circuit(n, 3, seed=8)
+    bfy.measure(qc, [2, 5, 9], seed=1234)
+    qc.transformations += W.random_layered_circuit(n, 2, seed=9).transformations
+    bfy.measure(qc, [0, 11], [None, False], seed=99)
+    re, im = O.basis(n)
+    for s in STRATS:
+        assert maxdiff(run_gpu(qc, re, im, s), oracle(qc, re, im)) <= TOL128
+
+
+def test_measure_zero_probability_raises():
+    st = bfy.QuantumState(6)
+    with pytest.raises(F.BFError, match="Measurement probability is zero"):
+        st.measure([1], [True], 3)
+    st.close()
+
+
+@pytest.mark.parametrize("n,k", [(10, 16), (17, 16), (20, 64), (5, 3)])
+@pytest.mark.parametrize("dtype", ["c128", "c64"])
+def test_topk(n, k, dtype):
+    re, im = W.random_normal_state(n, 40 + n)
+    st = bfy.QuantumState.from_soa(re, im, dtype)
+    idx, pr = st.topk(k)
+    st.close()
+    if dtype == "c64":
+        re, im = re.astype(np.float32).astype(np.float64), im.astype(np.float32).astype(np.float64)
+    ei, ep = O.topk(re, im, k)
+    assert idx.tolist() == ei.tolist()
+    assert np.max(np.abs(pr - ep)) <= (1e-15 if dtype == "c128" else 1e-12)

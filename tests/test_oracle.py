@@ -248,3 +248,35 @@ def test_oracle_validation_messages(build, msg):
     build(qc)
     with pytest.raises(O.OracleError, match=msg):
         O.run(qc, *O.basis(4))
+
+
+# ---- apply_measure (state.mojo:447-553) ---------------------------------------
+def test_measure_draw_follows_the_reference_generator():
+    n = 6
+    re, im = W.random_normal_state(n, 21)
+    p = re ** 2 + im ** 2
+    for seed in (1, 7, 12345, 2 ** 40 + 3):
+        oc, pr, r2, i2 = O.measure(re, im, [0, 1, 2, 3, 4, 5], None, seed)
+        rng = (seed % 2147483647) * 48271 % 2147483647
+        r = rng / 2147483647 * p.sum()
+        assert oc == int(np.searchsorted(np.cumsum(p), r))
+        assert abs(pr - p[oc]) < 1e-15
+        assert abs(r2[oc] ** 2 + i2[oc] ** 2 - 1) < 1e-12
+
+
+def test_measure_subset_and_postselection():
+    n = 5
+    re, im = W.random_normal_state(n, 22)
+    oc, pr, r2, i2 = O.measure(re, im, [3, 1], [None, True], 99)
+    z = r2 + 1j * i2
+    assert abs(np.sum(np.abs(z) ** 2) - 1) < 1e-12
+    idx = np.arange(1 << n)
+    assert np.all(z[((idx >> 1) & 1) == 0] == 0)
+    assert np.all(z[((idx >> 3) & 1) != oc] == 0)
+
+
+def test_topk_orders_by_probability_then_index():
+    re = np.array([0.1, 0.5, 0.5, 0.2, 0.0, 0.3, 0.5, 0.1])
+    im = np.zeros(8)
+    idx, pr = O.topk(re, im, 4)
+    assert idx.tolist() == [1, 2, 6, 5]
