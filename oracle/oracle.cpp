@@ -670,6 +670,15 @@ void run(St& s, const Ctx& c, const bf_op* ops, int64_t nops, bool do_validate) 
       case BF_OP_CSWAP:  // apply_swap (:434-444)
         swap_bits(s, o.target, o.target2);
         break;
+      case BF_OP_MEASURE: {  // MeasurementTransformation -> apply_measure (:447-553)
+        std::vector<int8_t> v;
+        for (int64_t k = 0; k < o.nqubits; ++k) v.push_back(o.data ? (int8_t)o.data[k] : (int8_t)-1);
+        char err[512];
+        int rc = or_measure(s.n, s.re, s.im, o.qubits, v.data(), (int32_t)o.nqubits, (int64_t)o.arg, nullptr,
+                            nullptr, err, sizeof err);
+        if (rc != 0) fail(rc, "%s", err);
+        break;
+      }
       default:
         fail(BF_EINVAL, "Unknown transformation type: %d", o.kind);
     }

@@ -280,3 +280,16 @@ def test_topk_orders_by_probability_then_index():
     im = np.zeros(8)
     idx, pr = O.topk(re, im, 4)
     assert idx.tolist() == [1, 2, 6, 5]
+
+
+def test_measure_op_inside_a_circuit_runs_on_the_oracle():
+    n = 6
+    qc = W.random_layered_circuit(n, 2, seed=3)
+    bfy.measure(qc, [1, 4], seed=5)
+    re, im = O.basis(n)
+    r, i = O.run(qc, re, im)
+    z = r + 1j * i
+    assert abs(np.sum(np.abs(z) ** 2) - 1) < 1e-12
+    idx = np.arange(1 << n)
+    nz = idx[np.abs(z) > 0]
+    assert len(set(((nz >> 1) & 1).tolist())) == 1 and len(set(((nz >> 4) & 1).tolist())) == 1
