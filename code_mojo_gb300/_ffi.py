@@ -20,7 +20,7 @@ BF_C128, BF_C64 = 0, 1
 BF_GATE_H, BF_GATE_P, BF_GATE_X, BF_GATE_Y, BF_GATE_Z, BF_GATE_RX, BF_GATE_RY, BF_GATE_RZ, BF_GATE_CUSTOM = range(9)
 # op kinds
 (BF_OP_GATE, BF_OP_SWAP, BF_OP_QREV, BF_OP_UNITARY, BF_OP_CUNITARY, BF_OP_BITREV, BF_OP_PERMUTE,
- BF_OP_CSWAP, BF_OP_MEASURE) = range(9)
+ BF_OP_CSWAP, BF_OP_MEASURE, BF_OP_GROVER_DIFFUSER, BF_OP_GROVER_INVERSION0) = range(11)
 BF_OPF_FUSE_WITH_NEXT = 1
 BF_STRATEGY_GPU, BF_STRATEGY_GPU_FUSED = 8, 9
 BF_SPEC_ALL = 127

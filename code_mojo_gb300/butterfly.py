@@ -232,10 +232,11 @@ class ControlledUnitaryTransformation:
 
 class ClassicalTransformation:
     """The classical transforms on the hot path: BITREV, PERMUTE and SWAP
-    (quantum_circuit.mojo:99-123)."""
+    (quantum_circuit.mojo:99-123) and the Grover diffuser / inversion about
+    |0> (grover_classical.mojo:262-326)."""
 
     def __init__(self, name: str, targets: Sequence[int]):
-        if name not in ("BITREV", "PERMUTE", "SWAP"):
+        if name not in ("BITREV", "PERMUTE", "SWAP", "GROVER_DIFFUSER", "GROVER_INVERSION_0"):
             raise ValueError(f"unsupported classical transform {name}")
         self.name = name
         self.targets = list(targets)
@@ -376,6 +377,10 @@ class QuantumCircuit:
                     ops.append(_list_op(F.BF_OP_BITREV, tr.targets, keep))
                 elif tr.name == "PERMUTE":
                     ops.append(_list_op(F.BF_OP_PERMUTE, tr.targets, keep))
+                elif tr.name == "GROVER_DIFFUSER":
+                    ops.append(_list_op(F.BF_OP_GROVER_DIFFUSER, tr.targets, keep))
+                elif tr.name == "GROVER_INVERSION_0":
+                    ops.append(_list_op(F.BF_OP_GROVER_INVERSION0, tr.targets, keep))
                 else:
                     if len(tr.targets) != 2:
                         raise ValueError("SWAP expects 2 targets")
@@ -471,6 +476,18 @@ def permute_qubits(circuit: QuantumCircuit, order: Sequence[int]) -> None:
 def measure(circuit: QuantumCircuit, targets: Sequence[int], values=None, seed: Optional[int] = None) -> None:
     """quantum_circuit.mojo:139-182."""
     circuit.transformations.append(MeasurementTransformation(targets, values, seed))
+
+
+def grover_diffuser(circuit: QuantumCircuit, targets: Optional[Sequence[int]] = None) -> None:
+    """Classical inversion about the mean over `targets` (all when empty),
+    apply_grover_diffuser (grover_classical.mojo:284-326), computed as
+    2*mean - x for both real and imaginary parts."""
+    circuit.transformations.append(ClassicalTransformation("GROVER_DIFFUSER", list(targets or [])))
+
+
+def grover_inversion_0(circuit: QuantumCircuit, targets: Optional[Sequence[int]] = None) -> None:
+    """Classical phase flip of |0...0> on `targets` (grover_classical.mojo:262-281)."""
+    circuit.transformations.append(ClassicalTransformation("GROVER_INVERSION_0", list(targets or [])))
 
 
 def swap_tr(a: int, b: int) -> ClassicalTransformation:

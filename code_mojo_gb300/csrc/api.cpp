@@ -74,7 +74,7 @@ static void upload_program(State& st, const std::vector<TileOp>& prog) {
 // ---- execution -------------------------------------------------------------
 // A step is one launch (or a launch group) in op order.
 struct Step {
-  enum Kind { GATE, TILE, BITREV, PERMUTE, SWAPBITS, UNITARY, MEASURE } kind;
+  enum Kind { GATE, TILE, BITREV, PERMUTE, SWAPBITS, UNITARY, MEASURE, DIFFUSER, INVERSION0 } kind;
   GateInstr gate;
   TilePass tile;            // ops moved into the program; tile.ops emptied
   size_t prog_off = 0;
@@ -323,6 +323,15 @@ static void build_steps(int n, const bf_op* ops, int64_t nops, const bf_exec_opt
         steps.push_back(std::move(s));
         break;
       }
+      case BF_OP_GROVER_DIFFUSER:     // apply_grover_diffuser (grover_classical.mojo:284-326)
+      case BF_OP_GROVER_INVERSION0: {  // apply_grover_inversion_0 (grover_classical.mojo:262-281)
+        flush();
+        Step s;
+        s.kind = op.kind == BF_OP_GROVER_DIFFUSER ? Step::DIFFUSER : Step::INVERSION0;
+        s.mq.assign(op.qubits, op.qubits + op.nqubits);
+        steps.push_back(std::move(s));
+        break;
+      }
       case BF_OP_UNITARY:
         emit_unitary(op.data, op.target, op.target2, -1);
         break;
@@ -349,6 +358,8 @@ static void run_steps(State& st, std::vector<Step>& steps, const std::vector<Til
       case Step::MEASURE:
         measure(st, s.mq.data(), s.mv.data(), (int32_t)s.mq.size(), s.seed, nullptr, nullptr);
         break;
+      case Step::DIFFUSER: launch_grover_diffuser(st, s.mq.data(), (int32_t)s.mq.size()); break;
+      case Step::INVERSION0: launch_grover_inversion0(st, s.mq.data(), (int32_t)s.mq.size()); break;
     }
   }
 }
@@ -632,7 +643,7 @@ int bf_plan_stats(int32_t n, const bf_op* ops, int64_t nops, const bf_exec_opts*
         bytes += gate_bytes_fraction(s.gate);
       } else {
         ++x;
-        bytes += (s.kind == Step::SWAPBITS) ? 1.0 : 2.0;
+        bytes += (s.kind == Step::SWAPBITS) ? 1.0 : (s.kind == Step::DIFFUSER ? 3.0 : 2.0);
       }
     }
     if (tile_passes) *tile_passes = t;

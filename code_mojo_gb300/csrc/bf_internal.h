@@ -130,6 +130,8 @@ void marginal_probs(State& st, const int32_t* q, const int8_t* values, int32_t n
 void measure(State& st, const int32_t* q, const int8_t* values, int32_t nq, int64_t seed, uint64_t* outcome,
              double* prob);
 void probs_topk(State& st, int k, uint64_t* idx, double* probs);
+void launch_grover_inversion0(State& st, const int32_t* q, int32_t nq);
+void launch_grover_diffuser(State& st, const int32_t* q, int32_t nq);
 // sum |amp|^2 of caller memory with the library's static scratch (noalloc.cu)
 void norm2_noalloc(const void* d_amps, uint64_t num_amps, int32_t dtype, double* d_out, cudaStream_t stream);
 

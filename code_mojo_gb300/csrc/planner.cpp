@@ -57,10 +57,12 @@ void validate_ops(int n, const bf_op* ops, int64_t nops) {
         break;
       case BF_OP_QREV:
       case BF_OP_BITREV:
-      case BF_OP_PERMUTE: {
+      case BF_OP_PERMUTE:
+      case BF_OP_GROVER_DIFFUSER:
+      case BF_OP_GROVER_INVERSION0: {
         if (o.nqubits < 0 || (o.nqubits > 0 && o.qubits == nullptr)) fail(BF_EINVAL, "qubit list is null");
         for (int64_t k = 0; k < o.nqubits; ++k) check_qubit(o.qubits[k], n, "Target");
-        if (o.kind == BF_OP_BITREV) {
+        if (o.kind == BF_OP_BITREV || o.kind == BF_OP_GROVER_DIFFUSER || o.kind == BF_OP_GROVER_INVERSION0) {
           uint64_t seen = 0;
           for (int64_t k = 0; k < o.nqubits; ++k) {
             if ((seen >> o.qubits[k]) & 1) fail(BF_EINVAL, "Duplicate target: %d", o.qubits[k]);

@@ -19,7 +19,7 @@ from typing import Sequence
 
 import numpy as np
 
-from .butterfly import QuantumCircuit, bit_reverse
+from .butterfly import QuantumCircuit, bit_reverse, grover_diffuser
 
 
 def iqft_circuit(qc: QuantumCircuit, targets: Sequence[int], swap: bool = False) -> None:
@@ -106,6 +106,29 @@ def grover_circuit(n: int, marked: int, iterations: int | None = None) -> Quantu
             qc.x(q)
         for q in range(n):
             qc.h(q)
+    return qc
+
+
+def grover_circuit_classical(n: int, marked: int, iterations: int | None = None) -> QuantumCircuit:
+    """The same search with the diffuser as one classical pass (the
+    reference's GROVER_DIFFUSER replacement, quantum_circuit.mojo:300-420):
+    H^n, then per iteration the phase oracle (X gates around an
+    (n-1)-controlled P(pi)) and the diffuser 2*mean - x over all qubits.  The
+    classical diffuser differs from the gate one by a global sign, which no
+    probability sees."""
+    it = grover_iterations(n) if iterations is None else iterations
+    qc = QuantumCircuit(n)
+    for q in range(n):
+        qc.h(q)
+    ctrls = list(range(n - 1))
+    flips = [q for q in range(n) if not (marked >> q) & 1]
+    for _ in range(it):
+        for q in flips:
+            qc.x(q)
+        qc.mcp(ctrls, n - 1, math.pi)
+        for q in flips:
+            qc.x(q)
+        grover_diffuser(qc)
     return qc
 
 

@@ -78,9 +78,13 @@ enum {
   BF_OP_BITREV = 5,    /* classical bit_reverse_tr(targets; none = all)      */
   BF_OP_PERMUTE = 6,   /* classical permute_qubits_tr(order)                 */
   BF_OP_CSWAP = 7,     /* classical swap_tr(a, b) (apply_swap)               */
-  BF_OP_MEASURE = 8    /* MeasurementTransformation (apply_measure): qubits =
+  BF_OP_MEASURE = 8,   /* MeasurementTransformation (apply_measure): qubits =
                           targets, data = per-target values as doubles (-1 free,
                           0, 1) or NULL (all free), arg = seed (< 0: clock)   */
+  BF_OP_GROVER_DIFFUSER = 9,   /* classical apply_grover_diffuser(qubits; none = all):
+                                  x <- 2 mean - x over each target block      */
+  BF_OP_GROVER_INVERSION0 = 10 /* classical apply_grover_inversion_0(qubits; none =
+                                  all): negate the all-zero target amplitude  */
 };
 
 /* bf_op.flags */

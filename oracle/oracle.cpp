@@ -567,6 +567,8 @@ void validate(const St& s, const bf_op* ops, int64_t nops) {
         for (int64_t k = 0; k < o.nqubits; ++k) check_qubit(o.qubits[k], n, "Target");
         break;
       case BF_OP_MEASURE:
+      case BF_OP_GROVER_DIFFUSER:
+      case BF_OP_GROVER_INVERSION0:
         for (int64_t k = 0; k < o.nqubits; ++k) check_qubit(o.qubits[k], n, "Target");
         break;
       case BF_OP_UNITARY:
@@ -670,6 +672,41 @@ void run(St& s, const Ctx& c, const bf_op* ops, int64_t nops, bool do_validate) 
       case BF_OP_CSWAP:  // apply_swap (:434-444)
         swap_bits(s, o.target, o.target2);
         break;
+      case BF_OP_GROVER_DIFFUSER:     // apply_grover_diffuser (grover_classical.mojo:284-326)
+      case BF_OP_GROVER_INVERSION0: {  // apply_grover_inversion_0 (grover_classical.mojo:262-281)
+        std::vector<bool> is_t(s.n, o.nqubits == 0);
+        for (int64_t k = 0; k < o.nqubits; ++k) is_t[o.qubits[k]] = true;
+        std::vector<int> tg, other;
+        if (o.nqubits == 0) for (int q = 0; q < s.n; ++q) tg.push_back(q);
+        else tg.assign(o.qubits, o.qubits + o.nqubits);
+        for (int q = 0; q < s.n; ++q) if (!is_t[q]) other.push_back(q);
+        size_t blocks = (size_t)1 << other.size(), bs = (size_t)1 << tg.size();
+        for (size_t b = 0; b < blocks; ++b) {
+          size_t base = 0;
+          for (size_t i = 0; i < other.size(); ++i) if ((b >> i) & 1) base |= (size_t)1 << other[i];
+          if (o.kind == BF_OP_GROVER_INVERSION0) {
+            s.re[base] = -s.re[base];
+            s.im[base] = -s.im[base];
+            continue;
+          }
+          auto idx_of = [&](size_t tm) {
+            size_t idx = base;
+            for (size_t j = 0; j < tg.size(); ++j) if ((tm >> j) & 1) idx |= (size_t)1 << tg[j];
+            return idx;
+          };
+          double sr = 0, si = 0;
+          for (size_t tm = 0; tm < bs; ++tm) { size_t i = idx_of(tm); sr += s.re[i]; si += s.im[i]; }
+          // 2 * mean for both parts (the reference negates the imaginary one,
+          // grover_classical.mojo:318, which is not the inversion about the mean)
+          double ar = 2.0 * (1.0 / (double)bs) * sr, ai = 2.0 * (1.0 / (double)bs) * si;
+          for (size_t tm = 0; tm < bs; ++tm) {
+            size_t i = idx_of(tm);
+            s.re[i] = ar - s.re[i];
+            s.im[i] = ai - s.im[i];
+          }
+        }
+        break;
+      }
       case BF_OP_MEASURE: {  // MeasurementTransformation -> apply_measure (:447-553)
         std::vector<int8_t> v;
         for (int64_t k = 0; k < o.nqubits; ++k) v.push_back(o.data ? (int8_t)o.data[k] : (int8_t)-1);

@@ -434,3 +434,30 @@ def test_topk(n, k, dtype):
     ei, ep = O.topk(re, im, k)
     assert idx.tolist() == ei.tolist()
     assert np.max(np.abs(pr - ep) / ep) <= 1e-13  # double-float squares: ~2^-47 relative
+
+
+# ---- classical Grover passes ----------------------------------------------------
+@pytest.mark.parametrize("targets", [[], [0, 3, 5], [2, 4, 6, 8, 9, 10, 11, 12, 13], list(range(1, 15)), [14]])
+@pytest.mark.parametrize("dtype", ["c128", "c64"])
+def test_grover_classical_passes(targets, dtype):
+    n = 15
+    re, im = W.random_normal_state(n, 60)
+    for build in (bfy.grover_diffuser, bfy.grover_inversion_0):
+        qc = bfy.QuantumCircuit(n)
+        build(qc, targets)
+        got = run_gpu(qc, re, im, dtype=dtype)
+        exp = oracle(qc, re, im)
+        if dtype == "c128":
+            assert maxdiff(got, exp) <= TOL128
+        else:
+            assert 1 - abs(np.vdot(exp, got)) ** 2 <= 1e-6
+
+
+@pytest.mark.parametrize("strategy", STRATS)
+def test_classical_grover_search(strategy):
+    n, marked = 12, 3001
+    re, im = O.basis(n)
+    qc = W.grover_circuit_classical(n, marked)
+    got = run_gpu(qc, re, im, strategy)
+    assert maxdiff(got, oracle(qc, re, im)) <= TOL128
+    assert int(np.argmax(np.abs(got))) == marked

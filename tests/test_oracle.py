@@ -293,3 +293,50 @@ def test_measure_op_inside_a_circuit_runs_on_the_oracle():
     idx = np.arange(1 << n)
     nz = idx[np.abs(z) > 0]
     assert len(set(((nz >> 1) & 1).tolist())) == 1 and len(set(((nz >> 4) & 1).tolist())) == 1
+
+
+# ---- classical Grover passes (grover_classical.mojo:262-326) ------------------
+@pytest.mark.parametrize("targets", [[], [0, 2, 3], [4]])
+def test_classical_diffuser_is_minus_the_gate_diffuser(targets):
+    n = 5
+    re, im = W.random_normal_state(n, 50)
+    t = targets or list(range(n))
+    gate = bfy.QuantumCircuit(n)
+    for q in t:
+        gate.h(q)
+    for q in t:
+        gate.x(q)
+    if len(t) > 1:
+        gate.mcp(t[:-1], t[-1], math.pi)
+    else:
+        gate.p(t[0], math.pi)
+    for q in t:
+        gate.x(q)
+    for q in t:
+        gate.h(q)
+    classical = bfy.QuantumCircuit(n)
+    bfy.grover_diffuser(classical, targets)
+    a = cplx(O.run(gate, re, im))
+    b = cplx(O.run(classical, re, im))
+    assert np.max(np.abs(a + b)) < 1e-13
+
+
+def test_classical_inversion_matches_gates():
+    n = 5
+    re, im = W.random_normal_state(n, 51)
+    t = [1, 3, 4]
+    gate = bfy.QuantumCircuit(n)
+    for q in t:
+        gate.x(q)
+    gate.mcp(t[:-1], t[-1], math.pi)
+    for q in t:
+        gate.x(q)
+    classical = bfy.QuantumCircuit(n)
+    bfy.grover_inversion_0(classical, t)
+    assert np.max(np.abs(cplx(O.run(gate, re, im)) - cplx(O.run(classical, re, im)))) < 1e-15
+
+
+def test_classical_grover_finds_marked():
+    n, marked = 8, 201
+    p = np.abs(cplx(O.run(W.grover_circuit_classical(n, marked), *O.basis(n)))) ** 2
+    assert int(np.argmax(p)) == marked and p[marked] > 0.99
