@@ -89,6 +89,15 @@ SIGNATURES = {
     "bf_measure": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int64, C.POINTER(C.c_uint64),
                    C.POINTER(C.c_double)],
     "bf_probs_topk": [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p],
+    "bf_batch_create": [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(bf_exec_opts),
+                        C.POINTER(C.c_void_p)],
+    "bf_batch_run": [C.c_void_p, C.c_int32],
+    "bf_batch_sync": [C.c_void_p],
+    "bf_batch_download": [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p],
+    "bf_batch_stats": [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_uint64),
+                       C.POINTER(C.c_int32), C.POINTER(C.c_uint64)],
+    "bf_batch_stream": [C.c_void_p, C.POINTER(C.c_void_p)],
+    "bf_batch_destroy": [C.c_void_p],
     "bf_norm2_noalloc": [C.c_void_p, C.c_uint64, C.c_int32, C.c_void_p, C.c_void_p],
     "bf_validate": [C.c_int32, C.POINTER(bf_op), C.c_int64],
     "bf_plan_stats": [C.c_int32, C.POINTER(bf_op), C.c_int64, C.POINTER(bf_exec_opts), C.POINTER(C.c_int64),

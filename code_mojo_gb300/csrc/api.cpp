@@ -613,6 +613,66 @@ int bf_probs_topk(bf_state* hst, int32_t k, uint64_t* indices, double* probs) {
   });
 }
 
+// ---- batches -------------------------------------------------------------------
+static inline Batch* B_(bf_batch* h) { return reinterpret_cast<Batch*>(h); }
+
+int bf_batch_create(int32_t ncirc, const int32_t* num_qubits, const bf_op* const* ops, const int64_t* nops,
+                    int32_t dtype, const bf_exec_opts* opts, bf_batch** out) {
+  return guarded([&]() {
+    if (!out) fail(BF_EINVAL, "out is null");
+    *out = nullptr;
+    if (dtype != BF_C128 && dtype != BF_C64) fail(BF_EINVAL, "unknown dtype %d", dtype);
+    bf_exec_opts o;
+    if (opts) o = *opts;
+    else bf_exec_opts_init(&o);
+    if (o.tile_qubits < 0 || o.tile_qubits > kMaxTileQubits)
+      fail(BF_EINVAL, "tile_qubits must be in [0, %d]", kMaxTileQubits);
+    const char* math = std::getenv("BFGPU_C128_MATH");
+    int prec = dtype == BF_C64 ? PREC_F32 : ((math && std::strcmp(math, "f64") == 0) ? PREC_F64 : PREC_DF);
+    *out = reinterpret_cast<bf_batch*>(batch_create(ncirc, num_qubits, ops, nops, dtype, o, prec));
+  });
+}
+
+int bf_batch_run(bf_batch* h, int32_t sync) {
+  return guarded([&]() {
+    if (!h) fail(BF_EINVAL, "batch is null");
+    batch_run(*B_(h), sync != 0);
+  });
+}
+
+int bf_batch_sync(bf_batch* h) {
+  return guarded([&]() {
+    if (!h) fail(BF_EINVAL, "batch is null");
+    batch_sync(*B_(h));
+  });
+}
+
+int bf_batch_download(bf_batch* h, int32_t circuit, double* re, double* im) {
+  return guarded([&]() {
+    if (!h || !re || !im) fail(BF_EINVAL, "null argument");
+    batch_download(*B_(h), circuit, re, im);
+  });
+}
+
+int bf_batch_stats(bf_batch* h, int64_t* tasks, int64_t* passes, uint64_t* state_bytes, int32_t* graph,
+                   uint64_t* launches) {
+  return guarded([&]() {
+    if (!h) fail(BF_EINVAL, "batch is null");
+    batch_stats(*B_(h), tasks, passes, state_bytes, graph, launches);
+  });
+}
+
+int bf_batch_stream(bf_batch* h, void** stream) {
+  return guarded([&]() {
+    if (!h || !stream) fail(BF_EINVAL, "null argument");
+    *stream = batch_stream(*B_(h));
+  });
+}
+
+int bf_batch_destroy(bf_batch* h) {
+  return guarded([&]() { batch_destroy(B_(h)); });
+}
+
 int bf_norm2_noalloc(const void* d_amps, uint64_t num_amps, int32_t dtype, double* d_out, void* stream) {
   return guarded([&]() { norm2_noalloc(d_amps, num_amps, dtype, d_out, static_cast<cudaStream_t>(stream)); });
 }

@@ -1,0 +1,380 @@
+// batch.cu — many independent circuits in one persistent launch.
+//
+// Every circuit of a batch is planned into tile passes (the same planner and
+// tile body as a single state).  A task is one tile of one pass of one
+// circuit; tasks are ordered pass-major, (pass index, circuit, tile), and the
+// CTAs of one cooperative launch take them from an atomic ticket.  A task of
+// pass p waits until its circuit has finished every tile of passes < p: the
+// tasks it waits for hold smaller tickets, so they are already running on
+// co-resident CTAs and the wait always ends.  The wait is bounded anyway
+// (spin_limit polls); on expiry the CTA records an error flag, skips its
+// task and the host reports BF_ETIMEDOUT.
+//
+// The states of all circuits live in one pooled buffer.  A run (|0...0> for
+// every state, then all tasks) is captured once into a CUDA graph and
+// replayed by bf_batch_run.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "tile_body.cuh"
+
+namespace bf {
+
+struct BatchTask {
+  uint32_t circuit;
+  uint32_t pass;   // index into the pass table
+  uint32_t tile;
+  uint32_t need;   // tasks of this circuit that must have finished
+};
+
+struct BatchPass {
+  uint64_t offset;  // first amplitude of the circuit's state in the pool
+  TileGeom geo;
+  uint32_t op_begin;
+  uint32_t nops;
+};
+
+struct BatchDesc {
+  void* pool;
+  const BatchTask* tasks;
+  const BatchPass* passes;
+  const TileOp* ops;
+  unsigned int* done;
+  unsigned long long* ticket;
+  int* error;
+  unsigned long long ntasks;
+  unsigned int spin_limit;
+};
+
+template <class P>
+__global__ void __launch_bounds__(kTileThreads) k_batch(const BatchDesc d) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ unsigned long long t_sh;
+  __shared__ int ok_sh;
+  for (;;) {
+    if (threadIdx.x == 0) t_sh = atomicAdd(d.ticket, 1ull);
+    __syncthreads();
+    const unsigned long long t = t_sh;
+    __syncthreads();
+    if (t >= d.ntasks) break;  // CTA-uniform
+    const BatchTask task = d.tasks[t];
+    if (threadIdx.x == 0) {
+      int ok = 1;
+      const volatile unsigned int* dn = d.done + task.circuit;
+      unsigned int polls = 0;
+      while (*dn < task.need) {
+        if (++polls > d.spin_limit) {
+          ok = 0;
+          atomicExch(d.error, 1);
+          break;
+        }
+        __nanosleep(128);
+      }
+      __threadfence();
+      ok_sh = ok;
+    }
+    __syncthreads();
+    if (ok_sh) {
+      const BatchPass& bp = d.passes[task.pass];
+      TileGeom geo = bp.geo;
+      run_tile<P, true>(static_cast<typename P::Glob*>(d.pool) + bp.offset, d.ops + bp.op_begin, (int)bp.nops,
+                        geo, task.tile, smem_raw);
+    }
+    __threadfence();  // every thread's stores are visible device-wide ...
+    __syncthreads();
+    if (threadIdx.x == 0) atomicAdd(d.done + task.circuit, 1u);  // ... before the task counts as done
+  }
+}
+
+template <class T>
+__global__ void k_batch_basis(T* pool, const uint64_t* offsets, int ncirc);
+template <>
+__global__ void k_batch_basis<double2>(double2* pool, const uint64_t* offsets, int ncirc) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < ncirc) pool[offsets[c]] = make_double2(1.0, 0.0);
+}
+template <>
+__global__ void k_batch_basis<float2>(float2* pool, const uint64_t* offsets, int ncirc) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < ncirc) pool[offsets[c]] = make_float2(1.0f, 0.0f);
+}
+
+struct Batch {
+  int device = 0, num_sms = 0;
+  int dtype = BF_C64, prec = PREC_F32;
+  int ncirc = 0;
+  std::vector<int32_t> nq;
+  std::vector<uint64_t> offsets;  // in amplitudes
+  uint64_t pool_amps = 0;
+  size_t smem = 0;
+  void* pool = nullptr;
+  BatchTask* d_tasks = nullptr;
+  BatchPass* d_passes = nullptr;
+  TileOp* d_ops = nullptr;
+  uint64_t* d_offsets = nullptr;
+  unsigned int* d_done = nullptr;
+  unsigned long long* d_ticket = nullptr;
+  int* d_error = nullptr;
+  int* h_error = nullptr;
+  uint64_t ntasks = 0, npasses = 0;
+  unsigned grid = 0;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  uint64_t launches = 0;
+  size_t amp_bytes() const { return dtype == BF_C128 ? 16 : 8; }
+};
+
+template <class P>
+static void enqueue_run(Batch& b) {
+  BF_CUDA(cudaMemsetAsync(b.pool, 0, b.pool_amps * b.amp_bytes(), b.stream));
+  k_batch_basis<typename P::Glob><<<(b.ncirc + 255) / 256, 256, 0, b.stream>>>(
+      static_cast<typename P::Glob*>(b.pool), b.d_offsets, b.ncirc);
+  BF_CUDA(cudaGetLastError());
+  BF_CUDA(cudaMemsetAsync(b.d_done, 0, b.ncirc * sizeof(unsigned int), b.stream));
+  BF_CUDA(cudaMemsetAsync(b.d_ticket, 0, sizeof(unsigned long long), b.stream));
+  BF_CUDA(cudaMemsetAsync(b.d_error, 0, sizeof(int), b.stream));
+  BatchDesc d;
+  d.pool = b.pool;
+  d.tasks = b.d_tasks;
+  d.passes = b.d_passes;
+  d.ops = b.d_ops;
+  d.done = b.d_done;
+  d.ticket = b.d_ticket;
+  d.error = b.d_error;
+  d.ntasks = b.ntasks;
+  d.spin_limit = 1u << 24;  // x 128 ns sleeps: about 2 s before the error flag
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(b.grid);
+  cfg.blockDim = dim3(kTileThreads);
+  cfg.dynamicSmemBytes = b.smem;
+  cfg.stream = b.stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  BF_CUDA(cudaLaunchKernelEx(&cfg, k_batch<P>, d));
+  BF_CUDA(cudaMemcpyAsync(b.h_error, b.d_error, sizeof(int), cudaMemcpyDeviceToHost, b.stream));
+}
+
+static void enqueue(Batch& b) {
+  switch (b.prec) {
+    case PREC_F64: enqueue_run<PolF64>(b); break;
+    case PREC_DF: enqueue_run<PolDF>(b); break;
+    default: enqueue_run<PolF32>(b); break;
+  }
+}
+
+template <class P>
+static void size_grid(Batch& b) {
+  BF_CUDA(cudaFuncSetAttribute(k_batch<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b.smem));
+  int per_sm = 0;
+  BF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<P>, kTileThreads, b.smem));
+  if (per_sm < 1) fail(BF_EUNSUPPORTED, "batch kernel cannot be resident with %zu bytes of shared memory", b.smem);
+  b.grid = (unsigned)(per_sm * b.num_sms);
+}
+
+static void free_batch(Batch* b) {
+  if (!b) return;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  cudaFree(b->pool);
+  cudaFree(b->d_tasks);
+  cudaFree(b->d_passes);
+  cudaFree(b->d_ops);
+  cudaFree(b->d_offsets);
+  cudaFree(b->d_done);
+  cudaFree(b->d_ticket);
+  cudaFree(b->d_error);
+  if (b->h_error) cudaFreeHost(b->h_error);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+template <class T>
+static void dev_upload(T** dst, const std::vector<T>& v) {
+  size_t bytes = std::max<size_t>(1, v.size()) * sizeof(T);
+  if (cudaMalloc(dst, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    *dst = nullptr;
+    fail(BF_ENOMEM, "cannot allocate %zu bytes of batch tables", bytes);
+  }
+  if (!v.empty()) BF_CUDA(cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+}
+
+Batch* batch_create(int ncirc, const int32_t* nq, const bf_op* const* ops, const int64_t* nops, int dtype,
+                    const bf_exec_opts& o, int prec) {
+  if (ncirc < 1) fail(BF_EINVAL, "a batch needs at least one circuit");
+  if (!nq || !ops || !nops) fail(BF_EINVAL, "null argument");
+  Batch* b = new Batch();
+  try {
+    b->dtype = dtype;
+    b->prec = prec;
+    b->ncirc = ncirc;
+    BF_CUDA(cudaGetDevice(&b->device));
+    BF_CUDA(cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, b->device));
+    const int Kcap = o.tile_qubits > 0 ? o.tile_qubits : 12;
+    std::vector<BatchPass> passes;
+    std::vector<TileOp> prog;
+    // per circuit: passes (each with its tile count)
+    std::vector<std::vector<uint32_t>> circ_passes(ncirc);
+    uint64_t off = 0;
+    size_t smem = 0;
+    for (int c = 0; c < ncirc; ++c) {
+      int n = nq[c];
+      if (n < 1 || n > 30) fail(BF_EINVAL, "circuit %d: num_qubits must be in [1, 30], got %d", c, n);
+      validate_ops(n, ops[c], nops[c]);
+      std::vector<GateInstr> gates;
+      for (int64_t i = 0; i < nops[c]; ++i) {
+        const bf_op& op = ops[c][i];
+        if (op.kind != BF_OP_GATE || (op.flags & BF_OPF_FUSE_WITH_NEXT))
+          fail(BF_EUNSUPPORTED, "circuit %d: batches take gate transformations only (op %lld)", c, (long long)i);
+        gates.push_back(lower_gate(op, o.specialized));
+      }
+      b->nq.push_back(n);
+      b->offsets.push_back(off);
+      off += ((1ull << n) + 31) & ~31ull;  // 256-byte aligned starts
+      int K = std::min(n, Kcap);
+      for (auto& ps : plan_gates(n, gates, K, /*allow_single=*/false)) {
+        BatchPass bp;
+        std::memset(&bp, 0, sizeof bp);
+        bp.offset = b->offsets.back();
+        bp.geo.K = ps.tile.K;
+        bp.geo.L = ps.tile.L;
+        for (int j = 0; j < ps.tile.K; ++j) bp.geo.q[j] = ps.tile.q[j];
+        bp.op_begin = (uint32_t)prog.size();
+        bp.nops = (uint32_t)ps.tile.ops.size();
+        prog.insert(prog.end(), ps.tile.ops.begin(), ps.tile.ops.end());
+        circ_passes[c].push_back((uint32_t)passes.size());
+        passes.push_back(bp);
+        size_t sm = 0;
+        switch (prec) {
+          case PREC_F64: sm = tile_smem_bytes<PolF64>(bp.geo.K, bp.geo.L); break;
+          case PREC_DF: sm = tile_smem_bytes<PolDF>(bp.geo.K, bp.geo.L); break;
+          default: sm = tile_smem_bytes<PolF32>(bp.geo.K, bp.geo.L); break;
+        }
+        smem = std::max(smem, sm);
+      }
+    }
+    b->pool_amps = off;
+    b->smem = std::max<size_t>(smem, 1024);
+    // tasks, pass-major
+    std::vector<BatchTask> tasks;
+    size_t max_p = 0;
+    for (auto& cp : circ_passes) max_p = std::max(max_p, cp.size());
+    std::vector<uint32_t> done_before(ncirc, 0);
+    for (size_t p = 0; p < max_p; ++p)
+      for (int c = 0; c < ncirc; ++c) {
+        if (p >= circ_passes[c].size()) continue;
+        uint32_t pi = circ_passes[c][p];
+        uint32_t tiles = (uint32_t)(1ull << (b->nq[c] - passes[pi].geo.K));
+        for (uint32_t t = 0; t < tiles; ++t) tasks.push_back(BatchTask{(uint32_t)c, pi, t, done_before[c]});
+        done_before[c] += tiles;
+      }
+    b->ntasks = tasks.size();
+    b->npasses = passes.size();
+    size_t pool_bytes = b->pool_amps * b->amp_bytes();
+    if (cudaMalloc(&b->pool, pool_bytes) != cudaSuccess) {
+      cudaGetLastError();
+      b->pool = nullptr;
+      fail(BF_ENOMEM, "cannot allocate %zu bytes for the batch states", pool_bytes);
+    }
+    dev_upload(&b->d_tasks, tasks);
+    dev_upload(&b->d_passes, passes);
+    dev_upload(&b->d_ops, prog);
+    dev_upload(&b->d_offsets, b->offsets);
+    std::vector<unsigned int> zeros(ncirc, 0);
+    dev_upload(&b->d_done, zeros);
+    std::vector<unsigned long long> z1(1, 0);
+    dev_upload(&b->d_ticket, z1);
+    std::vector<int> z2(1, 0);
+    dev_upload(&b->d_error, z2);
+    if (cudaHostAlloc(&b->h_error, sizeof(int), cudaHostAllocDefault) != cudaSuccess) {
+      cudaGetLastError();
+      b->h_error = nullptr;
+      fail(BF_ENOMEM, "cannot allocate the batch status word");
+    }
+    *b->h_error = 0;
+    BF_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    switch (prec) {
+      case PREC_F64: size_grid<PolF64>(*b); break;
+      case PREC_DF: size_grid<PolDF>(*b); break;
+      default: size_grid<PolF32>(*b); break;
+    }
+    // capture one run into a graph; if this stack cannot capture it, runs
+    // are enqueued directly
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      bool ok = true;
+      try {
+        enqueue(*b);
+      } catch (const Error&) {
+        ok = false;
+      }
+      cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+      if (ok && e == cudaSuccess && g && cudaGraphInstantiate(&b->graph, g, 0) == cudaSuccess) {
+        // captured
+      } else {
+        b->graph = nullptr;
+      }
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+    }
+  } catch (...) {
+    free_batch(b);
+    throw;
+  }
+  return b;
+}
+
+void batch_run(Batch& b, bool sync) {
+  if (b.graph) BF_CUDA(cudaGraphLaunch(b.graph, b.stream));
+  else enqueue(b);
+  b.launches += 2;  // basis kernel + persistent kernel
+  if (sync) {
+    BF_CUDA(cudaStreamSynchronize(b.stream));
+    if (*b.h_error) fail(BF_ETIMEDOUT, "batch: a task waited past its bound for its circuit's previous pass");
+  }
+}
+
+void batch_sync(Batch& b) {
+  BF_CUDA(cudaStreamSynchronize(b.stream));
+  if (*b.h_error) fail(BF_ETIMEDOUT, "batch: a task waited past its bound for its circuit's previous pass");
+}
+
+void batch_download(Batch& b, int c, double* re, double* im) {
+  if (c < 0 || c >= b.ncirc) fail(BF_EINVAL, "circuit index %d out of range", c);
+  batch_sync(b);
+  uint64_t N = 1ull << b.nq[c];
+  size_t eb = b.amp_bytes();
+  std::vector<unsigned char> h(N * eb);
+  BF_CUDA(cudaMemcpy(h.data(), static_cast<unsigned char*>(b.pool) + b.offsets[c] * eb, N * eb,
+                     cudaMemcpyDeviceToHost));
+  for (uint64_t i = 0; i < N; ++i) {
+    if (eb == 16) {
+      const double* p = reinterpret_cast<const double*>(h.data()) + 2 * i;
+      re[i] = p[0];
+      im[i] = p[1];
+    } else {
+      const float* p = reinterpret_cast<const float*>(h.data()) + 2 * i;
+      re[i] = (double)p[0];
+      im[i] = (double)p[1];
+    }
+  }
+}
+
+void batch_destroy(Batch* b) { free_batch(b); }
+
+void batch_stats(const Batch& b, int64_t* tasks, int64_t* passes, uint64_t* state_bytes, int32_t* graph,
+                 uint64_t* launches) {
+  if (tasks) *tasks = (int64_t)b.ntasks;
+  if (passes) *passes = (int64_t)b.npasses;
+  if (state_bytes) *state_bytes = b.pool_amps * b.amp_bytes();
+  if (graph) *graph = b.graph ? 1 : 0;
+  if (launches) *launches = b.launches;
+}
+
+void* batch_stream(const Batch& b) { return (void*)b.stream; }
+
+}  // namespace bf

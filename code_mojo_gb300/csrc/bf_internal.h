@@ -148,6 +148,18 @@ struct PlanStep {
   GateInstr gate;  // when !is_tile
   TilePass tile;   // when is_tile
 };
-std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int K);
+std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int K, bool allow_single = true);
+
+// Batches of independent circuits (batch.cu).
+struct Batch;
+Batch* batch_create(int ncirc, const int32_t* nq, const bf_op* const* ops, const int64_t* nops, int dtype,
+                    const bf_exec_opts& o, int prec);
+void batch_run(Batch& b, bool sync);
+void batch_sync(Batch& b);
+void batch_download(Batch& b, int c, double* re, double* im);
+void batch_destroy(Batch* b);
+void batch_stats(const Batch& b, int64_t* tasks, int64_t* passes, uint64_t* state_bytes, int32_t* graph,
+                 uint64_t* launches);
+void* batch_stream(const Batch& b);
 
 }  // namespace bf

@@ -197,7 +197,7 @@ static TileOp to_tile_op(const GateInstr& g, const int* loc_of) {
   return t;
 }
 
-std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int K) {
+std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int K, bool allow_single) {
   std::vector<PlanStep> steps;
   if (gates.empty()) return steps;
   K = std::max(1, std::min(K, std::min(n, kMaxTileQubits)));
@@ -238,7 +238,7 @@ std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int
     if (taken.empty()) fail(BF_EINVAL, "internal: tile planner made no progress (K=%d, n=%d)", K, n);
     double single_bytes = 0;
     for (const GateInstr* g : taken) single_bytes += gate_bytes_fraction(*g);
-    if (single_bytes <= 2.0) {
+    if (allow_single && single_bytes <= 2.0) {
       // a tile pass moves 2S; the gates on their own move no more
       for (const GateInstr* g : taken) {
         PlanStep st;

@@ -132,6 +132,35 @@ def grover_circuit_classical(n: int, marked: int, iterations: int | None = None)
     return qc
 
 
+def value_encoding_phase_circuit(n: int, v: float) -> QuantumCircuit:
+    """H on all n qubits, P(2*pi*2^j*v/2^n) on qubit j, then the inverse QFT
+    over the qubits LSB first without swap (gates only): for an integer v the
+    result is the bit-reversed basis state |rev(v)>."""
+    qc = QuantumCircuit(n)
+    for j in range(n):
+        qc.h(j)
+    for j in range(n):
+        qc.p(j, 2 * math.pi * (2 ** j) * v / 2 ** n)
+    iqft_circuit(qc, list(range(n)), swap=False)
+    return qc
+
+
+def batch_workload(count: int = 4096, seed: int = 0, nmin: int = 8, nmax: int = 20,
+                   depth: int = 20) -> list[QuantumCircuit]:
+    """The batched workload: `count` circuits with qubit counts uniform in
+    [nmin, nmax]; even positions are random layered circuits of `depth`
+    layers, odd ones value encodings with v uniform in [0, 2^n)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for i in range(count):
+        n = int(rng.integers(nmin, nmax + 1))
+        if i % 2 == 0:
+            out.append(random_layered_circuit(n, depth, seed=int(rng.integers(0, 2 ** 31))))
+        else:
+            out.append(value_encoding_phase_circuit(n, float(rng.uniform(0, 2 ** n))))
+    return out
+
+
 def random_normal_state(n: int, seed: int = 0) -> tuple[np.ndarray, np.ndarray]:
     """Amplitudes with re, im i.i.d. N(0, 1) from a seed, normalised to unit
     norm in FP64 (the QFT workload's initial state)."""

@@ -211,6 +211,31 @@ int bf_measure(bf_state* st, const int32_t* targets, const int8_t* values,
  * ascending index.  Blocks. */
 int bf_probs_topk(bf_state* st, int32_t k, uint64_t* indices, double* probs);
 
+/* ---- batches of independent circuits -------------------------------------
+ * No single counterpart in the reference (its benches run circuits one at a
+ * time through execute).  Many small circuits (1..30 qubits each, gate
+ * transformations only) run from |0...0> in ONE persistent cooperative
+ * launch: each circuit is planned into tile passes, every tile of every pass
+ * is a task, tasks are taken from an atomic ticket in pass-major order and a
+ * task waits (bounded) for its circuit's previous pass.  The run is captured
+ * into a CUDA graph at creation and replayed by bf_batch_run.
+ * ops[c] / nops[c]: circuit c; the arrays are read during the call only. */
+typedef struct bf_batch bf_batch;
+int bf_batch_create(int32_t ncircuits, const int32_t* num_qubits,
+                    const bf_op* const* ops, const int64_t* nops,
+                    int32_t dtype, const bf_exec_opts* opts, bf_batch** out);
+/* Runs every circuit from |0...0> (replays the graph); sync != 0 blocks and
+ * reports BF_ETIMEDOUT if a task's bounded wait expired. */
+int bf_batch_run(bf_batch* b, int32_t sync);
+int bf_batch_sync(bf_batch* b);
+/* Amplitudes of circuit c as SoA doubles (2^n each); blocks. */
+int bf_batch_download(bf_batch* b, int32_t circuit, double* re, double* im);
+int bf_batch_stats(bf_batch* b, int64_t* tasks, int64_t* passes,
+                   uint64_t* state_bytes, int32_t* graph_captured,
+                   uint64_t* launches);
+int bf_batch_stream(bf_batch* b, void** stream);
+int bf_batch_destroy(bf_batch* b);
+
 /* ---- sum |amp|^2 without allocating ---------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory: code running while its stream is captured into a CUDA graph, a

@@ -153,3 +153,12 @@ def test_diagonal_gates_never_constrain_tiles():
         qc.p(q, 0.2)
     s = stats(qc, K=6)
     assert s["tile_passes"] == 1 and s["gate_kernels"] == 0
+
+
+def test_batch_workload_shape():
+    circs = W.batch_workload(count=64, seed=1)
+    ns = [c.num_qubits for c in circs]
+    assert min(ns) >= 8 and max(ns) <= 20 and len(circs) == 64
+    # gate transformations only (a batch takes nothing else)
+    for c in circs:
+        assert all(isinstance(t, bfy.GateTransformation) for t in c.transformations)

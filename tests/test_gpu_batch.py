@@ -1,0 +1,56 @@
+"""Batches of independent circuits in one persistent launch, checked circuit by
+circuit against the FP64 oracle: complex128 within max|d amp| <= 1e-12,
+complex64 within infidelity <= 1e-6."""
+import numpy as np
+import pytest
+
+from code_mojo_gb300 import batch as B
+from code_mojo_gb300 import workloads as W
+from oracle import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def expected(qc):
+    r, i = O.run(qc, *O.basis(qc.num_qubits))
+    return r + 1j * i
+
+
+@pytest.mark.parametrize("dtype", ["c64", "c128"])
+def test_batch_matches_oracle(dtype):
+    circs = W.batch_workload(count=48, seed=3, nmin=4, nmax=16, depth=8)
+    b = B.Batch(circs, dtype=dtype)
+    st = b.stats()
+    assert st["graph"] and st["tasks"] >= len(circs)
+    for rep in range(2):  # the graph replays from |0...0> each time
+        b.run()
+        for c, qc in enumerate(circs):
+            got, exp = b.download(c), expected(qc)
+            if dtype == "c128":
+                assert np.max(np.abs(got - exp)) <= 1e-12, (rep, c)
+            else:
+                assert 1 - abs(np.vdot(exp, got)) ** 2 <= 1e-6, (rep, c)
+    b.close()
+
+
+def test_batch_with_many_passes_per_circuit():
+    # narrow tiles force several dependent passes per circuit
+    circs = [W.random_layered_circuit(n, 6, seed=n) for n in (14, 15, 16, 9, 18)]
+    b = B.Batch(circs, dtype="c128", tile_qubits=9)
+    assert b.stats()["passes"] > len(circs)
+    b.run()
+    for c, qc in enumerate(circs):
+        assert np.max(np.abs(b.download(c) - expected(qc))) <= 1e-12
+    b.close()
+
+
+def test_value_encoding_in_a_batch_lands_on_the_reversed_value():
+    vals = [(9, 300), (12, 4095), (10, 1)]
+    circs = [W.value_encoding_phase_circuit(n, v) for n, v in vals]
+    b = B.Batch(circs, dtype="c64")
+    b.run()
+    for c, (n, v) in enumerate(vals):
+        rev = int(format(v, f"0{n}b")[::-1], 2)
+        p = np.abs(b.download(c)) ** 2
+        assert int(np.argmax(p)) == rev and p[rev] > 1 - 1e-5
+    b.close()
