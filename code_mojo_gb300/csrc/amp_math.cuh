@@ -340,13 +340,16 @@ struct PolF32 {
     v.re = a.re * m[4] - a.im * m[5] + b.re * m[6] - b.im * m[7];
     v.im = a.re * m[5] + a.im * m[4] + b.re * m[7] + b.im * m[6];
   }
+  // sqrt(0.5) rounded to FP32 is 1.7e-8 low: multiplying by it would shrink
+  // the norm at every H.  x*hi + x*lo with one FMA keeps the product within
+  // half an ulp of x*sqrt(0.5), so no bias builds up.
+  __device__ static __forceinline__ float mul_sq_half(float x) { return fmaf(x, kSqHalfHi, x * kSqHalfLo); }
   __device__ static __forceinline__ void hadamard(R& u, R& v) {
-    const float s = 0.70710677f;
     R a = u, b = v;
-    u.re = (a.re + b.re) * s;
-    u.im = (a.im + b.im) * s;
-    v.re = (a.re - b.re) * s;
-    v.im = (a.im - b.im) * s;
+    u.re = mul_sq_half(a.re + b.re);
+    u.im = mul_sq_half(a.im + b.im);
+    v.re = mul_sq_half(a.re - b.re);
+    v.im = mul_sq_half(a.im - b.im);
   }
   __device__ static __forceinline__ void ry(R& u, R& v, const Coef& g) {
     float c = g.v[0], s = g.v[4];
