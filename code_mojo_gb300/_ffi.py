@@ -20,7 +20,7 @@ BF_C128, BF_C64 = 0, 1
 BF_GATE_H, BF_GATE_P, BF_GATE_X, BF_GATE_Y, BF_GATE_Z, BF_GATE_RX, BF_GATE_RY, BF_GATE_RZ, BF_GATE_CUSTOM = range(9)
 # op kinds
 (BF_OP_GATE, BF_OP_SWAP, BF_OP_QREV, BF_OP_UNITARY, BF_OP_CUNITARY, BF_OP_BITREV, BF_OP_PERMUTE,
- BF_OP_CSWAP, BF_OP_MEASURE, BF_OP_GROVER_DIFFUSER, BF_OP_GROVER_INVERSION0) = range(11)
+ BF_OP_CSWAP, BF_OP_MEASURE, BF_OP_GROVER_DIFFUSER, BF_OP_GROVER_INVERSION0, BF_OP_CLASSICAL_ORACLE) = range(12)
 BF_OPF_FUSE_WITH_NEXT = 1
 BF_STRATEGY_GPU, BF_STRATEGY_GPU_FUSED = 8, 9
 BF_SPEC_ALL = 127
@@ -55,6 +55,23 @@ class bf_exec_opts(C.Structure):
         ("sync", C.c_int32),
         ("reserved", C.c_int32 * 3),
     ]
+
+
+class bf_server_opts(C.Structure):
+    _fields_ = [("slots", C.c_int32), ("tile_qubits", C.c_int32), ("topk", C.c_int32), ("reserved", C.c_int32),
+                ("hbm_budget_bytes", C.c_uint64)]
+
+
+class bf_result(C.Structure):
+    _fields_ = [("id", C.c_uint64), ("status", C.c_int32), ("num_qubits", C.c_int32), ("dtype", C.c_int32),
+                ("slot", C.c_int32), ("k", C.c_int32), ("reserved", C.c_int32), ("t_submit", C.c_double),
+                ("t_start", C.c_double), ("t_done", C.c_double), ("top_index", C.c_uint64 * 16),
+                ("top_prob", C.c_double * 16), ("message", C.c_char * 128)]
+
+
+class bf_server_counters(C.Structure):
+    _fields_ = [(k, C.c_uint64) for k in ("submitted", "completed", "failed", "queued", "running", "bytes_in_use",
+                                          "peak_bytes", "budget_bytes")]
 
 
 class BFError(RuntimeError):
@@ -98,6 +115,12 @@ SIGNATURES = {
                        C.POINTER(C.c_int32), C.POINTER(C.c_uint64)],
     "bf_batch_stream": [C.c_void_p, C.POINTER(C.c_void_p)],
     "bf_batch_destroy": [C.c_void_p],
+    "bf_server_create": [C.POINTER(bf_server_opts), C.POINTER(C.c_void_p)],
+    "bf_server_submit": [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int64, C.POINTER(C.c_uint64)],
+    "bf_server_poll": [C.c_void_p, C.POINTER(bf_result), C.c_int32, C.POINTER(C.c_int32)],
+    "bf_server_wait_idle": [C.c_void_p, C.c_int64],
+    "bf_server_stats": [C.c_void_p, C.POINTER(bf_server_counters)],
+    "bf_server_destroy": [C.c_void_p],
     "bf_norm2_noalloc": [C.c_void_p, C.c_uint64, C.c_int32, C.c_void_p, C.c_void_p],
     "bf_validate": [C.c_int32, C.POINTER(bf_op), C.c_int64],
     "bf_plan_stats": [C.c_int32, C.POINTER(bf_op), C.c_int64, C.POINTER(bf_exec_opts), C.POINTER(C.c_int64),

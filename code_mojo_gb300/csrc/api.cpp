@@ -74,7 +74,7 @@ static void upload_program(State& st, const std::vector<TileOp>& prog) {
 // ---- execution -------------------------------------------------------------
 // A step is one launch (or a launch group) in op order.
 struct Step {
-  enum Kind { GATE, TILE, BITREV, PERMUTE, SWAPBITS, UNITARY, MEASURE, DIFFUSER, INVERSION0 } kind;
+  enum Kind { GATE, TILE, BITREV, PERMUTE, SWAPBITS, UNITARY, MEASURE, DIFFUSER, INVERSION0, ORACLE } kind;
   GateInstr gate;
   TilePass tile;            // ops moved into the program; tile.ops emptied
   size_t prog_off = 0;
@@ -323,6 +323,14 @@ static void build_steps(int n, const bf_op* ops, int64_t nops, const bf_exec_opt
         steps.push_back(std::move(s));
         break;
       }
+      case BF_OP_CLASSICAL_ORACLE: {  // classical_oracle (grover.mojo:64-66)
+        flush();
+        Step s;
+        s.kind = Step::ORACLE;
+        s.u.assign(op.data, op.data + op.nqubits);
+        steps.push_back(std::move(s));
+        break;
+      }
       case BF_OP_GROVER_DIFFUSER:     // apply_grover_diffuser (grover_classical.mojo:284-326)
       case BF_OP_GROVER_INVERSION0: {  // apply_grover_inversion_0 (grover_classical.mojo:262-281)
         flush();
@@ -360,23 +368,53 @@ static void run_steps(State& st, std::vector<Step>& steps, const std::vector<Til
         break;
       case Step::DIFFUSER: launch_grover_diffuser(st, s.mq.data(), (int32_t)s.mq.size()); break;
       case Step::INVERSION0: launch_grover_inversion0(st, s.mq.data(), (int32_t)s.mq.size()); break;
+      case Step::ORACLE: launch_classical_oracle(st, s.u.data(), (int64_t)s.u.size()); break;
     }
   }
 }
 
+static void free_state(State* st);
+
+void execute_ops(State& st, const bf_op* ops, int64_t nops, bf_exec_opts o) {
+  if (o.strategy >= 0 && o.strategy <= 7)
+    fail(BF_EUNSUPPORTED, "Execution strategy %d is a CPU strategy; use BF_STRATEGY_GPU(_FUSED)", o.strategy);
+  if (o.strategy != BF_STRATEGY_GPU && o.strategy != BF_STRATEGY_GPU_FUSED)
+    fail(BF_EINVAL, "Unknown execution strategy: %d", o.strategy);
+  if (o.tile_qubits < 0 || o.tile_qubits > kMaxTileQubits)
+    fail(BF_EINVAL, "tile_qubits must be in [0, %d]", kMaxTileQubits);
+  if (o.tile_qubits == 0) o.tile_qubits = env_int("BFGPU_TILE_QUBITS", default_tile_qubits(st));
+  if (o.validate) validate_ops(st.n, ops, nops);
+  std::vector<Step> steps;
+  std::vector<TileOp> prog;
+  build_steps(st.n, ops, nops, o, steps, prog);
+  run_steps(st, steps, prog);
+}
+
+void init_state_runtime(State& st) {
+  BF_CUDA(cudaGetDevice(&st.device));
+  BF_CUDA(cudaDeviceGetAttribute(&st.num_sms, cudaDevAttrMultiProcessorCount, st.device));
+  BF_CUDA(cudaStreamCreateWithFlags(&st.stream, cudaStreamNonBlocking));
+  BF_CUDA(cudaEventCreateWithFlags(&st.prog_event, cudaEventDisableTiming));
+}
+
+void release_state_members(State& st) {
+  if (st.stream) cudaStreamSynchronize(st.stream);
+  if (st.amp) cudaFree(st.amp);
+  if (st.scratch) cudaFree(st.scratch);
+  if (st.d_prog) cudaFree(st.d_prog);
+  if (st.h_prog) cudaFreeHost(st.h_prog);
+  if (st.d_stage) cudaFree(st.d_stage);
+  if (st.d_partial) cudaFree(st.d_partial);
+  if (st.h_partial) cudaFreeHost(st.h_partial);
+  if (st.d_umat) cudaFree(st.d_umat);
+  if (st.prog_event) cudaEventDestroy(st.prog_event);
+  if (st.stream) cudaStreamDestroy(st.stream);
+  st = State();
+}
+
 static void free_state(State* st) {
   if (!st) return;
-  if (st->stream) cudaStreamSynchronize(st->stream);
-  if (st->amp) cudaFree(st->amp);
-  if (st->scratch) cudaFree(st->scratch);
-  if (st->d_prog) cudaFree(st->d_prog);
-  if (st->h_prog) cudaFreeHost(st->h_prog);
-  if (st->d_stage) cudaFree(st->d_stage);
-  if (st->d_partial) cudaFree(st->d_partial);
-  if (st->h_partial) cudaFreeHost(st->h_partial);
-  if (st->d_umat) cudaFree(st->d_umat);
-  if (st->prog_event) cudaEventDestroy(st->prog_event);
-  if (st->stream) cudaStreamDestroy(st->stream);
+  release_state_members(*st);
   delete st;
 }
 
@@ -444,10 +482,7 @@ int bf_state_create(int32_t n, int32_t dtype, bf_state** out) {
       const char* math = std::getenv("BFGPU_C128_MATH");
       if (dtype == BF_C64) st->prec = PREC_F32;
       else st->prec = (math && std::strcmp(math, "f64") == 0) ? PREC_F64 : PREC_DF;
-      BF_CUDA(cudaGetDevice(&st->device));
-      BF_CUDA(cudaDeviceGetAttribute(&st->num_sms, cudaDevAttrMultiProcessorCount, st->device));
-      BF_CUDA(cudaStreamCreateWithFlags(&st->stream, cudaStreamNonBlocking));
-      BF_CUDA(cudaEventCreateWithFlags(&st->prog_event, cudaEventDisableTiming));
+      init_state_runtime(*st);
       if (cudaMalloc(&st->amp, st->bytes()) != cudaSuccess) {
         cudaGetLastError();
         st->amp = nullptr;
@@ -562,18 +597,7 @@ int bf_execute(bf_state* hst, const bf_op* ops, int64_t nops, const bf_exec_opts
     bf_exec_opts o;
     if (opts) o = *opts;
     else bf_exec_opts_init(&o);
-    if (o.strategy >= 0 && o.strategy <= 7)
-      fail(BF_EUNSUPPORTED, "Execution strategy %d is a CPU strategy; use BF_STRATEGY_GPU(_FUSED)", o.strategy);
-    if (o.strategy != BF_STRATEGY_GPU && o.strategy != BF_STRATEGY_GPU_FUSED)
-      fail(BF_EINVAL, "Unknown execution strategy: %d", o.strategy);
-    if (o.tile_qubits < 0 || o.tile_qubits > kMaxTileQubits)
-      fail(BF_EINVAL, "tile_qubits must be in [0, %d]", kMaxTileQubits);
-    if (o.tile_qubits == 0) o.tile_qubits = env_int("BFGPU_TILE_QUBITS", default_tile_qubits(*st));
-    if (o.validate) validate_ops(st->n, ops, nops);
-    std::vector<Step> steps;
-    std::vector<TileOp> prog;
-    build_steps(st->n, ops, nops, o, steps, prog);
-    run_steps(*st, steps, prog);
+    execute_ops(*st, ops, nops, o);
     if (o.sync) BF_CUDA(cudaStreamSynchronize(st->stream));
   });
 }
@@ -677,6 +701,56 @@ int bf_norm2_noalloc(const void* d_amps, uint64_t num_amps, int32_t dtype, doubl
   return guarded([&]() { norm2_noalloc(d_amps, num_amps, dtype, d_out, static_cast<cudaStream_t>(stream)); });
 }
 
+// ---- serving -----------------------------------------------------------------
+static inline Server* V_(bf_server* h) { return reinterpret_cast<Server*>(h); }
+
+int bf_server_create(const bf_server_opts* opts, bf_server** out) {
+  return guarded([&]() {
+    if (!out) fail(BF_EINVAL, "out is null");
+    *out = nullptr;
+    bf_server_opts o;
+    std::memset(&o, 0, sizeof o);
+    if (opts) o = *opts;
+    if (o.tile_qubits < 0 || o.tile_qubits > kMaxTileQubits)
+      fail(BF_EINVAL, "tile_qubits must be in [0, %d]", kMaxTileQubits);
+    *out = reinterpret_cast<bf_server*>(server_create(o));
+  });
+}
+
+int bf_server_submit(bf_server* h, int32_t n, int32_t dtype, const bf_op* ops, int64_t nops, uint64_t* id) {
+  return guarded([&]() {
+    if (!h) fail(BF_EINVAL, "server is null");
+    uint64_t r = server_submit(*V_(h), n, dtype, ops, nops);
+    if (id) *id = r;
+  });
+}
+
+int bf_server_poll(bf_server* h, bf_result* out, int32_t max, int32_t* count) {
+  return guarded([&]() {
+    if (!h || (max > 0 && !out)) fail(BF_EINVAL, "null argument");
+    int k = server_poll(*V_(h), out, max);
+    if (count) *count = k;
+  });
+}
+
+int bf_server_wait_idle(bf_server* h, int64_t timeout_ms) {
+  return guarded([&]() {
+    if (!h) fail(BF_EINVAL, "server is null");
+    if (!server_wait_idle(*V_(h), timeout_ms)) fail(BF_ETIMEDOUT, "server still busy after %lld ms", (long long)timeout_ms);
+  });
+}
+
+int bf_server_stats(bf_server* h, bf_server_counters* out) {
+  return guarded([&]() {
+    if (!h || !out) fail(BF_EINVAL, "null argument");
+    server_stats(*V_(h), *out);
+  });
+}
+
+int bf_server_destroy(bf_server* h) {
+  return guarded([&]() { server_destroy(V_(h)); });
+}
+
 // Host-only: validates and plans ops for a state of n qubits without a
 // device, reporting how many tile passes, per-gate kernels and other passes
 // bf_execute would launch and the algorithmic bytes they move (units of S).
@@ -703,7 +777,8 @@ int bf_plan_stats(int32_t n, const bf_op* ops, int64_t nops, const bf_exec_opts*
         bytes += gate_bytes_fraction(s.gate);
       } else {
         ++x;
-        bytes += (s.kind == Step::SWAPBITS) ? 1.0 : (s.kind == Step::DIFFUSER ? 3.0 : 2.0);
+        bytes += (s.kind == Step::SWAPBITS) ? 1.0
+                 : (s.kind == Step::DIFFUSER ? 3.0 : (s.kind == Step::ORACLE ? 0.0 : 2.0));
       }
     }
     if (tile_passes) *tile_passes = t;

@@ -132,6 +132,7 @@ void measure(State& st, const int32_t* q, const int8_t* values, int32_t nq, int6
 void probs_topk(State& st, int k, uint64_t* idx, double* probs);
 void launch_grover_inversion0(State& st, const int32_t* q, int32_t nq);
 void launch_grover_diffuser(State& st, const int32_t* q, int32_t nq);
+void launch_classical_oracle(State& st, const double* idx, int64_t count);
 // sum |amp|^2 of caller memory with the library's static scratch (noalloc.cu)
 void norm2_noalloc(const void* d_amps, uint64_t num_amps, int32_t dtype, double* d_out, cudaStream_t stream);
 
@@ -150,6 +151,12 @@ struct PlanStep {
 };
 std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int K, bool allow_single = true);
 
+// bf_execute's body on a prepared state; stream, event and SM count of a
+// state; releasing every buffer a state owns (api.cpp).
+void execute_ops(State& st, const bf_op* ops, int64_t nops, bf_exec_opts o);
+void init_state_runtime(State& st);
+void release_state_members(State& st);
+
 // Batches of independent circuits (batch.cu).
 struct Batch;
 Batch* batch_create(int ncirc, const int32_t* nq, const bf_op* const* ops, const int64_t* nops, int dtype,
@@ -161,5 +168,14 @@ void batch_destroy(Batch* b);
 void batch_stats(const Batch& b, int64_t* tasks, int64_t* passes, uint64_t* state_bytes, int32_t* graph,
                  uint64_t* launches);
 void* batch_stream(const Batch& b);
+
+// Serving loop (server.cpp).
+struct Server;
+Server* server_create(const bf_server_opts& opts);
+uint64_t server_submit(Server& sv, int32_t n, int32_t dtype, const bf_op* ops, int64_t nops);
+int server_poll(Server& sv, bf_result* out, int max);
+bool server_wait_idle(Server& sv, int64_t timeout_ms);
+void server_stats(Server& sv, bf_server_counters& s);
+void server_destroy(Server* sv);
 
 }  // namespace bf

@@ -191,6 +191,49 @@ static DiffArgs diff_args(const State& st, const int32_t* q, int32_t nq) {
   return a;
 }
 
+// classical_oracle (grover.mojo:64-66): negate listed amplitudes, eight per launch
+struct OracleIdx {
+  int32_t count;
+  uint64_t idx[8];
+};
+
+template <class T>
+__global__ void k_negate(T* s, OracleIdx a) {
+  if ((int)threadIdx.x < a.count) {
+    T v = s[a.idx[threadIdx.x]];
+    v.x = -v.x;
+    v.y = -v.y;
+    s[a.idx[threadIdx.x]] = v;
+  }
+}
+
+void launch_classical_oracle(State& st, const double* idx, int64_t count) {
+  for (int64_t k = 0; k < count; k += 8) {
+    OracleIdx a;
+    a.count = (int32_t)std::min<int64_t>(8, count - k);
+    for (int j = 0; j < a.count; ++j) a.idx[j] = (uint64_t)idx[k + j];
+    // a repeated index is negated twice, as in the reference's loop
+    bool dup = false;
+    for (int i = 0; i < a.count; ++i)
+      for (int j = i + 1; j < a.count; ++j) dup |= a.idx[i] == a.idx[j];
+    if (dup) {
+      for (int j = 0; j < a.count; ++j) {
+        OracleIdx one;
+        one.count = 1;
+        one.idx[0] = a.idx[j];
+        if (st.dtype == BF_C128) k_negate<double2><<<1, 32, 0, st.stream>>>(static_cast<double2*>(st.amp), one);
+        else k_negate<float2><<<1, 32, 0, st.stream>>>(static_cast<float2*>(st.amp), one);
+        st.launches++;
+      }
+    } else {
+      if (st.dtype == BF_C128) k_negate<double2><<<1, 32, 0, st.stream>>>(static_cast<double2*>(st.amp), a);
+      else k_negate<float2><<<1, 32, 0, st.stream>>>(static_cast<float2*>(st.amp), a);
+      st.launches++;
+    }
+    BF_CUDA(cudaGetLastError());
+  }
+}
+
 void launch_grover_inversion0(State& st, const int32_t* q, int32_t nq) {
   DiffArgs a = diff_args(st, q, nq);
   unsigned g = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((a.blocks + 255) / 256, (uint64_t)st.num_sms * 16));

@@ -79,6 +79,15 @@ void validate_ops(int n, const bf_op* ops, int64_t nops) {
         }
         break;
       }
+      case BF_OP_CLASSICAL_ORACLE: {
+        if (o.nqubits < 0 || (o.nqubits > 0 && o.data == nullptr)) fail(BF_EINVAL, "oracle index list is null");
+        double N = std::ldexp(1.0, n);
+        for (int64_t k = 0; k < o.nqubits; ++k) {
+          double v = o.data[k];
+          if (!(v >= 0 && v < N) || v != std::floor(v)) fail(BF_EINVAL, "Oracle index out of range: %.17g", v);
+        }
+        break;
+      }
       case BF_OP_MEASURE: {
         if (o.nqubits < 0 || (o.nqubits > 0 && o.qubits == nullptr)) fail(BF_EINVAL, "qubit list is null");
         uint64_t seen = 0;

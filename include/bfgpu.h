@@ -83,8 +83,11 @@ enum {
                           0, 1) or NULL (all free), arg = seed (< 0: clock)   */
   BF_OP_GROVER_DIFFUSER = 9,   /* classical apply_grover_diffuser(qubits; none = all):
                                   x <- 2 mean - x over each target block      */
-  BF_OP_GROVER_INVERSION0 = 10 /* classical apply_grover_inversion_0(qubits; none =
+  BF_OP_GROVER_INVERSION0 = 10, /* classical apply_grover_inversion_0(qubits; none =
                                   all): negate the all-zero target amplitude  */
+  BF_OP_CLASSICAL_ORACLE = 11  /* classical_oracle (grover.mojo:64-66): negate the
+                                  amplitudes at the basis indices data[0..nqubits)
+                                  (integers held exactly as doubles)          */
 };
 
 /* bf_op.flags */
@@ -235,6 +238,52 @@ int bf_batch_stats(bf_batch* b, int64_t* tasks, int64_t* passes,
                    uint64_t* launches);
 int bf_batch_stream(bf_batch* b, void** stream);
 int bf_batch_destroy(bf_batch* b);
+
+/* ---- serving: continuous batching of requests ------------------------------
+ * No counterpart in the reference.  A request is a circuit (bf_op records,
+ * copied at submission) with a qubit count and a dtype; it runs from
+ * |0...0> and returns its top-k outcomes.  `slots` worker threads, each with
+ * its own stream and state, admit the oldest queued request whose
+ * statevector footprint 2^n * (8 | 16) B fits in the HBM budget left by the
+ * running ones; states are allocated and freed stream-ordered, and requests
+ * in different slots overlap on the device. */
+typedef struct bf_server bf_server;
+typedef struct bf_server_opts {
+  int32_t slots;              /* concurrent requests; 0 = 8, at most 64        */
+  int32_t tile_qubits;        /* fusion width; 0 = default                     */
+  int32_t topk;               /* outcomes returned per request, 1..16; 0 = 16 */
+  int32_t reserved;
+  uint64_t hbm_budget_bytes;  /* statevector bytes admitted at once;
+                                 0 = 80 % of the free HBM at creation         */
+} bf_server_opts;
+typedef struct bf_result {
+  uint64_t id;
+  int32_t status;             /* BF_OK or the request's error code             */
+  int32_t num_qubits;
+  int32_t dtype;
+  int32_t slot;
+  int32_t k;
+  int32_t reserved;
+  double t_submit, t_start, t_done;   /* seconds on a monotonic clock          */
+  uint64_t top_index[16];
+  double top_prob[16];
+  char message[128];
+} bf_result;
+typedef struct bf_server_counters {
+  uint64_t submitted, completed, failed, queued, running;
+  uint64_t bytes_in_use, peak_bytes, budget_bytes;
+} bf_server_counters;
+int bf_server_create(const bf_server_opts* opts, bf_server** out);
+/* Queues a request; BF_EBUSY if its state can never fit the budget. */
+int bf_server_submit(bf_server* s, int32_t num_qubits, int32_t dtype,
+                     const bf_op* ops, int64_t nops, uint64_t* request_id);
+/* Moves up to `max` finished results to out (oldest first). */
+int bf_server_poll(bf_server* s, bf_result* out, int32_t max, int32_t* count);
+/* Waits (bounded) until nothing is queued or running: BF_ETIMEDOUT else. */
+int bf_server_wait_idle(bf_server* s, int64_t timeout_ms);
+int bf_server_stats(bf_server* s, bf_server_counters* out);
+/* Finishes the running requests, drops the queued ones, frees everything. */
+int bf_server_destroy(bf_server* s);
 
 /* ---- sum |amp|^2 without allocating ---------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device

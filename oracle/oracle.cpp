@@ -571,6 +571,11 @@ void validate(const St& s, const bf_op* ops, int64_t nops) {
       case BF_OP_GROVER_INVERSION0:
         for (int64_t k = 0; k < o.nqubits; ++k) check_qubit(o.qubits[k], n, "Target");
         break;
+      case BF_OP_CLASSICAL_ORACLE:
+        for (int64_t k = 0; k < o.nqubits; ++k)
+          if (!(o.data[k] >= 0 && o.data[k] < (double)s.N) || o.data[k] != floor(o.data[k]))
+            fail(BF_EINVAL, "Oracle index out of range: %.17g", o.data[k]);
+        break;
       case BF_OP_UNITARY:
       case BF_OP_CUNITARY: {
         int m = o.target2;
@@ -707,6 +712,13 @@ void run(St& s, const Ctx& c, const bf_op* ops, int64_t nops, bool do_validate) 
         }
         break;
       }
+      case BF_OP_CLASSICAL_ORACLE:  // classical_oracle (grover.mojo:64-66)
+        for (int64_t k = 0; k < o.nqubits; ++k) {
+          size_t i = (size_t)o.data[k];
+          s.re[i] = -s.re[i];
+          s.im[i] = -s.im[i];
+        }
+        break;
       case BF_OP_MEASURE: {  // MeasurementTransformation -> apply_measure (:447-553)
         std::vector<int8_t> v;
         for (int64_t k = 0; k < o.nqubits; ++k) v.push_back(o.data ? (int8_t)o.data[k] : (int8_t)-1);
