@@ -34,6 +34,10 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "30q HBM GB/s vs peak; served circuits/s, p50/p99 ms at fidelity≥1-1e-6"
+# DRAM bytes (read + write) of one double-float tile launch per amplitude,
+# from an ncu capture of the same kernel at 26 qubits (2.153 GB / 2^26);
+# traffic grows in proportion to the amplitudes a launch processes.
+TILE_TRAFFIC_BYTES_PER_AMP = 32.08
 N_QUBITS = 30
 LAYERS = 40
 SEED = 0
@@ -201,6 +205,73 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_batch_bench(count: int, reps: int, sample: int) -> dict:
+    """The batched workload: `count` circuits, qubit counts uniform in [8, 20],
+    half random layered (depth 20), half value encodings; one persistent
+    launch per run, replayed from a CUDA graph.  complex64 and complex128
+    (double-float) runs of the same circuits; the infidelity of the complex64
+    outputs against the complex128 ones is checked on a sample."""
+    import torch
+    from code_mojo_gb300 import batch as B
+    from code_mojo_gb300 import opsarray as OA
+    rng = np.random.Generator(np.random.PCG64(7))
+    circs = []
+    for i in range(count):
+        n = int(rng.integers(8, 21))
+        if i % 2 == 0:
+            circs.append(OA.random_layered(n, 20, int(rng.integers(0, 2 ** 31))))
+        else:
+            circs.append(OA.value_encoding(n, float(rng.uniform(0, 2 ** n))))
+    out = {"circuits": count, "qubits": "uniform 8..20", "mix": "half random layered depth 20, half value encoding"}
+    batches = {}
+    for dtype in ("c64", "c128"):
+        b = B.Batch(circs, dtype=dtype)
+        stream = torch.cuda.ExternalStream(b.stream_ptr())
+        b.run()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            b.run(sync=False)
+        e1.record(stream)
+        e1.synchronize()
+        b.sync()
+        ms = e0.elapsed_time(e1) / reps
+        st = b.stats()
+        out[dtype] = {"ms_per_batch": ms, "circuits_per_s": count / (ms * 1e-3), "tasks": st["tasks"],
+                      "passes": st["passes"], "graph": st["graph"], "state_bytes": st["state_bytes"],
+                      "launches_per_batch": 2}
+        batches[dtype] = b
+    idx = rng.choice(count, size=min(sample, count), replace=False)
+    worst = 0.0
+    for c in idx:
+        a = batches["c64"].download(int(c))
+        r = batches["c128"].download(int(c))
+        worst = max(worst, 1 - abs(np.vdot(r, a)) ** 2)
+    out["max_infidelity_c64_vs_c128"] = worst
+    out["infidelity_sample"] = len(idx)
+    out["c64_over_c128_speed"] = out["c64"]["circuits_per_s"] / out["c128"]["circuits_per_s"]
+    for b in batches.values():
+        b.close()
+    return out
+
+
+def run_serving_bench(rate: float, seconds: float, drain: float, slots: int) -> dict:
+    """Poisson arrivals (seeded) of mixed circuits, qubits log-uniform in
+    [10, 28] (Grover, value encoding, random layered depth 10..40), each
+    returning its top-16 outcomes; complex64 and complex128 runs."""
+    from code_mojo_gb300 import serving as SV
+    reqs = SV.request_mix(2000, seed=11)
+    out = {"rate_per_s": rate, "submit_window_s": seconds, "drain_limit_s": drain, "slots": slots,
+           "mix": "Grover / value encoding / random layered, qubits log-uniform 10..28, top-16 returned"}
+    for dtype in ("c64", "c128"):
+        srv = SV.Server(slots=slots)
+        out[dtype] = SV.poisson_run(srv, reqs, rate, seconds, drain, seed=3, dtype=dtype)
+        srv.close()
+    c64, c128 = out["c64"]["circuits_per_s"], out["c128"]["circuits_per_s"]
+    out["c64_over_c128_circuits_per_s"] = c64 / c128 if c128 else None
+    return out
+
+
 def autotune_width(st, qc, candidates) -> tuple[int, dict]:
     """Fusion width: times one layer-block of the circuit at each width and
     keeps the fastest per unit of work."""
@@ -295,6 +366,10 @@ def run_ours(args) -> None:
                "d2h_bytes_per_step": 2 * 8 * N, "ms_per_step": dt * 1e3}
         del hre, him
 
+    batch = run_batch_bench(args.batch_count, 3, 256) if args.batch_count > 0 else None
+    serving = (run_serving_bench(args.serve_rate, args.serve_seconds, args.serve_seconds, 8)
+               if args.serve_seconds > 0 else None)
+
     cpu = None
     if rank == 0 and args.cpu_gates > 0:
         from oracle import pyoracle as O
@@ -322,7 +397,7 @@ def run_ours(args) -> None:
         "per_gate_bytes_per_circuit": pg_bytes,
         "fused_plan": plan,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": "bf::k_tile<bf::PolDF>",
+                     "traffic": TILE_TRAFFIC_BYTES_PER_AMP * (1 << n), "kernel": "bf::k_tile<bf::PolDF>",
                      "bytes_per_launch": 2 * S, "avg_launch_ms": tile_launch_ms, "peak_source": f"{peak_src} hbm_gbs"},
         "autotune": tune,
         "per_gate_path": per_gate,
@@ -331,6 +406,8 @@ def run_ours(args) -> None:
         "clocks": clk.summary(),
         "e2e": e2e,
         "cpu_baseline": cpu,
+        "batch": batch,
+        "serving": serving,
     }
     print(json.dumps(line), flush=True)
     st.close()
@@ -347,6 +424,9 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-gates", type=int, default=45)
     ap.add_argument("--ref-gates", type=int, default=15)
+    ap.add_argument("--batch-count", type=int, default=4096)
+    ap.add_argument("--serve-seconds", type=float, default=10.0)
+    ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--qubits", type=int, default=N_QUBITS,
                     help="state size; anything but 30 is a profiling case, not the benchmark")
     ap.add_argument("--layers", type=int, default=LAYERS,
