@@ -53,13 +53,14 @@ class bf_exec_opts(C.Structure):
         ("specialized", C.c_uint32),
         ("tile_qubits", C.c_int32),
         ("sync", C.c_int32),
-        ("reserved", C.c_int32 * 3),
+        ("renormalize", C.c_int32),
+        ("reserved", C.c_int32 * 2),
     ]
 
 
 class bf_server_opts(C.Structure):
-    _fields_ = [("slots", C.c_int32), ("tile_qubits", C.c_int32), ("topk", C.c_int32), ("reserved", C.c_int32),
-                ("hbm_budget_bytes", C.c_uint64)]
+    _fields_ = [("slots", C.c_int32), ("tile_qubits", C.c_int32), ("topk", C.c_int32), ("large_slots", C.c_int32),
+                ("hbm_budget_bytes", C.c_uint64), ("large_cost", C.c_uint64)]
 
 
 class bf_result(C.Structure):

@@ -387,7 +387,13 @@ void execute_ops(State& st, const bf_op* ops, int64_t nops, bf_exec_opts o) {
   std::vector<Step> steps;
   std::vector<TileOp> prog;
   build_steps(st.n, ops, nops, o, steps, prog);
+  // FP32 matrices are unitary only to ~6e-8, and that error changes the norm
+  // coherently at every gate; the complex64 form restores the input norm.
+  // renormalize == 2 (internal): the input is known to have unit norm.
+  bool renorm = st.dtype == BF_C64 && nops > 0 && o.renormalize >= 0;
+  if (renorm && o.renormalize != 2) launch_norm_before(st);
   run_steps(st, steps, prog);
+  if (renorm) launch_renormalize(st, o.renormalize == 2);
 }
 
 void init_state_runtime(State& st) {

@@ -21,11 +21,18 @@
 
 namespace bf {
 
+// Task kinds: a tile of a pass; for complex64, after a circuit's last pass,
+// a contiguous chunk's sum |amp|^2 (added to the circuit's norm) and then
+// the chunk's rescale to unit norm.
+enum : uint32_t { TASK_TILE = 0, TASK_NORM = 1, TASK_SCALE = 2 };
+
 struct BatchTask {
   uint32_t circuit;
-  uint32_t pass;   // index into the pass table
+  uint32_t pass;   // index into the pass table (its geometry gives the chunk size)
   uint32_t tile;
   uint32_t need;   // tasks of this circuit that must have finished
+  uint32_t kind;
+  uint32_t pad;
 };
 
 struct BatchPass {
@@ -37,6 +44,7 @@ struct BatchPass {
 
 struct BatchDesc {
   void* pool;
+  double* norm;    // per circuit, complex64 renormalisation
   const BatchTask* tasks;
   const BatchPass* passes;
   const TileOp* ops;
@@ -77,9 +85,39 @@ __global__ void __launch_bounds__(kTileThreads) k_batch(const BatchDesc d) {
     __syncthreads();
     if (ok_sh) {
       const BatchPass& bp = d.passes[task.pass];
-      TileGeom geo = bp.geo;
-      run_tile<P, true>(static_cast<typename P::Glob*>(d.pool) + bp.offset, d.ops + bp.op_begin, (int)bp.nops,
-                        geo, task.tile, smem_raw);
+      if (task.kind == TASK_TILE) {
+        TileGeom geo = bp.geo;
+        run_tile<P, true>(static_cast<typename P::Glob*>(d.pool) + bp.offset, d.ops + bp.op_begin, (int)bp.nops,
+                          geo, task.tile, smem_raw);
+      } else if constexpr (sizeof(typename P::Glob) == 8) {
+        float2* base = reinterpret_cast<float2*>(d.pool) + bp.offset + ((uint64_t)task.tile << bp.geo.K);
+        const int cnt = 1 << bp.geo.K;
+        if (task.kind == TASK_NORM) {
+          dfl acc{0.f, 0.f};
+          for (int e = threadIdx.x; e < cnt; e += kTileThreads) {
+            float2 v = __ldcg(base + e);
+            acc = df_add(acc, df_dot2(dfl{v.x, 0.f}, dfl{v.x, 0.f}, dfl{v.y, 0.f}, dfl{v.y, 0.f}));
+          }
+          double* red = reinterpret_cast<double*>(smem_raw);
+          red[threadIdx.x] = (double)acc.hi + (double)acc.lo;
+          __syncthreads();
+          for (int off = kTileThreads / 2; off > 0; off >>= 1) {
+            if ((int)threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
+            __syncthreads();
+          }
+          if (threadIdx.x == 0) atomicAdd(d.norm + task.circuit, red[0]);
+        } else {
+          const double nrm = __ldcg(d.norm + task.circuit);
+          const double f = nrm > 0 ? 1.0 / sqrt(nrm) : 1.0;
+          const float hi = (float)f, lo = (float)(f - (double)hi);
+          for (int e = threadIdx.x; e < cnt; e += kTileThreads) {
+            float2 v = __ldcg(base + e);
+            v.x = fmaf(v.x, hi, v.x * lo);
+            v.y = fmaf(v.y, hi, v.y * lo);
+            base[e] = v;
+          }
+        }
+      }
     }
     __threadfence();  // every thread's stores are visible device-wide ...
     __syncthreads();
@@ -114,6 +152,7 @@ struct Batch {
   TileOp* d_ops = nullptr;
   uint64_t* d_offsets = nullptr;
   unsigned int* d_done = nullptr;
+  double* d_norm = nullptr;
   unsigned long long* d_ticket = nullptr;
   int* d_error = nullptr;
   int* h_error = nullptr;
@@ -132,10 +171,12 @@ static void enqueue_run(Batch& b) {
       static_cast<typename P::Glob*>(b.pool), b.d_offsets, b.ncirc);
   BF_CUDA(cudaGetLastError());
   BF_CUDA(cudaMemsetAsync(b.d_done, 0, b.ncirc * sizeof(unsigned int), b.stream));
+  BF_CUDA(cudaMemsetAsync(b.d_norm, 0, b.ncirc * sizeof(double), b.stream));
   BF_CUDA(cudaMemsetAsync(b.d_ticket, 0, sizeof(unsigned long long), b.stream));
   BF_CUDA(cudaMemsetAsync(b.d_error, 0, sizeof(int), b.stream));
   BatchDesc d;
   d.pool = b.pool;
+  d.norm = b.d_norm;
   d.tasks = b.d_tasks;
   d.passes = b.d_passes;
   d.ops = b.d_ops;
@@ -185,6 +226,7 @@ static void free_batch(Batch* b) {
   cudaFree(b->d_ops);
   cudaFree(b->d_offsets);
   cudaFree(b->d_done);
+  cudaFree(b->d_norm);
   cudaFree(b->d_ticket);
   cudaFree(b->d_error);
   if (b->h_error) cudaFreeHost(b->h_error);
@@ -258,18 +300,22 @@ Batch* batch_create(int ncirc, const int32_t* nq, const bf_op* const* ops, const
       }
     }
     b->pool_amps = off;
-    b->smem = std::max<size_t>(smem, 1024);
+    b->smem = std::max<size_t>(smem, kTileThreads * sizeof(double));  // the norm stage reduces in it
     // tasks, pass-major
     std::vector<BatchTask> tasks;
     size_t max_p = 0;
     for (auto& cp : circ_passes) max_p = std::max(max_p, cp.size());
+    // complex64: two more stages per circuit, norm then rescale
+    const size_t extra = (dtype == BF_C64) ? 2 : 0;
     std::vector<uint32_t> done_before(ncirc, 0);
-    for (size_t p = 0; p < max_p; ++p)
+    for (size_t p = 0; p < max_p + extra; ++p)
       for (int c = 0; c < ncirc; ++c) {
-        if (p >= circ_passes[c].size()) continue;
-        uint32_t pi = circ_passes[c][p];
+        size_t np = circ_passes[c].size();
+        if (np == 0 || p >= np + extra) continue;
+        uint32_t kind = p < np ? TASK_TILE : (p == np ? TASK_NORM : TASK_SCALE);
+        uint32_t pi = circ_passes[c][std::min(p, np - 1)];
         uint32_t tiles = (uint32_t)(1ull << (b->nq[c] - passes[pi].geo.K));
-        for (uint32_t t = 0; t < tiles; ++t) tasks.push_back(BatchTask{(uint32_t)c, pi, t, done_before[c]});
+        for (uint32_t t = 0; t < tiles; ++t) tasks.push_back(BatchTask{(uint32_t)c, pi, t, done_before[c], kind, 0});
         done_before[c] += tiles;
       }
     b->ntasks = tasks.size();
@@ -286,6 +332,8 @@ Batch* batch_create(int ncirc, const int32_t* nq, const bf_op* const* ops, const
     dev_upload(&b->d_offsets, b->offsets);
     std::vector<unsigned int> zeros(ncirc, 0);
     dev_upload(&b->d_done, zeros);
+    std::vector<double> dz(ncirc, 0.0);
+    dev_upload(&b->d_norm, dz);
     std::vector<unsigned long long> z1(1, 0);
     dev_upload(&b->d_ticket, z1);
     std::vector<int> z2(1, 0);

@@ -125,6 +125,9 @@ void launch_set_basis(State& s, uint64_t idx);
 void launch_interleave(State& s, const double* d_re, const double* d_im, uint64_t off, uint64_t cnt);
 void launch_deinterleave(State& s, double* d_re, double* d_im, uint64_t off, uint64_t cnt);
 double reduce_norm2(State& s);
+// complex64: restore the norm measured by launch_norm_before (or 1), stream-ordered
+void launch_norm_before(State& st);
+void launch_renormalize(State& st, bool unit_before);
 void ensure_partials(State& st, size_t blocks);  // 2*blocks doubles, device + pinned host
 void marginal_probs(State& st, const int32_t* q, const int8_t* values, int32_t nq, std::vector<double>& out);
 void measure(State& st, const int32_t* q, const int8_t* values, int32_t nq, int64_t seed, uint64_t* outcome,

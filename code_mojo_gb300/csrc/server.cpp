@@ -38,6 +38,7 @@ struct ServedRequest {
   std::vector<std::vector<double>> data;     // owned copies of op.data
   std::vector<std::vector<int32_t>> qubits;  // owned copies of op.qubits
   double t_submit = 0;
+  bool large = false;
   uint64_t bytes() const { return (1ull << n) * (dtype == BF_C128 ? 16 : 8); }
 };
 
@@ -46,7 +47,8 @@ struct Server {
   int device = 0;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
-  std::deque<ServedRequest*> queue;
+  std::deque<ServedRequest*> queue;        // small requests, oldest first
+  std::deque<ServedRequest*> large_queue;  // large requests, oldest first
   std::vector<bf_result> done;
   uint64_t next_id = 1, bytes_in_use = 0, peak_bytes = 0, budget = 0;
   uint64_t submitted = 0, completed = 0, failed = 0, running = 0;
@@ -112,6 +114,7 @@ static void serve_one(Server& sv, State& st, ServedRequest& r, bf_result& res) {
   o.validate = 1;
   o.specialized = BF_SPEC_ALL;
   o.tile_qubits = sv.opts.tile_qubits;
+  o.renormalize = 2;  // starts from |0...0>: unit norm
   execute_ops(st, r.ops.data(), (int64_t)r.ops.size(), o);
   int k = std::min<int>(sv.opts.topk, (int)std::min<uint64_t>(16, st.N));
   res.k = k;
@@ -129,14 +132,18 @@ static void worker_main(Server* sv, int slot) {
   }
   for (;;) {
     ServedRequest* r = nullptr;
+    const bool large_slot = slot < sv->opts.large_slots;
     {
       std::unique_lock<std::mutex> lk(sv->mu);
-      sv->cv_work.wait(lk, [&]() {
-        return sv->stop || (!sv->queue.empty() && sv->bytes_in_use + sv->queue.front()->bytes() <= sv->budget);
-      });
+      auto fits = [&](const std::deque<ServedRequest*>& q) {
+        return !q.empty() && sv->bytes_in_use + q.front()->bytes() <= sv->budget;
+      };
+      // large slots take large requests first and otherwise help with small ones
+      sv->cv_work.wait(lk, [&]() { return sv->stop || fits(sv->queue) || (large_slot && fits(sv->large_queue)); });
       if (sv->stop) break;
-      r = sv->queue.front();
-      sv->queue.pop_front();
+      std::deque<ServedRequest*>& q = (large_slot && fits(sv->large_queue)) ? sv->large_queue : sv->queue;
+      r = q.front();
+      q.pop_front();
       sv->bytes_in_use += r->bytes();
       sv->peak_bytes = std::max(sv->peak_bytes, sv->bytes_in_use);
       sv->running++;
@@ -180,8 +187,11 @@ static void worker_main(Server* sv, int slot) {
 Server* server_create(const bf_server_opts& opts) {
   auto* sv = new Server();
   sv->opts = opts;
-  if (sv->opts.slots <= 0) sv->opts.slots = 8;
+  if (sv->opts.slots <= 0) sv->opts.slots = 12;
   if (sv->opts.slots > 64) fail(BF_EINVAL, "at most 64 slots");
+  if (sv->opts.large_slots <= 0) sv->opts.large_slots = std::max(1, sv->opts.slots / 4);
+  if (sv->opts.large_slots > sv->opts.slots) fail(BF_EINVAL, "large_slots exceeds slots");
+  if (sv->opts.large_cost == 0) sv->opts.large_cost = 1ull << 28;
   if (sv->opts.topk <= 0) sv->opts.topk = 16;
   if (sv->opts.topk > 16) fail(BF_EINVAL, "topk must be in [1, 16]");
   BF_CUDA(cudaGetDevice(&sv->device));
@@ -209,11 +219,12 @@ uint64_t server_submit(Server& sv, int32_t n, int32_t dtype, const bf_op* ops, i
     delete r;
     fail(BF_EBUSY, "a %d-qubit state needs more than the server's HBM budget", n);
   }
+  r->large = (double)(1ull << n) * (double)std::max<int64_t>(1, nops) > (double)sv.opts.large_cost;
   {
     std::lock_guard<std::mutex> lk(sv.mu);
     r->id = sv.next_id++;
     r->t_submit = now_s();
-    sv.queue.push_back(r);
+    (r->large ? sv.large_queue : sv.queue).push_back(r);
     sv.submitted++;
   }
   sv.cv_work.notify_all();
@@ -231,7 +242,7 @@ int server_poll(Server& sv, bf_result* out, int max) {
 bool server_wait_idle(Server& sv, int64_t timeout_ms) {
   std::unique_lock<std::mutex> lk(sv.mu);
   return sv.cv_done.wait_for(lk, std::chrono::milliseconds(std::max<int64_t>(0, timeout_ms)),
-                             [&]() { return sv.queue.empty() && sv.running == 0; });
+                             [&]() { return sv.queue.empty() && sv.large_queue.empty() && sv.running == 0; });
 }
 
 void server_stats(Server& sv, bf_server_counters& s) {
@@ -239,7 +250,7 @@ void server_stats(Server& sv, bf_server_counters& s) {
   s.submitted = sv.submitted;
   s.completed = sv.completed;
   s.failed = sv.failed;
-  s.queued = sv.queue.size();
+  s.queued = sv.queue.size() + sv.large_queue.size();
   s.running = sv.running;
   s.bytes_in_use = sv.bytes_in_use;
   s.peak_bytes = sv.peak_bytes;
@@ -255,6 +266,7 @@ void server_destroy(Server* sv) {
   sv->cv_work.notify_all();
   for (auto& t : sv->workers) t.join();
   for (auto* r : sv->queue) delete r;
+  for (auto* r : sv->large_queue) delete r;
   delete sv;
 }
 

@@ -160,6 +160,80 @@ double reduce_norm2(State& st) {
   return hi + lo;
 }
 
+// ---- renormalisation (complex64 states) -------------------------------------
+// FP32 gate matrices are unitary only to ~6e-8 and that error changes the
+// norm coherently at every gate, so the complex64 form restores the norm
+// the state had before the circuit: sum |amp|^2 in double-float before and
+// after (k_norm2 partials), one thread forms sqrt(before / after) in FP64 and
+// stores it as an FP32 (hi, lo) pair, and every amplitude is multiplied by
+// hi + lo (x*hi + x*lo with one FMA: unbiased).  All stream-ordered.
+__device__ __forceinline__ double sum_partials(const double* __restrict__ partial, int blocks) {
+  __shared__ double sh[256];
+  double acc = 0;
+  for (int b = threadIdx.x; b < blocks; b += blockDim.x) acc += partial[2 * b] + partial[2 * b + 1];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+    if ((int)threadIdx.x < off) sh[threadIdx.x] += sh[threadIdx.x + off];
+    __syncthreads();
+  }
+  double r = sh[0];
+  __syncthreads();
+  return r;
+}
+
+// before == nullptr: the norm before the circuit is 1
+__global__ void k_norm_factor(const double* __restrict__ before, const double* __restrict__ after, int blocks,
+                              float* __restrict__ factor) {
+  double b = before ? sum_partials(before, blocks) : 1.0;
+  double a = sum_partials(after, blocks);
+  if (threadIdx.x == 0) {
+    double f = (a > 0 && b > 0) ? sqrt(b / a) : 1.0;
+    float hi = (float)f;
+    factor[0] = hi;
+    factor[1] = (float)(f - (double)hi);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_scale_c64(float2* __restrict__ s, uint64_t N, const float* __restrict__ factor) {
+  const float hi = factor[0], lo = factor[1];
+  const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += step) {
+    float2 v = s[i];
+    v.x = fmaf(v.x, hi, v.x * lo);
+    v.y = fmaf(v.y, hi, v.y * lo);
+    s[i] = v;
+  }
+}
+
+static unsigned renorm_blocks(const State& st) {
+  return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((st.N + 255) / 256, (uint64_t)st.num_sms * 8));
+}
+
+// partials layout in st.d_partial: [before: 2*blocks][after: 2*blocks][factor]
+void launch_norm_before(State& st) {
+  if (st.dtype != BF_C64) return;
+  unsigned blocks = renorm_blocks(st);
+  ensure_partials(st, 2 * blocks + 1);
+  k_norm2<float2><<<blocks, 256, 0, st.stream>>>(static_cast<const float2*>(st.amp), st.N, st.d_partial);
+  BF_CUDA(cudaGetLastError());
+  st.launches++;
+}
+
+void launch_renormalize(State& st, bool unit_before) {
+  if (st.dtype != BF_C64) fail(BF_EUNSUPPORTED, "renormalisation is for complex64 states");
+  unsigned blocks = renorm_blocks(st);
+  ensure_partials(st, 2 * blocks + 1);
+  double* before = st.d_partial;
+  double* after = st.d_partial + 2 * blocks;
+  float* factor = reinterpret_cast<float*>(st.d_partial + 4 * blocks);
+  k_norm2<float2><<<blocks, 256, 0, st.stream>>>(static_cast<const float2*>(st.amp), st.N, after);
+  k_norm_factor<<<1, 256, 0, st.stream>>>(unit_before ? nullptr : before, after, (int)blocks, factor);
+  k_scale_c64<<<grid_for(st, st.N), 256, 0, st.stream>>>(static_cast<float2*>(st.amp), st.N, factor);
+  BF_CUDA(cudaGetLastError());
+  st.launches += 3;
+}
+
 // ---- dense m-qubit unitary on contiguous qubits [t, t+m) ------------------
 // apply_unitary / apply_controlled_unitary (transformations_unitary.mojo:
 // 22-139): groups of 2^m amplitudes base + (k << t); out[row] =

@@ -35,8 +35,9 @@ class Result:
 
 
 class Server:
-    def __init__(self, slots: int = 8, topk: int = 16, tile_qubits: int = 0, hbm_budget_bytes: int = 0):
-        o = bf_server_opts(slots, tile_qubits, topk, 0, hbm_budget_bytes)
+    def __init__(self, slots: int = 12, topk: int = 16, tile_qubits: int = 0, hbm_budget_bytes: int = 0,
+                 large_slots: int = 0, large_cost: int = 0):
+        o = bf_server_opts(slots, tile_qubits, topk, large_slots, hbm_budget_bytes, large_cost)
         self._h = C.c_void_p()
         F.check(_lib().bf_server_create(C.byref(o), C.byref(self._h)))
 

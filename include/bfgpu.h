@@ -149,7 +149,11 @@ typedef struct bf_exec_opts {
   uint32_t specialized;      /* BF_SPEC_* mask (default BF_SPEC_ALL)           */
   int32_t tile_qubits;       /* fusion width of a tile pass; 0 = autotuned     */
   int32_t sync;              /* non-zero: block until the work has finished    */
-  int32_t reserved[3];
+  int32_t renormalize;       /* 0 (default): a complex64 state ends with the
+                                norm it had before the circuit (double-float
+                                norms, FP64 factor); -1: never.  complex128
+                                states are never rescaled.                    */
+  int32_t reserved[2];
 } bf_exec_opts;
 
 /* Fills *opts with the defaults above (strategy GPU_FUSED). */
@@ -246,15 +250,19 @@ int bf_batch_destroy(bf_batch* b);
  * its own stream and state, admit the oldest queued request whose
  * statevector footprint 2^n * (8 | 16) B fits in the HBM budget left by the
  * running ones; states are allocated and freed stream-ordered, and requests
- * in different slots overlap on the device. */
+ * in different slots overlap on the device.  Requests whose estimated cost
+ * (2^n * ops) is large wait in their own queue, served by `large_slots`
+ * slots, so they never hold every slot while small requests queue. */
 typedef struct bf_server bf_server;
 typedef struct bf_server_opts {
-  int32_t slots;              /* concurrent requests; 0 = 8, at most 64        */
+  int32_t slots;              /* concurrent requests; 0 = 12, at most 64       */
   int32_t tile_qubits;        /* fusion width; 0 = default                     */
   int32_t topk;               /* outcomes returned per request, 1..16; 0 = 16 */
-  int32_t reserved;
+  int32_t large_slots;        /* slots that run large requests; 0 = slots/4   */
   uint64_t hbm_budget_bytes;  /* statevector bytes admitted at once;
                                  0 = 80 % of the free HBM at creation         */
+  uint64_t large_cost;        /* a request is large when 2^n * ops exceeds
+                                 this; 0 = 2^28                               */
 } bf_server_opts;
 typedef struct bf_result {
   uint64_t id;
