@@ -413,6 +413,7 @@ void release_state_members(State& st) {
   if (st.d_partial) cudaFree(st.d_partial);
   if (st.h_partial) cudaFreeHost(st.h_partial);
   if (st.d_umat) cudaFree(st.d_umat);
+  if (st.d_renorm) cudaFree(st.d_renorm);
   if (st.prog_event) cudaEventDestroy(st.prog_event);
   if (st.stream) cudaStreamDestroy(st.stream);
   st = State();

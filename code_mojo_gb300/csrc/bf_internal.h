@@ -104,6 +104,9 @@ struct State {
   size_t stage_bytes = 0;
   // dense unitary matrix (device copy of the current op's matrix)
   double* d_umat = nullptr;
+  // norms before / after a complex64 circuit and the rescale factor
+  double* d_renorm = nullptr;
+  size_t renorm_cap = 0;
   // reduction partials
   double* d_partial = nullptr;
   double* h_partial = nullptr;

@@ -21,6 +21,7 @@
 namespace bf {
 
 struct DiffArgs {
+  int32_t low;               // 1: the targets are qubits 0..k-1 (index = b << k | t)
   int32_t k;                 // targets
   int8_t tpos[64];           // target positions, ascending
   int32_t nother;
@@ -36,12 +37,17 @@ __device__ __forceinline__ uint64_t deposit_pos(uint64_t x, const int8_t* pos, i
   return r;
 }
 
+__device__ __forceinline__ uint64_t diff_index(const DiffArgs& a, uint64_t b, uint64_t t) {
+  if (a.low) return (b << a.k) | t;
+  return deposit_pos(b, a.opos, a.nother) | deposit_pos(t, a.tpos, a.k);
+}
+
 // negate the amplitudes whose target bits are all zero (sign bits only: exact)
 template <class T>
 __global__ void __launch_bounds__(256) k_inversion0(T* __restrict__ s, uint64_t count, DiffArgs a) {
   const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; b < count; b += step) {
-    uint64_t i = deposit_pos(b, a.opos, a.nother);
+    uint64_t i = diff_index(a, b, 0);
     T v = s[i];
     v.x = -v.x;
     v.y = -v.y;
@@ -66,13 +72,12 @@ __device__ __forceinline__ void amp_df<float2>(float2 g, dfl& re, dfl& im) {
 template <class T>
 __global__ void __launch_bounds__(256) k_diff_sum(const T* __restrict__ s, DiffArgs a, float4* __restrict__ partial) {
   const uint64_t b = blockIdx.x / a.chunks, c = blockIdx.x % a.chunks;
-  const uint64_t base = deposit_pos(b, a.opos, a.nother);
   const uint64_t sub = 1ull << a.k;
   const uint64_t begin = c * a.chunk, end = min(begin + a.chunk, sub);
   dfl sr{0.f, 0.f}, si{0.f, 0.f};
   for (uint64_t t = begin + threadIdx.x; t < end; t += blockDim.x) {
     dfl xr, xi;
-    amp_df<T>(s[base | deposit_pos(t, a.tpos, a.k)], xr, xi);
+    amp_df<T>(s[diff_index(a, b, t)], xr, xi);
     sr = df_add(sr, xr);
     si = df_add(si, xi);
   }
@@ -97,19 +102,36 @@ __global__ void __launch_bounds__(256) k_diff_sum(const T* __restrict__ s, DiffA
   }
 }
 
-// one thread per block: 2 * mean_b in double-float
-__global__ void k_diff_mean(const float4* __restrict__ partial, DiffArgs a, float4* __restrict__ mean2) {
-  const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= a.blocks) return;
+// one CTA per block b: 2 * mean_b in double-float from its chunk partials
+__global__ void __launch_bounds__(256) k_diff_mean(const float4* __restrict__ partial, DiffArgs a,
+                                                   float4* __restrict__ mean2) {
+  const uint64_t b = blockIdx.x;
   dfl r{0.f, 0.f}, im{0.f, 0.f};
-  for (uint32_t c = 0; c < a.chunks; ++c) {
+  for (uint32_t c = threadIdx.x; c < a.chunks; c += blockDim.x) {
     float4 p = partial[b * a.chunks + c];
     r = df_add(r, dfl{p.x, p.y});
     im = df_add(im, dfl{p.z, p.w});
   }
-  // scale by 2 / 2^k: a power of two, exact on both parts
-  const float sc = ldexpf(1.0f, 1 - a.k);
-  mean2[b] = make_float4(r.hi * sc, r.lo * sc, im.hi * sc, im.lo * sc);
+  __shared__ dfl wr[8], wi[8];
+  for (int off = 16; off > 0; off >>= 1) {
+    r = df_add(r, dfl{__shfl_down_sync(0xffffffffu, r.hi, off), __shfl_down_sync(0xffffffffu, r.lo, off)});
+    im = df_add(im, dfl{__shfl_down_sync(0xffffffffu, im.hi, off), __shfl_down_sync(0xffffffffu, im.lo, off)});
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    wr[warp] = r;
+    wi[warp] = im;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+      wr[0] = df_add(wr[0], wr[w]);
+      wi[0] = df_add(wi[0], wi[w]);
+    }
+    // scale by 2 / 2^k: a power of two, exact on both parts
+    const float sc = ldexpf(1.0f, 1 - a.k);
+    mean2[b] = make_float4(wr[0].hi * sc, wr[0].lo * sc, wi[0].hi * sc, wi[0].lo * sc);
+  }
 }
 
 template <class P>
@@ -120,7 +142,7 @@ __global__ void __launch_bounds__(256) k_diff_update(typename P::Glob* __restric
   const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < total; j += step) {
     const uint64_t b = j >> a.k, t = j & (sub - 1);
-    const uint64_t i = deposit_pos(b, a.opos, a.nother) | deposit_pos(t, a.tpos, a.k);
+    const uint64_t i = diff_index(a, b, t);
     const float4 m = mean2[b];
     typename P::R x = P::from_glob(s[i]);
     if constexpr (std::is_same<P, PolDF>::value) {
@@ -188,6 +210,7 @@ static DiffArgs diff_args(const State& st, const int32_t* q, int32_t nq) {
     else a.opos[a.nother++] = (int8_t)b;
   }
   a.blocks = 1ull << a.nother;
+  a.low = (a.k == 0) || (a.tpos[a.k - 1] == a.k - 1);  // ascending: targets are 0..k-1
   return a;
 }
 
@@ -253,8 +276,9 @@ static void diffuser_p(State& st, DiffArgs& a) {
     return;
   }
   const uint64_t sub = 1ull << a.k;
-  uint64_t want = std::max<uint64_t>(1, (uint64_t)st.num_sms * 4 / std::max<uint64_t>(1, a.blocks));
-  a.chunk = std::max<uint64_t>(2048, (sub + want - 1) / want);
+  // short CTAs (16 Ki amplitudes each) so that other streams' kernels get SMs
+  // between them
+  a.chunk = std::min<uint64_t>(sub, 1ull << 14);
   a.chunks = (uint32_t)((sub + a.chunk - 1) / a.chunk);
   uint64_t slots = a.blocks * a.chunks;
   if (slots > 0x7fffffffull) fail(BF_EUNSUPPORTED, "too many diffuser blocks");
@@ -265,8 +289,10 @@ static void diffuser_p(State& st, DiffArgs& a) {
   float4* mean2 = partial + slots;
   auto* s = static_cast<typename P::Glob*>(st.amp);
   k_diff_sum<typename P::Glob><<<(unsigned)slots, 256, 0, st.stream>>>(s, a, partial);
-  k_diff_mean<<<(unsigned)((a.blocks + 255) / 256), 256, 0, st.stream>>>(partial, a, mean2);
-  unsigned g = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((st.N + 255) / 256, (uint64_t)st.num_sms * 16));
+  if (a.blocks > 0x7fffffffull) fail(BF_EUNSUPPORTED, "too many diffuser blocks");
+  k_diff_mean<<<(unsigned)a.blocks, 256, 0, st.stream>>>(partial, a, mean2);
+  // one element per thread: short CTAs
+  unsigned g = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((st.N + 255) / 256, 0x7fffffffull));
   k_diff_update<P><<<g, 256, 0, st.stream>>>(s, a, mean2);
   BF_CUDA(cudaGetLastError());
   st.launches += 3;

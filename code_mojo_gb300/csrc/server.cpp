@@ -127,6 +127,13 @@ static void worker_main(Server* sv, int slot) {
   bool ready = true;
   try {
     init_state_runtime(st);
+    // small-request slots run at the highest stream priority, large-request
+    // slots at the lowest: the block scheduler then hands SMs that free up to
+    // the short requests first
+    int lo = 0, hi = 0;
+    BF_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    BF_CUDA(cudaStreamDestroy(st.stream));
+    BF_CUDA(cudaStreamCreateWithPriority(&st.stream, cudaStreamNonBlocking, slot < sv->opts.large_slots ? lo : hi));
   } catch (const Error&) {
     ready = false;
   }

@@ -210,12 +210,31 @@ static unsigned renorm_blocks(const State& st) {
   return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((st.N + 255) / 256, (uint64_t)st.num_sms * 8));
 }
 
-// partials layout in st.d_partial: [before: 2*blocks][after: 2*blocks][factor]
+// The state's own buffer (not the shared reduction partials, which the
+// circuit's diffusers and measurements reuse in between):
+// [before: 2*blocks][after: 2*blocks][factor]
+static void ensure_renorm(State& st, unsigned blocks) {
+  size_t need = 4 * (size_t)blocks + 2;
+  if (st.renorm_cap >= need) return;
+  if (st.d_renorm) {
+    BF_CUDA(cudaStreamSynchronize(st.stream));
+    cudaFree(st.d_renorm);
+  }
+  st.d_renorm = nullptr;
+  st.renorm_cap = 0;
+  if (cudaMalloc(&st.d_renorm, need * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    st.d_renorm = nullptr;
+    fail(BF_ENOMEM, "cannot allocate the renormalisation buffer");
+  }
+  st.renorm_cap = need;
+}
+
 void launch_norm_before(State& st) {
   if (st.dtype != BF_C64) return;
   unsigned blocks = renorm_blocks(st);
-  ensure_partials(st, 2 * blocks + 1);
-  k_norm2<float2><<<blocks, 256, 0, st.stream>>>(static_cast<const float2*>(st.amp), st.N, st.d_partial);
+  ensure_renorm(st, blocks);
+  k_norm2<float2><<<blocks, 256, 0, st.stream>>>(static_cast<const float2*>(st.amp), st.N, st.d_renorm);
   BF_CUDA(cudaGetLastError());
   st.launches++;
 }
@@ -223,10 +242,10 @@ void launch_norm_before(State& st) {
 void launch_renormalize(State& st, bool unit_before) {
   if (st.dtype != BF_C64) fail(BF_EUNSUPPORTED, "renormalisation is for complex64 states");
   unsigned blocks = renorm_blocks(st);
-  ensure_partials(st, 2 * blocks + 1);
-  double* before = st.d_partial;
-  double* after = st.d_partial + 2 * blocks;
-  float* factor = reinterpret_cast<float*>(st.d_partial + 4 * blocks);
+  ensure_renorm(st, blocks);
+  double* before = st.d_renorm;
+  double* after = st.d_renorm + 2 * blocks;
+  float* factor = reinterpret_cast<float*>(st.d_renorm + 4 * blocks);
   k_norm2<float2><<<blocks, 256, 0, st.stream>>>(static_cast<const float2*>(st.amp), st.N, after);
   k_norm_factor<<<1, 256, 0, st.stream>>>(unit_before ? nullptr : before, after, (int)blocks, factor);
   k_scale_c64<<<grid_for(st, st.N), 256, 0, st.stream>>>(static_cast<float2*>(st.amp), st.N, factor);

@@ -131,6 +131,8 @@ def poisson_run(server: Server, requests, rate: float, duration_s: float, drain_
     wall = time.perf_counter() - t0
     ok = [r for r in results if r.status == 0]
     lat = np.array([r.latency_s for r in ok]) * 1e3
+    svc = np.array([r.latency_s - r.queue_s for r in ok]) * 1e3
+    nq = np.array([r.num_qubits for r in ok])
     st = server.stats()
     return {"dtype": dtype, "rate_per_s": rate, "submitted": len(ids), "completed": len(ok),
             "failed": len(results) - len(ok), "backlog_at_end": int(st["queued"] + st["running"]),
@@ -138,4 +140,7 @@ def poisson_run(server: Server, requests, rate: float, duration_s: float, drain_
             "circuits_per_s": len(ok) / wall if wall > 0 else 0.0,
             "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
             "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
+            "service_p50_ms": float(np.percentile(svc, 50)) if len(svc) else None,
+            "service_p99_ms": float(np.percentile(svc, 99)) if len(svc) else None,
+            "completed_by_qubits": {int(k): int(v) for k, v in zip(*np.unique(nq, return_counts=True))},
             "peak_state_bytes": int(st["peak_bytes"])}
