@@ -42,29 +42,53 @@ static int env_int(const char* name, int dflt) {
   return (v && *v) ? std::atoi(v) : dflt;
 }
 
+// ---- stream-ordered work buffers ------------------------------------------------
+void* dev_alloc(State& st, size_t bytes) {
+  void* p = nullptr;
+  if (cudaMallocAsync(&p, std::max<size_t>(bytes, 256), st.stream) != cudaSuccess) {
+    cudaGetLastError();
+    fail(BF_ENOMEM, "cannot allocate %zu bytes of device work space", bytes);
+  }
+  return p;
+}
+
+void dev_free(State& st, void* p) {
+  if (p) cudaFreeAsync(p, st.stream);
+}
+
+void* host_alloc(size_t bytes) {
+  void* p = nullptr;
+  if (cudaHostAlloc(&p, std::max<size_t>(bytes, 64), cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    fail(BF_ENOMEM, "cannot allocate %zu bytes of pinned host memory", bytes);
+  }
+  return p;
+}
+
+void host_retire(State& st, void* p) {
+  if (p) st.retired_host.push_back(p);
+}
+
 // ---- program buffer for tile ops ---------------------------------------------
+void upload_program_reserve(State& st, size_t ops) {
+  if (ops <= st.prog_cap) return;
+  size_t cap = std::max(ops, st.prog_cap * 2);
+  // copies out of the old pinned buffer may still be in flight: retire it
+  host_retire(st, st.h_prog);
+  st.h_prog = nullptr;
+  dev_free(st, st.d_prog);  // stream-ordered: kernels already queued keep their copy
+  st.d_prog = nullptr;
+  st.prog_cap = 0;
+  st.d_prog = static_cast<TileOp*>(dev_alloc(st, cap * sizeof(TileOp)));
+  st.h_prog = static_cast<TileOp*>(host_alloc(cap * sizeof(TileOp)));
+  st.prog_cap = cap;
+  st.prog_event_live = false;
+}
+
 static void upload_program(State& st, const std::vector<TileOp>& prog) {
   if (prog.empty()) return;
   if (st.prog_event_live) BF_CUDA(cudaEventSynchronize(st.prog_event));
-  if (prog.size() > st.prog_cap) {
-    size_t cap = std::max(prog.size(), st.prog_cap * 2);
-    if (st.d_prog) {
-      BF_CUDA(cudaStreamSynchronize(st.stream));
-      cudaFree(st.d_prog);
-      st.d_prog = nullptr;
-    }
-    if (st.h_prog) {
-      cudaFreeHost(st.h_prog);
-      st.h_prog = nullptr;
-    }
-    st.prog_cap = 0;
-    if (cudaMalloc(&st.d_prog, cap * sizeof(TileOp)) != cudaSuccess ||
-        cudaHostAlloc(&st.h_prog, cap * sizeof(TileOp), cudaHostAllocDefault) != cudaSuccess) {
-      cudaGetLastError();
-      fail(BF_ENOMEM, "cannot allocate the tile program buffer (%zu ops)", cap);
-    }
-    st.prog_cap = cap;
-  }
+  upload_program_reserve(st, prog.size());
   std::memcpy(st.h_prog, prog.data(), prog.size() * sizeof(TileOp));
   BF_CUDA(cudaMemcpyAsync(st.d_prog, st.h_prog, prog.size() * sizeof(TileOp), cudaMemcpyHostToDevice, st.stream));
   BF_CUDA(cudaEventRecord(st.prog_event, st.stream));
@@ -404,16 +428,19 @@ void init_state_runtime(State& st) {
 }
 
 void release_state_members(State& st) {
-  if (st.stream) cudaStreamSynchronize(st.stream);
+  if (st.stream) {
+    dev_free(st, st.d_prog);
+    dev_free(st, st.d_partial);
+    dev_free(st, st.d_renorm);
+    cudaStreamSynchronize(st.stream);
+  }
   if (st.amp) cudaFree(st.amp);
   if (st.scratch) cudaFree(st.scratch);
-  if (st.d_prog) cudaFree(st.d_prog);
   if (st.h_prog) cudaFreeHost(st.h_prog);
   if (st.d_stage) cudaFree(st.d_stage);
-  if (st.d_partial) cudaFree(st.d_partial);
   if (st.h_partial) cudaFreeHost(st.h_partial);
   if (st.d_umat) cudaFree(st.d_umat);
-  if (st.d_renorm) cudaFree(st.d_renorm);
+  for (void* p : st.retired_host) cudaFreeHost(p);
   if (st.prog_event) cudaEventDestroy(st.prog_event);
   if (st.stream) cudaStreamDestroy(st.stream);
   st = State();

@@ -112,9 +112,23 @@ struct State {
   double* h_partial = nullptr;
   size_t partial_cap = 0;
 
+  // pinned host buffers outgrown while copies from them may be in flight;
+  // freed with the state (cudaFreeHost can synchronise the device)
+  std::vector<void*> retired_host;
+
   size_t amp_bytes() const { return dtype == BF_C128 ? 16 : 8; }
   size_t bytes() const { return (size_t)N * amp_bytes(); }
 };
+
+// Work buffers of a state are (re)allocated stream-ordered on its own stream
+// (cudaMallocAsync / cudaFreeAsync) so that growing one never waits for
+// kernels of other states; pinned host buffers that are outgrown are retired
+// until the state is released.
+void* dev_alloc(State& st, size_t bytes);   // throws BF_ENOMEM
+void dev_free(State& st, void* p);
+void* host_alloc(size_t bytes);             // pinned; throws BF_ENOMEM
+void host_retire(State& st, void* p);
+void upload_program_reserve(State& st, size_t ops);
 
 // ---------------------------------------------------------------------------
 // Kernel launchers (device code lives in the .cu files).

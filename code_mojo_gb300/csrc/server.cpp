@@ -134,6 +134,10 @@ static void worker_main(Server* sv, int slot) {
     BF_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
     BF_CUDA(cudaStreamDestroy(st.stream));
     BF_CUDA(cudaStreamCreateWithPriority(&st.stream, cudaStreamNonBlocking, slot < sv->opts.large_slots ? lo : hi));
+    // size the work buffers for the typical request up front
+    upload_program_reserve(st, 16384);
+    ensure_partials(st, 1 << 15);
+    BF_CUDA(cudaStreamSynchronize(st.stream));
   } catch (const Error&) {
     ready = false;
   }

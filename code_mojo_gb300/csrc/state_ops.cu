@@ -127,16 +127,14 @@ __global__ void __launch_bounds__(256) k_norm2(const T* __restrict__ s, uint64_t
 
 void ensure_partials(State& st, size_t blocks) {
   if (st.partial_cap >= blocks) return;
-  if (st.d_partial) cudaFree(st.d_partial);
-  if (st.h_partial) cudaFreeHost(st.h_partial);
+  blocks = std::max(blocks, 2 * st.partial_cap);
+  dev_free(st, st.d_partial);
+  host_retire(st, st.h_partial);
   st.d_partial = nullptr;
   st.h_partial = nullptr;
   st.partial_cap = 0;
-  if (cudaMalloc(&st.d_partial, 2 * blocks * sizeof(double)) != cudaSuccess ||
-      cudaHostAlloc(&st.h_partial, 2 * blocks * sizeof(double), cudaHostAllocDefault) != cudaSuccess) {
-    cudaGetLastError();
-    fail(BF_ENOMEM, "cannot allocate reduction partials");
-  }
+  st.d_partial = static_cast<double*>(dev_alloc(st, 2 * blocks * sizeof(double)));
+  st.h_partial = static_cast<double*>(host_alloc(2 * blocks * sizeof(double)));
   st.partial_cap = blocks;
 }
 
@@ -216,17 +214,10 @@ static unsigned renorm_blocks(const State& st) {
 static void ensure_renorm(State& st, unsigned blocks) {
   size_t need = 4 * (size_t)blocks + 2;
   if (st.renorm_cap >= need) return;
-  if (st.d_renorm) {
-    BF_CUDA(cudaStreamSynchronize(st.stream));
-    cudaFree(st.d_renorm);
-  }
+  dev_free(st, st.d_renorm);
   st.d_renorm = nullptr;
   st.renorm_cap = 0;
-  if (cudaMalloc(&st.d_renorm, need * sizeof(double)) != cudaSuccess) {
-    cudaGetLastError();
-    st.d_renorm = nullptr;
-    fail(BF_ENOMEM, "cannot allocate the renormalisation buffer");
-  }
+  st.d_renorm = static_cast<double*>(dev_alloc(st, need * sizeof(double)));
   st.renorm_cap = need;
 }
 
