@@ -367,7 +367,7 @@ def run_ours(args) -> None:
         del hre, him
 
     batch = run_batch_bench(args.batch_count, 3, 256) if args.batch_count > 0 else None
-    serving = (run_serving_bench(args.serve_rate, args.serve_seconds, args.serve_seconds, 8)
+    serving = (run_serving_bench(args.serve_rate, args.serve_seconds, args.serve_seconds, 12)
                if args.serve_seconds > 0 else None)
 
     cpu = None

@@ -54,7 +54,8 @@ class bf_exec_opts(C.Structure):
         ("tile_qubits", C.c_int32),
         ("sync", C.c_int32),
         ("renormalize", C.c_int32),
-        ("reserved", C.c_int32 * 2),
+        ("tensor_blocks", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 

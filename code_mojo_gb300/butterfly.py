@@ -64,6 +64,7 @@ class ExecContext:
         self.validate_circuit = True
         self.execution_strategy = ExecutionStrategy.GPU_FUSED
         self.gpu_tile_qubits = 0     # fusion width of a tile pass (0 = default)
+        self.gpu_tensor_blocks = False  # complex64: 5-qubit blocks as 3xTF32 tensor-core GEMMs
         self.gpu_sync = True         # block until the device has finished
 
     def copy(self) -> "ExecContext":
@@ -627,6 +628,7 @@ def exec_opts(ctx: ExecContext) -> F.bf_exec_opts:
     o.specialized = ctx.specialized_mask()
     o.tile_qubits = ctx.gpu_tile_qubits
     o.sync = 1 if ctx.gpu_sync else 0
+    o.tensor_blocks = 1 if ctx.gpu_tensor_blocks else 0
     return o
 
 

@@ -69,6 +69,32 @@ void host_retire(State& st, void* p) {
   if (p) st.retired_host.push_back(p);
 }
 
+int* state_flag(State& st) {
+  if (!st.d_flag) {
+    st.d_flag = static_cast<int*>(dev_alloc(st, 16));
+    st.h_flag = static_cast<int*>(host_alloc(16));
+    *st.h_flag = 0;
+    BF_CUDA(cudaMemsetAsync(st.d_flag, 0, 16, st.stream));
+  }
+  st.flag_used = true;
+  return st.d_flag;
+}
+
+void flag_readback(State& st) {
+  if (!st.flag_used) return;
+  BF_CUDA(cudaMemcpyAsync(st.h_flag, st.d_flag, sizeof(int), cudaMemcpyDeviceToHost, st.stream));
+  st.flag_used = false;
+}
+
+void sync_state(State& st) {
+  BF_CUDA(cudaStreamSynchronize(st.stream));
+  if (st.h_flag && *st.h_flag) {
+    *st.h_flag = 0;
+    BF_CUDA(cudaMemsetAsync(st.d_flag, 0, sizeof(int), st.stream));
+    fail(BF_ETIMEDOUT, "a bounded wait on the device expired; the state's contents are undefined");
+  }
+}
+
 // ---- program buffer for tile ops ---------------------------------------------
 void upload_program_reserve(State& st, size_t ops) {
   if (ops <= st.prog_cap) return;
@@ -85,12 +111,42 @@ void upload_program_reserve(State& st, size_t ops) {
   st.prog_event_live = false;
 }
 
-static void upload_program(State& st, const std::vector<TileOp>& prog) {
-  if (prog.empty()) return;
+// Everything a plan uploads: tile ops, and for tensor-core passes the block
+// descriptors followed (at a 256-byte boundary) by their matrix images.
+struct Program {
+  std::vector<TileOp> ops;
+  std::vector<Blk5> blocks;
+  std::vector<unsigned char> images;
+  size_t images_offset() const { return (blocks.size() * sizeof(Blk5) + 255) & ~(size_t)255; }
+  size_t aux_bytes() const { return blocks.empty() ? 0 : images_offset() + images.size(); }
+};
+
+static void upload_program(State& st, const Program& pg) {
+  const std::vector<TileOp>& prog = pg.ops;
+  const size_t aux = pg.aux_bytes();
+  if (prog.empty() && aux == 0) return;
   if (st.prog_event_live) BF_CUDA(cudaEventSynchronize(st.prog_event));
-  upload_program_reserve(st, prog.size());
-  std::memcpy(st.h_prog, prog.data(), prog.size() * sizeof(TileOp));
-  BF_CUDA(cudaMemcpyAsync(st.d_prog, st.h_prog, prog.size() * sizeof(TileOp), cudaMemcpyHostToDevice, st.stream));
+  if (!prog.empty()) {
+    upload_program_reserve(st, prog.size());
+    std::memcpy(st.h_prog, prog.data(), prog.size() * sizeof(TileOp));
+    BF_CUDA(cudaMemcpyAsync(st.d_prog, st.h_prog, prog.size() * sizeof(TileOp), cudaMemcpyHostToDevice, st.stream));
+  }
+  if (aux) {
+    if (aux > st.aux_cap) {
+      size_t cap = std::max(aux, 2 * st.aux_cap);
+      host_retire(st, st.h_aux);
+      dev_free(st, st.d_aux);
+      st.h_aux = nullptr;
+      st.d_aux = nullptr;
+      st.aux_cap = 0;
+      st.d_aux = static_cast<unsigned char*>(dev_alloc(st, cap));
+      st.h_aux = static_cast<unsigned char*>(host_alloc(cap));
+      st.aux_cap = cap;
+    }
+    std::memcpy(st.h_aux, pg.blocks.data(), pg.blocks.size() * sizeof(Blk5));
+    std::memcpy(st.h_aux + pg.images_offset(), pg.images.data(), pg.images.size());
+    BF_CUDA(cudaMemcpyAsync(st.d_aux, st.h_aux, aux, cudaMemcpyHostToDevice, st.stream));
+  }
   BF_CUDA(cudaEventRecord(st.prog_event, st.stream));
   st.prog_event_live = true;
 }
@@ -98,7 +154,7 @@ static void upload_program(State& st, const std::vector<TileOp>& prog) {
 // ---- execution -------------------------------------------------------------
 // A step is one launch (or a launch group) in op order.
 struct Step {
-  enum Kind { GATE, TILE, BITREV, PERMUTE, SWAPBITS, UNITARY, MEASURE, DIFFUSER, INVERSION0, ORACLE } kind;
+  enum Kind { GATE, TILE, TBLOCK, BITREV, PERMUTE, SWAPBITS, UNITARY, MEASURE, DIFFUSER, INVERSION0, ORACLE, GROVER_LOOP } kind;
   GateInstr gate;
   TilePass tile;            // ops moved into the program; tile.ops emptied
   size_t prog_off = 0;
@@ -110,7 +166,40 @@ struct Step {
   std::vector<int32_t> mq;   // measured qubits
   std::vector<int8_t> mv;    // their values (-1 free)
   int64_t seed = -1;
+  std::vector<uint64_t> marked;  // Grover loop: indices the oracle negates
+  int reps = 0;                  // Grover loop: iterations
+  size_t blk_off = 0;            // tensor-core pass: its blocks in the program
+  int nblk = 0;
 };
+
+// Grover loop detection: the number of consecutive (classical oracle with
+// the same index list, diffuser over every qubit) pairs starting at ops[i],
+// or 0 when the oracle's odd-multiplicity indices exceed the loop's limit.
+static bool full_diffuser(int n, const bf_op& o) {
+  if (o.kind != BF_OP_GROVER_DIFFUSER) return false;
+  if (o.nqubits == 0) return true;
+  if (o.nqubits != n || !o.qubits) return false;
+  uint64_t seen = 0;
+  for (int k = 0; k < n; ++k) {
+    int q = o.qubits[k];
+    if (q < 0 || q >= n || ((seen >> q) & 1)) return false;
+    seen |= 1ull << q;
+  }
+  return true;
+}
+
+static int64_t grover_loop_reps(int n, const bf_op* ops, int64_t nops, int64_t i) {
+  const bf_op& o = ops[i];
+  if (o.nqubits < 0 || o.nqubits > grover_loop_max_marked() || (o.nqubits > 0 && !o.data)) return 0;
+  int64_t reps = 0;
+  for (int64_t j = i; j + 1 < nops; j += 2) {
+    const bf_op& a = ops[j];
+    if (a.kind != BF_OP_CLASSICAL_ORACLE || a.nqubits != o.nqubits || !full_diffuser(n, ops[j + 1])) break;
+    if (o.nqubits > 0 && (!a.data || std::memcmp(a.data, o.data, (size_t)o.nqubits * sizeof(double)) != 0)) break;
+    ++reps;
+  }
+  return reps;
+}
 
 static bool is_h(const bf_op& o) { return o.ncontrols == 0 && o.gate == BF_GATE_H; }
 static bool is_p(const bf_op& o) { return o.ncontrols == 0 && o.gate == BF_GATE_P; }
@@ -189,15 +278,37 @@ static void fused_pair_matrix(const bf_op& t0, const bf_op& t1, int& q_low, std:
     }
 }
 
+// Grover loops run for states of up to kLoopAlwaysQubits qubits, and for
+// larger ones only when grover_loop_large (a server slot keeps long searches
+// as short per-op kernels so that other requests get SMs between them).
+constexpr int kLoopAlwaysQubits = 22;
+
+// tensor: complex64 tile passes as tensor-core block passes (12-qubit tiles)
 static void build_steps(int n, const bf_op* ops, int64_t nops, const bf_exec_opts& o, std::vector<Step>& steps,
-                        std::vector<TileOp>& prog) {
+                        Program& pg, bool grover_loop_large = true, bool tensor = false) {
+  std::vector<TileOp>& prog = pg.ops;
   const bool fused = o.strategy == BF_STRATEGY_GPU_FUSED;
-  const int K = o.tile_qubits > 0 ? o.tile_qubits : 11;
+  tensor = tensor && fused && n >= kBlockTileQubits;
+  const int K = tensor ? kBlockTileQubits : (o.tile_qubits > 0 ? o.tile_qubits : 11);
   std::vector<GateInstr> run;
   auto flush = [&]() {
     if (run.empty()) return;
     for (auto& ps : plan_gates(n, run, K)) {
       Step s;
+      if (ps.is_tile && tensor && ps.tile.K == kBlockTileQubits && ps.tile.L == kTileLowQubits) {
+        size_t b0 = pg.blocks.size(), i0 = pg.images.size();
+        if (plan_blocks(ps.tile, pg.blocks, pg.images)) {
+          s.kind = Step::TBLOCK;
+          s.tile = ps.tile;
+          s.tile.ops.clear();
+          s.blk_off = b0;
+          s.nblk = (int)(pg.blocks.size() - b0);
+          steps.push_back(std::move(s));
+          continue;
+        }
+        pg.blocks.resize(b0);
+        pg.images.resize(i0);
+      }
       if (ps.is_tile) {
         s.kind = Step::TILE;
         s.tile = ps.tile;
@@ -349,6 +460,25 @@ static void build_steps(int n, const bf_op* ops, int64_t nops, const bf_exec_opt
       }
       case BF_OP_CLASSICAL_ORACLE: {  // classical_oracle (grover.mojo:64-66)
         flush();
+        int64_t reps = grover_loop_reps(n, ops, nops, i);
+        if (reps >= 2 && (grover_loop_large || n <= kLoopAlwaysQubits)) {
+          // repeated (oracle, full diffuser) iterations: one cooperative loop
+          std::vector<uint64_t> idx;
+          for (int64_t k = 0; k < op.nqubits; ++k) idx.push_back((uint64_t)op.data[k]);
+          std::sort(idx.begin(), idx.end());
+          Step s;
+          s.kind = Step::GROVER_LOOP;
+          for (size_t k = 0; k < idx.size();) {  // an index listed twice is negated twice
+            size_t e = k;
+            while (e < idx.size() && idx[e] == idx[k]) ++e;
+            if ((e - k) & 1) s.marked.push_back(idx[k]);
+            k = e;
+          }
+          s.reps = (int)reps;
+          steps.push_back(std::move(s));
+          i += 2 * reps - 1;
+          break;
+        }
         Step s;
         s.kind = Step::ORACLE;
         s.u.assign(op.data, op.data + op.nqubits);
@@ -377,12 +507,16 @@ static void build_steps(int n, const bf_op* ops, int64_t nops, const bf_exec_opt
   flush();
 }
 
-static void run_steps(State& st, std::vector<Step>& steps, const std::vector<TileOp>& prog) {
-  upload_program(st, prog);
+static void run_steps(State& st, std::vector<Step>& steps, const Program& pg) {
+  upload_program(st, pg);
   for (auto& s : steps) {
     switch (s.kind) {
       case Step::GATE: launch_gate(st, s.gate); break;
       case Step::TILE: launch_tile_pass(st, st.d_prog + s.prog_off, s.nprog, s.tile); break;
+      case Step::TBLOCK:
+        launch_block_pass(st, reinterpret_cast<const Blk5*>(st.d_aux) + s.blk_off, s.nblk,
+                          st.d_aux + pg.images_offset(), s.tile);
+        break;
       case Step::BITREV: launch_bitrev_full(st); break;
       case Step::PERMUTE: launch_permute(st, s.src_of.data()); break;
       case Step::SWAPBITS: launch_swap_bits(st, s.a, s.b); break;
@@ -393,6 +527,7 @@ static void run_steps(State& st, std::vector<Step>& steps, const std::vector<Til
       case Step::DIFFUSER: launch_grover_diffuser(st, s.mq.data(), (int32_t)s.mq.size()); break;
       case Step::INVERSION0: launch_grover_inversion0(st, s.mq.data(), (int32_t)s.mq.size()); break;
       case Step::ORACLE: launch_classical_oracle(st, s.u.data(), (int64_t)s.u.size()); break;
+      case Step::GROVER_LOOP: launch_grover_loop(st, s.marked.data(), (int)s.marked.size(), s.reps); break;
     }
   }
 }
@@ -409,8 +544,8 @@ void execute_ops(State& st, const bf_op* ops, int64_t nops, bf_exec_opts o) {
   if (o.tile_qubits == 0) o.tile_qubits = env_int("BFGPU_TILE_QUBITS", default_tile_qubits(st));
   if (o.validate) validate_ops(st.n, ops, nops);
   std::vector<Step> steps;
-  std::vector<TileOp> prog;
-  build_steps(st.n, ops, nops, o, steps, prog);
+  Program prog;
+  build_steps(st.n, ops, nops, o, steps, prog, st.coop_ctas == 0, o.tensor_blocks != 0 && st.dtype == BF_C64);
   // FP32 matrices are unitary only to ~6e-8, and that error changes the norm
   // coherently at every gate; the complex64 form restores the input norm.
   // renormalize == 2 (internal): the input is known to have unit norm.
@@ -418,6 +553,7 @@ void execute_ops(State& st, const bf_op* ops, int64_t nops, bf_exec_opts o) {
   if (renorm && o.renormalize != 2) launch_norm_before(st);
   run_steps(st, steps, prog);
   if (renorm) launch_renormalize(st, o.renormalize == 2);
+  flag_readback(st);
 }
 
 void init_state_runtime(State& st) {
@@ -432,6 +568,8 @@ void release_state_members(State& st) {
     dev_free(st, st.d_prog);
     dev_free(st, st.d_partial);
     dev_free(st, st.d_renorm);
+    dev_free(st, st.d_flag);
+    dev_free(st, st.d_aux);
     cudaStreamSynchronize(st.stream);
   }
   if (st.amp) cudaFree(st.amp);
@@ -439,6 +577,8 @@ void release_state_members(State& st) {
   if (st.h_prog) cudaFreeHost(st.h_prog);
   if (st.d_stage) cudaFree(st.d_stage);
   if (st.h_partial) cudaFreeHost(st.h_partial);
+  if (st.h_flag) cudaFreeHost(st.h_flag);
+  if (st.h_aux) cudaFreeHost(st.h_aux);
   if (st.d_umat) cudaFree(st.d_umat);
   for (void* p : st.retired_host) cudaFreeHost(p);
   if (st.prog_event) cudaEventDestroy(st.prog_event);
@@ -586,7 +726,7 @@ int bf_state_download_range(bf_state* hst, uint64_t offset, uint64_t count, doub
       BF_CUDA(cudaMemcpyAsync(re + done, d_re, cnt * sizeof(double), cudaMemcpyDeviceToHost, st->stream));
       BF_CUDA(cudaMemcpyAsync(im + done, d_im, cnt * sizeof(double), cudaMemcpyDeviceToHost, st->stream));
     }
-    BF_CUDA(cudaStreamSynchronize(st->stream));
+    sync_state(*st);
   });
 }
 
@@ -603,7 +743,7 @@ int bf_state_sync(bf_state* hst) {
   State* st = S_(hst);
   return guarded([&]() {
     if (!st) fail(BF_EINVAL, "state is null");
-    BF_CUDA(cudaStreamSynchronize(st->stream));
+    sync_state(*st);
   });
 }
 
@@ -632,7 +772,7 @@ int bf_execute(bf_state* hst, const bf_op* ops, int64_t nops, const bf_exec_opts
     if (opts) o = *opts;
     else bf_exec_opts_init(&o);
     execute_ops(*st, ops, nops, o);
-    if (o.sync) BF_CUDA(cudaStreamSynchronize(st->stream));
+    if (o.sync) sync_state(*st);
   });
 }
 
@@ -798,17 +938,20 @@ int bf_plan_stats(int32_t n, const bf_op* ops, int64_t nops, const bf_exec_opts*
     if (o.tile_qubits <= 0) o.tile_qubits = 11;
     if (o.validate) validate_ops(n, ops, nops);
     std::vector<Step> steps;
-    std::vector<TileOp> prog;
-    build_steps(n, ops, nops, o, steps, prog);
+    Program prog;
+    build_steps(n, ops, nops, o, steps, prog, true, o.tensor_blocks != 0);
     int64_t t = 0, g = 0, x = 0;
     double bytes = 0;
     for (auto& s : steps) {
-      if (s.kind == Step::TILE) {
+      if (s.kind == Step::TILE || s.kind == Step::TBLOCK) {
         ++t;
         bytes += 2.0;
       } else if (s.kind == Step::GATE) {
         ++g;
         bytes += gate_bytes_fraction(s.gate);
+      } else if (s.kind == Step::GROVER_LOOP) {
+        ++x;
+        bytes += 2.0 * (s.reps + 1);
       } else {
         ++x;
         bytes += (s.kind == Step::SWAPBITS) ? 1.0

@@ -81,6 +81,31 @@ struct TilePass {
 };
 
 // ---------------------------------------------------------------------------
+// Tensor-core block passes (complex64): a 12-qubit tile whose gates are
+// grouped into blocks of 5 tile qubits, each applied as one 32x32 complex
+// matrix.  A block's matrix may depend on up to 3 qubits outside the tile
+// (controls, or targets of diagonal gates); its 2^nout variants are stored
+// consecutively, variant v for outside bits (bit k of v = qubit outpos[k]).
+constexpr int kBlockTileQubits = 12;
+constexpr uint32_t kBlockImageBytes = 32768;  // one matrix: TF32 hi and lo parts, swizzled
+
+struct Blk5 {
+  uint32_t tmask;     // the block's 5 local positions (bits of the 12-bit tile index)
+  int32_t nout;
+  int32_t outpos[3];
+  uint32_t img;       // image index of variant 0
+};
+
+// Partitions the ops of a 12-qubit tile pass into blocks and appends their
+// matrix images; false when an op cannot be placed (more than 5 tile qubits
+// or more than 3 outside qubits on its own).
+bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsigned char>& images);
+// The matrix image of a 32x32 complex matrix u (row-major, interleaved
+// re/im): the real 64x64 operand R^T, split into TF32 hi and lo parts, in
+// the swizzled K-major layout of the block kernel.
+void block_image(const double* u, unsigned char* img);
+
+// ---------------------------------------------------------------------------
 // The device state.
 struct State {
   int32_t n = 0;
@@ -111,6 +136,17 @@ struct State {
   double* d_partial = nullptr;
   double* h_partial = nullptr;
   size_t partial_cap = 0;
+  // error flag of kernels with bounded waits (device word, pinned copy)
+  int* d_flag = nullptr;
+  int* h_flag = nullptr;
+  bool flag_used = false;
+  // CTA cap of cooperative loops (0: sized for the whole GPU)
+  int32_t coop_ctas = 0;
+  // block descriptors and matrix images of tensor-core passes (device) and
+  // their pinned staging; uploaded with the tile program
+  unsigned char* d_aux = nullptr;
+  unsigned char* h_aux = nullptr;
+  size_t aux_cap = 0;
 
   // pinned host buffers outgrown while copies from them may be in flight;
   // freed with the state (cudaFreeHost can synchronise the device)
@@ -129,11 +165,20 @@ void dev_free(State& st, void* p);
 void* host_alloc(size_t bytes);             // pinned; throws BF_ENOMEM
 void host_retire(State& st, void* p);
 void upload_program_reserve(State& st, size_t ops);
+// The state's device error flag (allocated and zeroed on first use); kernels
+// with bounded waits set it.  flag_readback queues its copy to the host after
+// such kernels; sync_state synchronises the stream and throws BF_ETIMEDOUT
+// (clearing the flag) when a wait had expired.
+int* state_flag(State& st);
+void flag_readback(State& st);
+void sync_state(State& st);
 
 // ---------------------------------------------------------------------------
 // Kernel launchers (device code lives in the .cu files).
 void launch_gate(State& s, const GateInstr& g);
 void launch_tile_pass(State& s, const TileOp* d_ops, int nops, const TilePass& p);
+void launch_block_pass(State& st, const Blk5* d_blocks, int nblocks, const unsigned char* d_images,
+                       const TilePass& p);
 void launch_bitrev_full(State& s);
 void launch_permute(State& s, const int32_t* src_bit_of_dst);  // dst bit j <- src bit perm[j]
 void launch_swap_bits(State& s, int a, int b);
@@ -153,6 +198,9 @@ void probs_topk(State& st, int k, uint64_t* idx, double* probs);
 void launch_grover_inversion0(State& st, const int32_t* q, int32_t nq);
 void launch_grover_diffuser(State& st, const int32_t* q, int32_t nq);
 void launch_classical_oracle(State& st, const double* idx, int64_t count);
+// iters x (negate marked[0..nmarked), diffuser over every qubit) in one launch
+void launch_grover_loop(State& st, const uint64_t* marked, int nmarked, int iters);
+int grover_loop_max_marked();
 // sum |amp|^2 of caller memory with the library's static scratch (noalloc.cu)
 void norm2_noalloc(const void* d_amps, uint64_t num_amps, int32_t dtype, double* d_out, cudaStream_t stream);
 

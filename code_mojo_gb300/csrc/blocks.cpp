@@ -1,0 +1,166 @@
+// blocks.cpp — host side of the tensor-core block passes: groups the gates of
+// a 12-qubit tile pass into 5-qubit blocks and builds each block's 32x32
+// matrix, split and laid out for the kernel in tblock.cu.
+//
+// This is the GPU form of the reference's dense fusion
+// (fuse_contiguous_target_pairs, transformations_fusion.mojo:539-876: runs
+// of gates on neighbouring qubits multiplied into one 2^m x 2^m unitary on
+// the host and applied by apply_unitary, transformations_unitary.mojo:22-75),
+// widened to any 5 qubits of the tile and to gates that are not adjacent in
+// the op list.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <vector>
+
+#include "bf_internal.h"
+
+namespace bf {
+
+using cd = std::complex<double>;
+
+static float tf32_round_host(float x) {
+  uint32_t u;
+  std::memcpy(&u, &x, 4);
+  u = (u + 0x1000u) & 0xFFFFE000u;
+  std::memcpy(&x, &u, 4);
+  return x;
+}
+
+// byte offset of element (row n, column k) of a 64 x 64 FP32 K-major operand
+// stored as two 128-byte-wide spans (k < 32, k >= 32) of 8 KiB, the 16-byte
+// chunks of each 128-byte row swizzled by the row's low three bits
+static size_t image_off(int n, int k) {
+  return (size_t)(k >> 5) * 8192 + (size_t)n * 128 + (size_t)((((k & 31) >> 2) ^ (n & 7)) << 4) + (size_t)((k & 3) << 2);
+}
+
+// out_j = sum_l u[j][l] x_l on interleaved (re, im) vectors is the real
+// product out = x R with R[2l+c][2j+d]:
+//   R[2l][2j] = Re u[j][l]   R[2l+1][2j] = -Im u[j][l]
+//   R[2l][2j+1] = Im u[j][l] R[2l+1][2j+1] = Re u[j][l]
+// The kernel's B operand is R^T (rows n = output column, K-major).
+void block_image(const double* u, unsigned char* img) {
+  std::memset(img, 0, kBlockImageBytes);
+  for (int n = 0; n < 64; ++n)
+    for (int k = 0; k < 64; ++k) {
+      const int j = n >> 1, d = n & 1, l = k >> 1, c = k & 1;
+      const double re = u[2 * (j * 32 + l)], im = u[2 * (j * 32 + l) + 1];
+      const double v = c == 0 ? (d == 0 ? re : im) : (d == 0 ? -im : re);
+      const float big = tf32_round_host((float)v);
+      const float small = tf32_round_host((float)(v - (double)big));
+      std::memcpy(img + image_off(n, k), &big, 4);
+      std::memcpy(img + 16384 + image_off(n, k), &small, 4);
+    }
+}
+
+namespace {
+
+struct BlockBuild {
+  uint32_t qset = 0;   // local positions used by its ops
+  uint64_t outs = 0;   // outside qubits its ops depend on
+  std::vector<const TileOp*> ops;
+};
+
+uint32_t local_set(const TileOp& t) { return t.cmask_loc | (t.tloc >= 0 ? (1u << t.tloc) : 0u); }
+uint64_t outside_set(const TileOp& t) { return t.cmask_out | (t.tloc < 0 ? (1ull << t.tglob) : 0ull); }
+
+}  // namespace
+
+bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsigned char>& images) {
+  if (tp.K != kBlockTileQubits) return false;
+  std::vector<BlockBuild> bl;
+  // Each op goes into the earliest block at or after the last block that
+  // shares a tile qubit with it (everything after that block acts on other
+  // tile qubits, and gates on disjoint tile qubits commute for a fixed
+  // assignment of the outside qubits), if the block stays within 5 tile
+  // qubits and 3 outside qubits; otherwise into a new block at the end.
+  for (const TileOp& t : tp.ops) {
+    const uint32_t Q = local_set(t);
+    const uint64_t O = outside_set(t);
+    if (__builtin_popcount(Q) > 5 || __builtin_popcountll(O) > 3) return false;
+    int last = -1;
+    for (int b = 0; b < (int)bl.size(); ++b)
+      if (bl[b].qset & Q) last = b;
+    int place = -1;
+    for (int b = std::max(last, 0); b < (int)bl.size(); ++b)
+      if (__builtin_popcount(bl[b].qset | Q) <= 5 && __builtin_popcountll(bl[b].outs | O) <= 3) {
+        place = b;
+        break;
+      }
+    if (place < 0) {
+      bl.emplace_back();
+      place = (int)bl.size() - 1;
+    }
+    bl[place].qset |= Q;
+    bl[place].outs |= O;
+    bl[place].ops.push_back(&t);
+  }
+
+  for (auto& b : bl) {
+    // pad to exactly 5 positions with unused tile qubits (identity on them)
+    uint32_t T = b.qset;
+    for (int pos = 0; pos < kBlockTileQubits && __builtin_popcount(T) < 5; ++pos) T |= 1u << pos;
+    int rank_of[kBlockTileQubits];
+    int r = 0;
+    for (int pos = 0; pos < kBlockTileQubits; ++pos) rank_of[pos] = ((T >> pos) & 1u) ? r++ : -1;
+    Blk5 d;
+    std::memset(&d, 0, sizeof d);
+    d.tmask = T;
+    for (int q = 0; q < 64; ++q)
+      if ((b.outs >> q) & 1ull) d.outpos[d.nout++] = q;
+    d.img = (uint32_t)(images.size() / kBlockImageBytes);
+    const int variants = 1 << d.nout;
+    std::vector<cd> U(32 * 32);
+    std::vector<double> flat(2 * 32 * 32);
+    for (int v = 0; v < variants; ++v) {
+      std::fill(U.begin(), U.end(), cd(0.0, 0.0));
+      for (int i = 0; i < 32; ++i) U[i * 32 + i] = cd(1.0, 0.0);
+      auto out_bit = [&](int q) {
+        for (int k = 0; k < d.nout; ++k)
+          if (d.outpos[k] == q) return (v >> k) & 1;
+        return 0;
+      };
+      for (const TileOp* t : b.ops) {
+        bool active = true;  // outside controls all set in this variant
+        for (int q = 0; q < 64; ++q)
+          if (((t->cmask_out >> q) & 1ull) && !out_bit(q)) active = false;
+        if (!active) continue;
+        uint32_t cb = 0;
+        for (int pos = 0; pos < kBlockTileQubits; ++pos)
+          if ((t->cmask_loc >> pos) & 1u) cb |= 1u << rank_of[pos];
+        const double* m = t->m;
+        if (t->tloc < 0) {  // diagonal gate on an outside target: one entry for the variant
+          const cd e = out_bit(t->tglob) ? cd(m[6], m[7]) : cd(m[0], m[1]);
+          for (int row = 0; row < 32; ++row)
+            if ((row & cb) == cb)
+              for (int c = 0; c < 32; ++c) U[row * 32 + c] *= e;
+          continue;
+        }
+        const int tb = rank_of[t->tloc];
+        const cd m00(m[0], m[1]), m01(m[2], m[3]), m10(m[4], m[5]), m11(m[6], m[7]);
+        for (int r0 = 0; r0 < 32; ++r0) {
+          if ((r0 >> tb) & 1) continue;
+          if ((r0 & cb) != cb) continue;
+          const int r1 = r0 | (1 << tb);
+          for (int c = 0; c < 32; ++c) {
+            const cd x0 = U[r0 * 32 + c], x1 = U[r1 * 32 + c];
+            U[r0 * 32 + c] = m00 * x0 + m01 * x1;
+            U[r1 * 32 + c] = m10 * x0 + m11 * x1;
+          }
+        }
+      }
+      for (int i = 0; i < 32 * 32; ++i) {
+        flat[2 * i] = U[i].real();
+        flat[2 * i + 1] = U[i].imag();
+      }
+      size_t at = images.size();
+      images.resize(at + kBlockImageBytes);
+      block_image(flat.data(), images.data() + at);
+    }
+    blocks.push_back(d);
+  }
+  return true;
+}
+
+}  // namespace bf

@@ -167,7 +167,7 @@ void marginal_probs(State& st, const int32_t* q, const int8_t* values, int32_t n
   st.launches++;
   BF_CUDA(cudaMemcpyAsync(st.h_partial, st.d_partial, 2 * slots * sizeof(double), cudaMemcpyDeviceToHost,
                           st.stream));
-  BF_CUDA(cudaStreamSynchronize(st.stream));
+  sync_state(st);
   out.assign(outcomes, 0.0);
   for (uint64_t o = 0; o < outcomes; ++o) {
     double hi = 0, lo = 0;
@@ -338,7 +338,7 @@ void probs_topk(State& st, int k, uint64_t* idx, double* probs) {
   st.launches++;
   std::vector<Cand> h((size_t)blocks * k);
   BF_CUDA(cudaMemcpyAsync(h.data(), d, need, cudaMemcpyDeviceToHost, st.stream));
-  BF_CUDA(cudaStreamSynchronize(st.stream));
+  sync_state(st);
   std::sort(h.begin(), h.end(), [](const Cand& a, const Cand& b) {
     double pa = (double)a.hi + (double)a.lo, pb = (double)b.hi + (double)b.lo;
     if (pa != pb) return pa > pb;

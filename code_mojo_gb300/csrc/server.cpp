@@ -127,6 +127,8 @@ static void worker_main(Server* sv, int slot) {
   bool ready = true;
   try {
     init_state_runtime(st);
+    // a slot's cooperative loops take a quarter of the SMs at most
+    st.coop_ctas = std::max(8, st.num_sms / 4);
     // small-request slots run at the highest stream priority, large-request
     // slots at the lowest: the block scheduler then hands SMs that free up to
     // the short requests first

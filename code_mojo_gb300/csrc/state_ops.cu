@@ -149,7 +149,7 @@ double reduce_norm2(State& st) {
   st.launches++;
   BF_CUDA(cudaMemcpyAsync(st.h_partial, st.d_partial, 2 * blocks * sizeof(double), cudaMemcpyDeviceToHost,
                           st.stream));
-  BF_CUDA(cudaStreamSynchronize(st.stream));
+  sync_state(st);
   double hi = 0, lo = 0;
   for (unsigned b = 0; b < blocks; ++b) {
     hi += st.h_partial[2 * b];

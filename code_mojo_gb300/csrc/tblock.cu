@@ -1,0 +1,427 @@
+// tblock.cu — complex64 tile passes whose gates are fused into 5-qubit
+// blocks (32x32 complex unitaries) applied on the tensor cores.
+//
+// The reference fuses neighbouring gates into dense 2^m x 2^m unitaries and
+// applies them by gather -> matrix-vector -> scatter
+// (transformations_fusion.mojo:539-876, transformations_unitary.mojo:22-75).
+// Here a CTA holds a 12-qubit tile (4096 amplitudes) and applies a sequence
+// of 5-qubit blocks whose qubits are all tile qubits.  For one block the tile
+// is a 128 x 32 complex matrix X (rows: the 7 other tile qubits; columns:
+// the block's 5 qubits) and the block is X <- X U^T, i.e. as a real GEMM
+//   D[128 x 64] = A[128 x 64] * R[64 x 64],   A = X with (re, im) interleaved,
+// R[2l+c][2j+d] built from U[j][l].  It runs as tcgen05.mma kind::tf32
+// (M=128, N=64, K=8 per instruction) with FP32 accumulation in tensor
+// memory, in 3xTF32 form: A = Ab + As and R = Rb + Rs with Ab, Rb rounded
+// to TF32 and As, Rs the rounded remainders, D = As*Rb + Ab*Rs + Ab*Rb
+// (the As*Rs term is below FP32 resolution).  Relative error per block is
+// about 2^-22, against 2^-11 for plain TF32.
+//
+// Per tile: coalesced 16-byte loads -> split into the two A operands in
+// shared memory (K-major, 128-byte swizzle) -> per block: one thread issues
+// 24 MMAs and commits them to an mbarrier, the epilogue reads D from tensor
+// memory (tcgen05.ld 32x32b), and writes it either as the next block's A
+// operands (a bit permutation of the tile index) or, after the last block,
+// into a staging copy of the tile -> coalesced 16-byte stores.  The block
+// matrices (pre-split and pre-swizzled on the host, 32 KiB each) stream in
+// with cp.async.bulk behind the MMAs of the previous block.  Gates with
+// controls (or diagonal targets) outside the tile select one of up to 8
+// precomputed variants of their block's matrix from the CTA's fixed
+// outside bits.
+//
+// Every wait is bounded: on expiry the CTA sets the state's error flag,
+// waits (bounded) for its own copy in flight, frees its tensor memory and
+// returns.
+#include <algorithm>
+#include <cstring>
+
+#include "amp_math.cuh"
+#include "bf_internal.h"
+
+namespace bf {
+
+constexpr int kBlkThreads = 256;
+constexpr uint32_t kAOpBytes = 128 * 64 * 4;  // 32 KiB: 128 rows x 64 FP32
+constexpr uint32_t kSmemA0 = 0;               // Ab
+constexpr uint32_t kSmemA1 = kAOpBytes;       // As
+constexpr uint32_t kSmemB = 2 * kAOpBytes;    // Rb (2 x 8 KiB), Rs (2 x 8 KiB)
+constexpr uint32_t kSmemTab = kSmemB + kBlockImageBytes;
+constexpr uint32_t kTabWords = 288;           // ext_lo 64, ext_hi 64, dep_g 128, dep_j 32
+constexpr uint32_t kSmemHoff = kSmemTab + 2 * kTabWords * 4;
+constexpr uint32_t kSmemBar = kSmemHoff + 128 * 8;
+constexpr uint32_t kSmemUsed = kSmemBar + 32;
+constexpr uint32_t kSmemAlloc = kSmemUsed + 1024;  // slack for 1024-byte alignment
+constexpr uint32_t kTmemCols = 64;
+
+struct BlkPassArgs {
+  float2* s;
+  const Blk5* blocks;
+  const unsigned char* images;  // kBlockImageBytes per image, 16-byte aligned
+  uint64_t ntiles;
+  int32_t nblocks;
+  int32_t q[kBlockTileQubits];  // tile qubits; q[j] = j for j < 5
+  int* flag;
+  uint32_t spin_limit;
+};
+
+// ---- PTX wrappers ------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait for the phase with parity `parity`; false when it expired
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint32_t limit) {
+  for (uint32_t i = 0; i < limit; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (i > 64) __nanosleep(32);
+  }
+  return false;
+}
+
+// one 32 KiB block image: global -> shared, completing on `bar`
+__device__ __forceinline__ void load_image(uint32_t dst, const void* src, uint32_t bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(kBlockImageBytes)
+               : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(kBlockImageBytes), "r"(bar)
+               : "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor (tcgen05): K-major operand with the
+// 128-byte swizzle; 8-row core-matrix groups 1024 bytes apart.
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+// 32 lanes x 32 consecutive FP32 columns: thread `lane` of the warp gets
+// row (32 * (warp % 4) + lane), columns col..col+31
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// ---- operand layout ----------------------------------------------------------
+// TF32 rounding to nearest (ties away from zero) of an FP32 value: the tensor
+// cores read the top 19 bits of each operand.
+__device__ __forceinline__ float tf32_round(float x) {
+  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+}
+
+// Byte offset of complex element (row g, column j) inside an A operand: the
+// real part at k = 2j, the imaginary part at k = 2j + 1, K-major rows of
+// 64 FP32 split into two 128-byte spans of 16 KiB each, 16-byte chunks
+// swizzled by the row's low three bits.
+__device__ __forceinline__ uint32_t a_off(uint32_t g, uint32_t j) {
+  return ((j >> 4) << 14) + (g << 7) + (((((j & 15) >> 1)) ^ (g & 7)) << 4) + ((j & 1) << 3);
+}
+
+__device__ __forceinline__ void put_split(unsigned char* sm, uint32_t off, float re, float im) {
+  const float rb = tf32_round(re), ib = tf32_round(im);
+  *reinterpret_cast<float2*>(sm + kSmemA0 + off) = make_float2(rb, ib);
+  *reinterpret_cast<float2*>(sm + kSmemA1 + off) = make_float2(tf32_round(re - rb), tf32_round(im - ib));
+}
+
+// staging slot of tile element i (pairs stay together; spreads banks when
+// the epilogue's lanes walk the tile at a power-of-two stride)
+__device__ __forceinline__ uint32_t stage_slot(uint32_t i) { return i ^ (((i >> 5) & 15u) << 1); }
+
+// Index tables of one block (target mask T over the 12 local bits):
+//   ext_lo[x], ext_hi[y]: (g | j << 8) contributions of local bits 0..5 / 6..11
+//   dep_g[g], dep_j[j]:   local index bits of row g / column j
+__device__ __forceinline__ void build_tables(uint32_t* tab, uint32_t T) {
+  const uint32_t G = ~T & 0xFFFu;
+  const int glo = __popc(G & 63u), jlo = __popc(T & 63u);
+  for (int e = threadIdx.x; e < (int)kTabWords; e += kBlkThreads) {
+    uint32_t v = 0;
+    if (e < 128) {
+      const int x = e & 63;
+      const int base = (e < 64) ? 0 : 6;
+      uint32_t g = 0, j = 0;
+      int gr = (e < 64) ? 0 : glo, jr = (e < 64) ? 0 : jlo;
+      for (int b = 0; b < 6; ++b) {
+        const int pos = base + b;
+        const uint32_t bit = (x >> b) & 1u;
+        if ((G >> pos) & 1u) g |= bit << gr++;
+        else j |= bit << jr++;
+      }
+      v = g | (j << 8);
+    } else if (e < 256) {
+      const uint32_t g = e - 128;
+      int r = 0;
+      for (int pos = 0; pos < 12; ++pos)
+        if ((G >> pos) & 1u) v |= ((g >> r++) & 1u) << pos;
+    } else {
+      const uint32_t j = e - 256;
+      int r = 0;
+      for (int pos = 0; pos < 12; ++pos)
+        if ((T >> pos) & 1u) v |= ((j >> r++) & 1u) << pos;
+    }
+    tab[e] = v;
+  }
+}
+
+__device__ __forceinline__ uint32_t variant_of(const Blk5& b, uint64_t obase) {
+  uint32_t v = 0;
+  for (int k = 0; k < b.nout; ++k) v |= (uint32_t)((obase >> b.outpos[k]) & 1ull) << k;
+  return v;
+}
+
+__global__ void __launch_bounds__(kBlkThreads, 2) k_tblock(const BlkPassArgs a) {
+  extern __shared__ unsigned char smem_raw[];
+  // 1024-byte alignment for the swizzled operands
+  unsigned char* sm = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+  uint32_t* tabs = reinterpret_cast<uint32_t*>(sm + kSmemTab);
+  uint64_t* hoff = reinterpret_cast<uint64_t*>(sm + kSmemHoff);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + kSmemBar);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + kSmemBar + 16);
+  int* ok_slot = reinterpret_cast<int*>(sm + kSmemBar + 20);
+  const uint32_t bar_b = smem_u32(&bars[0]), bar_mma = smem_u32(&bars[1]);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 32) {
+    mbar_init(bar_b, 1);
+    mbar_init(bar_mma, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  for (int h = tid; h < 128; h += kBlkThreads) {  // local bits 5..11 -> global offsets
+    uint64_t off = 0;
+    for (int j = 0; j < 7; ++j)
+      if ((h >> j) & 1) off |= 1ull << a.q[5 + j];
+    hoff[h] = off;
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  // this warp's rows and columns of D
+  const uint32_t row = 32u * (warp & 3) + lane;
+  const uint32_t colh = (uint32_t)(warp >> 2);  // columns 32*colh .. +31
+  const uint32_t taddr = tmem + ((32u * (warp & 3)) << 16) + 32u * colh;
+
+  // instruction descriptor: D FP32, A and B TF32, both K-major, N = 64, M = 128
+  const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+  const uint32_t sA0 = smem_u32(sm + kSmemA0), sA1 = smem_u32(sm + kSmemA1), sB = smem_u32(sm + kSmemB);
+
+  uint32_t ph_b = 0, ph_mma = 0;
+  bool b_in_flight = false;     // thread 0: an image copy has not been waited for
+  int mma_lost_phase = -1;      // thread 0: MMAs whose completion wait expired
+  bool failed = false;
+
+  auto tile_base = [&](uint64_t tile) {
+    uint64_t ob = tile;
+    for (int j = 0; j < kBlockTileQubits; ++j) ob = insert_zero_bit(ob, a.q[j]);
+    return ob;
+  };
+
+  uint64_t tile = blockIdx.x;
+  if (tid == 0 && tile < a.ntiles) {
+    const Blk5& b0 = a.blocks[0];
+    load_image(sB, a.images + (size_t)(b0.img + variant_of(b0, tile_base(tile))) * kBlockImageBytes, bar_b);
+    b_in_flight = true;
+  }
+
+  for (; tile < a.ntiles && !failed; tile += gridDim.x) {
+    const uint64_t obase = tile_base(tile);
+    build_tables(tabs, a.blocks[0].tmask);
+    __syncthreads();
+    // load: 8 x 16 bytes per thread, split into the block-0 operands
+#pragma unroll 4
+    for (int it = 0; it < 8; ++it) {
+      const uint32_t i0 = (uint32_t)(it * kBlkThreads + tid) * 2u;
+      const uint64_t gi = obase | (i0 & 31u) | hoff[i0 >> 5];
+      const float4 v = __ldcs(reinterpret_cast<const float4*>(a.s + gi));
+      uint32_t t = tabs[i0 & 63u] + tabs[64 + (i0 >> 6)];
+      put_split(sm, a_off(t & 0xFFu, t >> 8), v.x, v.y);
+      t = tabs[(i0 + 1) & 63u] + tabs[64 + ((i0 + 1) >> 6)];
+      put_split(sm, a_off(t & 0xFFu, t >> 8), v.z, v.w);
+    }
+    fence_proxy_async();
+    __syncthreads();
+
+    for (int bi = 0; bi < a.nblocks; ++bi) {
+      const uint32_t* cur = tabs + (bi & 1) * kTabWords;
+      uint32_t* nxt = tabs + ((bi + 1) & 1) * kTabWords;
+      const bool more = bi + 1 < a.nblocks;
+      if (more) build_tables(nxt, a.blocks[bi + 1].tmask);
+      if (tid == 0) {
+        int ok = mbar_wait(bar_b, ph_b, a.spin_limit) ? 1 : 0;
+        if (ok) {
+          b_in_flight = false;
+          tc_fence_after();
+          uint32_t acc = 0;
+          // small products first: As*Rb, Ab*Rs, then Ab*Rb
+#pragma unroll
+          for (int pass = 0; pass < 3; ++pass) {
+            const uint32_t abase = pass == 0 ? sA1 : sA0;
+            const uint32_t bbase = pass == 1 ? sB + 16384u : sB;
+#pragma unroll
+            for (int s = 0; s < 8; ++s) {
+              const uint64_t ad = sdesc(abase + (uint32_t)(s >> 2) * 16384u + (uint32_t)(s & 3) * 32u);
+              const uint64_t bd = sdesc(bbase + (uint32_t)(s >> 2) * 8192u + (uint32_t)(s & 3) * 32u);
+              mma_tf32(tmem, ad, bd, idesc, acc);
+              acc = 1;
+            }
+          }
+          mma_commit(bar_mma);
+          ok = mbar_wait(bar_mma, ph_mma, a.spin_limit) ? 1 : 0;
+          if (!ok) mma_lost_phase = (int)ph_mma;
+        }
+        if (!ok) atomicExch(a.flag, 1);
+        *ok_slot = ok;
+        // the B buffer is free once the MMAs are done: fetch the next image
+        if (ok) {
+          const Blk5* nb = nullptr;
+          uint64_t nbase = obase;
+          if (more) {
+            nb = &a.blocks[bi + 1];
+          } else if (tile + gridDim.x < a.ntiles) {
+            nb = &a.blocks[0];
+            nbase = tile_base(tile + gridDim.x);
+          }
+          if (nb) {
+            load_image(sB, a.images + (size_t)(nb->img + variant_of(*nb, nbase)) * kBlockImageBytes, bar_b);
+            b_in_flight = true;
+          }
+        }
+      }
+      ph_b ^= 1u;
+      ph_mma ^= 1u;
+      __syncthreads();
+      if (!*ok_slot) {
+        failed = true;
+        break;
+      }
+      tc_fence_after();
+      float d[32];
+      tmem_ld32(taddr, d);
+      const uint32_t gpart = cur[128 + row];
+      if (more) {
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+          const uint32_t i = gpart | cur[256 + 16u * colh + c];
+          const uint32_t t = nxt[i & 63u] + nxt[64 + (i >> 6)];
+          put_split(sm, a_off(t & 0xFFu, t >> 8), d[2 * c], d[2 * c + 1]);
+        }
+        fence_proxy_async();
+      } else {
+        float2* stage = reinterpret_cast<float2*>(sm + kSmemA0);
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+          const uint32_t i = gpart | cur[256 + 16u * colh + c];
+          stage[stage_slot(i)] = make_float2(d[2 * c], d[2 * c + 1]);
+        }
+      }
+      tc_fence_before();
+      __syncthreads();
+    }
+    if (failed) break;
+    // store the staged tile: 8 x 16 bytes per thread
+    const float2* stage = reinterpret_cast<const float2*>(sm + kSmemA0);
+#pragma unroll 4
+    for (int it = 0; it < 8; ++it) {
+      const uint32_t i0 = (uint32_t)(it * kBlkThreads + tid) * 2u;
+      const uint64_t gi = obase | (i0 & 31u) | hoff[i0 >> 5];
+      const float4 v = *reinterpret_cast<const float4*>(stage + stage_slot(i0));
+      __stcs(reinterpret_cast<float4*>(a.s + gi), v);
+    }
+    __syncthreads();
+  }
+
+  // nothing of ours may be in flight when the tensor memory is freed
+  if (tid == 0) {
+    if (b_in_flight && !mbar_wait(bar_b, ph_b, a.spin_limit)) atomicExch(a.flag, 1);
+    if (mma_lost_phase >= 0 && !mbar_wait(bar_mma, (uint32_t)mma_lost_phase, a.spin_limit)) atomicExch(a.flag, 1);
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+}
+
+void launch_block_pass(State& st, const Blk5* d_blocks, int nblocks, const unsigned char* d_images,
+                       const TilePass& p) {
+  if (st.dtype != BF_C64) fail(BF_EINVAL, "internal: tensor-core blocks need a complex64 state");
+  if (p.K != kBlockTileQubits || st.n < kBlockTileQubits) fail(BF_EINVAL, "internal: block pass needs a 12-qubit tile");
+  if (nblocks < 1) fail(BF_EINVAL, "internal: empty block pass");
+  if (((uintptr_t)d_images & 15u) != 0) fail(BF_EINVAL, "internal: block images must be 16-byte aligned");
+  BlkPassArgs a;
+  std::memset(&a, 0, sizeof a);
+  for (int j = 0; j < kBlockTileQubits; ++j) {
+    a.q[j] = p.q[j];
+    if (j < 5 && p.q[j] != j) fail(BF_EINVAL, "internal: block tile must hold qubits 0..4");
+  }
+  a.s = static_cast<float2*>(st.amp);
+  a.blocks = d_blocks;
+  a.images = d_images;
+  a.nblocks = nblocks;
+  a.ntiles = st.N >> kBlockTileQubits;
+  a.flag = state_flag(st);
+  a.spin_limit = 1u << 24;
+  static bool configured = false;
+  if (!configured) {
+    BF_CUDA(cudaFuncSetAttribute(k_tblock, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemAlloc));
+    // the whole L1/shared split as shared memory: two CTAs per SM
+    BF_CUDA(cudaFuncSetAttribute(k_tblock, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    configured = true;
+  }
+  int per_sm = 0;
+  BF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tblock, kBlkThreads, kSmemAlloc));
+  per_sm = std::max(1, std::min(per_sm, 2));
+  uint64_t grid = std::min<uint64_t>(a.ntiles, (uint64_t)per_sm * st.num_sms);
+  k_tblock<<<(unsigned)grid, kBlkThreads, kSmemAlloc, st.stream>>>(a);
+  BF_CUDA(cudaGetLastError());
+  st.launches++;
+}
+
+}  // namespace bf

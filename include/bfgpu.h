@@ -153,7 +153,11 @@ typedef struct bf_exec_opts {
                                 norm it had before the circuit (double-float
                                 norms, FP64 factor); -1: never.  complex128
                                 states are never rescaled.                    */
-  int32_t reserved[2];
+  int32_t tensor_blocks;     /* non-zero: complex64 tile passes group their
+                                gates into 5-qubit blocks applied as 3xTF32
+                                tensor-core GEMMs (states of >= 12 qubits;
+                                ignored for complex128)                       */
+  int32_t reserved;
 } bf_exec_opts;
 
 /* Fills *opts with the defaults above (strategy GPU_FUSED). */
