@@ -272,6 +272,63 @@ def run_serving_bench(rate: float, seconds: float, drain: float, slots: int) -> 
     return out
 
 
+def run_precision_bench(n_big: int, n_cmp: int, layers: int) -> dict:
+    """complex64 at n_big qubits: the layered circuit and a QFT with the gates
+    fused into 5-qubit blocks on the tensor cores (3xTF32) against the
+    CUDA-core FP32 tile passes; infidelity 1 - |<psi64|psi32>|^2 of the
+    tensor-core result against the complex128 (FP64 storage) run of the same
+    circuits at n_cmp qubits."""
+    from code_mojo_gb300 import butterfly as bfy
+    from code_mojo_gb300 import workloads as W
+
+    def ctx(tensor):
+        c = bfy.ExecContext()
+        c.execution_strategy = bfy.ExecutionStrategy.GPU_FUSED
+        c.gpu_tensor_blocks = tensor
+        c.gpu_tile_qubits = 12
+        return c
+
+    def timed(st, qc, c):
+        t0 = time.perf_counter()
+        bfy.execute(st, qc, c)  # synchronous
+        return (time.perf_counter() - t0) * 1e3
+
+    out = {"qubits": n_big, "layers": layers, "state_bytes": 8 << n_big,
+           "workload": f"random layered circuit ({layers} layers) then QFT, complex64, from |0>"}
+    # warm-up of both kernels on a small state
+    w = bfy.QuantumState(16, "c64")
+    for t in (True, False):
+        bfy.execute(w, W.random_layered_circuit(16, 2, 0), ctx(t))
+    w.close()
+    qc, qft = W.random_layered_circuit(n_big, layers, SEED), W.qft_circuit(n_big)
+    st = bfy.QuantumState(n_big, "c64")
+    for name, t in (("tensor_cores", True), ("cuda_cores", False)):
+        st.set_basis(0)
+        lay = timed(st, qc, ctx(t))
+        q = timed(st, qft, ctx(t))
+        out[name] = {"layered_ms": lay, "qft_ms": q, "plan_layered": bfy.plan_stats(qc, ctx(t)),
+                     "plan_qft": bfy.plan_stats(qft, ctx(t))}
+    st.close()
+    out["tensor_over_cuda_core_speed"] = ((out["cuda_cores"]["layered_ms"] + out["cuda_cores"]["qft_ms"]) /
+                                          (out["tensor_cores"]["layered_ms"] + out["tensor_cores"]["qft_ms"]))
+    # fidelity at n_cmp qubits against complex128
+    qc, qft = W.random_layered_circuit(n_cmp, layers, SEED), W.qft_circuit(n_cmp)
+    ref = bfy.QuantumState(n_cmp, "c128")
+    t128 = timed(ref, qc, ctx(False)) + timed(ref, qft, ctx(False))
+    inf = {}
+    for name, t in (("tensor_cores", True), ("cuda_cores", False)):
+        s32 = bfy.QuantumState(n_cmp, "c64")
+        bfy.execute(s32, qc, ctx(t))
+        bfy.execute(s32, qft, ctx(t))
+        ip = ref.inner(s32)
+        inf[name] = 1.0 - abs(ip) ** 2 / (ref.norm2() * s32.norm2())
+        s32.close()
+    ref.close()
+    out["infidelity_vs_complex128"] = {"qubits": n_cmp, **inf}
+    out["complex128_ms_at_cmp_qubits"] = t128
+    return out
+
+
 def autotune_width(st, qc, candidates) -> tuple[int, dict]:
     """Fusion width: times one layer-block of the circuit at each width and
     keeps the fastest per unit of work."""
@@ -369,6 +426,8 @@ def run_ours(args) -> None:
     batch = run_batch_bench(args.batch_count, 3, 256) if args.batch_count > 0 else None
     serving = (run_serving_bench(args.serve_rate, args.serve_seconds, args.serve_seconds, 12)
                if args.serve_seconds > 0 else None)
+    precision = (run_precision_bench(args.precision_qubits, args.precision_qubits - 1, LAYERS)
+                 if args.precision_qubits > 0 and rank == 0 else None)
 
     cpu = None
     if rank == 0 and args.cpu_gates > 0:
@@ -408,6 +467,7 @@ def run_ours(args) -> None:
         "cpu_baseline": cpu,
         "batch": batch,
         "serving": serving,
+        "precision": precision,
     }
     print(json.dumps(line), flush=True)
     st.close()
@@ -427,6 +487,8 @@ def main():
     ap.add_argument("--batch-count", type=int, default=4096)
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--serve-rate", type=float, default=2000.0)
+    ap.add_argument("--precision-qubits", type=int, default=33,
+                    help="complex64 tensor-core vs CUDA-core run at this size (0: skip); fidelity at one qubit less")
     ap.add_argument("--qubits", type=int, default=N_QUBITS,
                     help="state size; anything but 30 is a profiling case, not the benchmark")
     ap.add_argument("--layers", type=int, default=LAYERS,

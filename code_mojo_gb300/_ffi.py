@@ -104,6 +104,7 @@ SIGNATURES = {
     "bf_execute": [C.c_void_p, C.POINTER(bf_op), C.c_int64, C.POINTER(bf_exec_opts)],
     "bf_state_launch_count": [C.c_void_p, C.POINTER(C.c_uint64), C.c_int32],
     "bf_norm2": [C.c_void_p, C.POINTER(C.c_double)],
+    "bf_inner": [C.c_void_p, C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)],
     "bf_probabilities": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p],
     "bf_measure": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int64, C.POINTER(C.c_uint64),
                    C.POINTER(C.c_double)],
@@ -126,7 +127,8 @@ SIGNATURES = {
     "bf_norm2_noalloc": [C.c_void_p, C.c_uint64, C.c_int32, C.c_void_p, C.c_void_p],
     "bf_validate": [C.c_int32, C.POINTER(bf_op), C.c_int64],
     "bf_plan_stats": [C.c_int32, C.POINTER(bf_op), C.c_int64, C.POINTER(bf_exec_opts), C.POINTER(C.c_int64),
-                      C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_double)],
+                      C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_double), C.POINTER(C.c_int64),
+                      C.POINTER(C.c_int64)],
 }
 
 

@@ -592,6 +592,12 @@ class QuantumState:
                                    C.byref(pr)))
         return oc.value, pr.value
 
+    def inner(self, other: "QuantumState") -> complex:
+        """<self|other> on the device (double-float accumulation)."""
+        re, im = C.c_double(), C.c_double()
+        F.check(F.lib().bf_inner(self.handle, other.handle, C.byref(re), C.byref(im)))
+        return complex(re.value, im.value)
+
     def topk(self, k: int = 16) -> tuple[np.ndarray, np.ndarray]:
         idx = np.empty(k, dtype=np.uint64)
         pr = np.empty(k, dtype=np.float64)
@@ -650,12 +656,13 @@ def plan_stats(circuit: QuantumCircuit, ctx: Optional[ExecContext] = None) -> di
     ctx = ctx or ExecContext()
     arr, n, keep = circuit.to_ops()
     opts = exec_opts(ctx)
-    t, g, x = C.c_int64(), C.c_int64(), C.c_int64()
+    t, g, x, bp, nb = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
     b = C.c_double()
     F.check(F.lib().bf_plan_stats(circuit.num_qubits, arr, n, C.byref(opts), C.byref(t), C.byref(g), C.byref(x),
-                                  C.byref(b)))
+                                  C.byref(b), C.byref(bp), C.byref(nb)))
     del keep
-    return {"tile_passes": t.value, "gate_kernels": g.value, "other_passes": x.value, "bytes_in_S": b.value}
+    return {"tile_passes": t.value, "gate_kernels": g.value, "other_passes": x.value, "bytes_in_S": b.value,
+            "block_passes": bp.value, "blocks": nb.value}
 
 
 def validate(circuit: QuantumCircuit, num_qubits: Optional[int] = None) -> None:

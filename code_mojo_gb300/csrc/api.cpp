@@ -283,6 +283,30 @@ static void fused_pair_matrix(const bf_op& t0, const bf_op& t1, int& q_low, std:
 // as short per-op kernels so that other requests get SMs between them).
 constexpr int kLoopAlwaysQubits = 22;
 
+// Tensor cores or CUDA cores for one 12-qubit pass: the CUDA-core tile
+// kernel's work in units of one dense gate over the tile, against the blocks
+// the pass needs (one block costs about kBlockUnits dense gates: measured on
+// the 30-qubit complex64 layered circuit, 4.2 ms per block against 0.81 ms
+// per dense gate, beyond the 2.6 ms that moving the state costs either way).
+constexpr double kBlockUnits = 5.0;
+
+static double cuda_core_units(const TilePass& tp) {
+  double u = 0;
+  for (const TileOp& t : tp.ops) {
+    if (t.tloc < 0) {
+      u += 0.4;  // diagonal gate on an outside target: one multiply per amplitude
+      continue;
+    }
+    switch (t.kind) {
+      case GK_SWAP: u += 0.5; break;
+      case GK_PHASE: u += 0.4; break;
+      case GK_DIAG: u += 0.6; break;
+      default: u += 1.0; break;
+    }
+  }
+  return u;
+}
+
 // tensor: complex64 tile passes as tensor-core block passes (12-qubit tiles)
 static void build_steps(int n, const bf_op* ops, int64_t nops, const bf_exec_opts& o, std::vector<Step>& steps,
                         Program& pg, bool grover_loop_large = true, bool tensor = false) {
@@ -297,7 +321,8 @@ static void build_steps(int n, const bf_op* ops, int64_t nops, const bf_exec_opt
       Step s;
       if (ps.is_tile && tensor && ps.tile.K == kBlockTileQubits && ps.tile.L == kTileLowQubits) {
         size_t b0 = pg.blocks.size(), i0 = pg.images.size();
-        if (plan_blocks(ps.tile, pg.blocks, pg.images)) {
+        if (plan_blocks(ps.tile, pg.blocks, pg.images) &&
+            (double)(pg.blocks.size() - b0) * kBlockUnits < cuda_core_units(ps.tile)) {
           s.kind = Step::TBLOCK;
           s.tile = ps.tile;
           s.tile.ops.clear();
@@ -545,7 +570,7 @@ void execute_ops(State& st, const bf_op* ops, int64_t nops, bf_exec_opts o) {
   if (o.validate) validate_ops(st.n, ops, nops);
   std::vector<Step> steps;
   Program prog;
-  build_steps(st.n, ops, nops, o, steps, prog, st.coop_ctas == 0, o.tensor_blocks != 0 && st.dtype == BF_C64);
+  build_steps(st.n, ops, nops, o, steps, prog, !st.shared_gpu, o.tensor_blocks != 0 && st.dtype == BF_C64);
   // FP32 matrices are unitary only to ~6e-8, and that error changes the norm
   // coherently at every gate; the complex64 form restores the input norm.
   // renormalize == 2 (internal): the input is known to have unit norm.
@@ -784,6 +809,15 @@ int bf_norm2(bf_state* hst, double* out) {
   });
 }
 
+int bf_inner(bf_state* ha, bf_state* hb, double* re, double* im) {
+  State* a = S_(ha);
+  State* b = S_(hb);
+  return guarded([&]() {
+    if (!a || !b || !re || !im) fail(BF_EINVAL, "null argument");
+    inner_product(*a, *b, re, im);
+  });
+}
+
 int bf_probabilities(bf_state* hst, const int32_t* qubits, const int8_t* values, int32_t nq, double* out) {
   State* st = S_(hst);
   return guarded([&]() {
@@ -929,7 +963,8 @@ int bf_server_destroy(bf_server* h) {
 // device, reporting how many tile passes, per-gate kernels and other passes
 // bf_execute would launch and the algorithmic bytes they move (units of S).
 int bf_plan_stats(int32_t n, const bf_op* ops, int64_t nops, const bf_exec_opts* opts, int64_t* tile_passes,
-                  int64_t* gate_kernels, int64_t* other_passes, double* bytes_in_S) {
+                  int64_t* gate_kernels, int64_t* other_passes, double* bytes_in_S, int64_t* block_passes,
+                  int64_t* blocks) {
   return guarded([&]() {
     if (n < 1 || n > 40) fail(BF_EINVAL, "num_qubits must be in [1, 40], got %d", n);
     bf_exec_opts o;
@@ -940,9 +975,13 @@ int bf_plan_stats(int32_t n, const bf_op* ops, int64_t nops, const bf_exec_opts*
     std::vector<Step> steps;
     Program prog;
     build_steps(n, ops, nops, o, steps, prog, true, o.tensor_blocks != 0);
-    int64_t t = 0, g = 0, x = 0;
+    int64_t t = 0, g = 0, x = 0, bp = 0, nb = 0;
     double bytes = 0;
     for (auto& s : steps) {
+      if (s.kind == Step::TBLOCK) {
+        ++bp;
+        nb += s.nblk;
+      }
       if (s.kind == Step::TILE || s.kind == Step::TBLOCK) {
         ++t;
         bytes += 2.0;
@@ -962,6 +1001,8 @@ int bf_plan_stats(int32_t n, const bf_op* ops, int64_t nops, const bf_exec_opts*
     if (gate_kernels) *gate_kernels = g;
     if (other_passes) *other_passes = x;
     if (bytes_in_S) *bytes_in_S = bytes;
+    if (block_passes) *block_passes = bp;
+    if (blocks) *blocks = nb;
   });
 }
 

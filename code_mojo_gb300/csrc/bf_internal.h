@@ -140,8 +140,9 @@ struct State {
   int* d_flag = nullptr;
   int* h_flag = nullptr;
   bool flag_used = false;
-  // CTA cap of cooperative loops (0: sized for the whole GPU)
-  int32_t coop_ctas = 0;
+  // the state runs in a server slot that shares the GPU with other slots:
+  // long persistent kernels (grid-wide Grover loops) are not used
+  bool shared_gpu = false;
   // block descriptors and matrix images of tensor-core passes (device) and
   // their pinned staging; uploaded with the tile program
   unsigned char* d_aux = nullptr;
@@ -187,6 +188,8 @@ void launch_set_basis(State& s, uint64_t idx);
 void launch_interleave(State& s, const double* d_re, const double* d_im, uint64_t off, uint64_t cnt);
 void launch_deinterleave(State& s, double* d_re, double* d_im, uint64_t off, uint64_t cnt);
 double reduce_norm2(State& s);
+// <a|b> = sum conj(a_i) b_i (states of equal size, either dtype); synchronises a
+void inner_product(State& a, State& b, double* re, double* im);
 // complex64: restore the norm measured by launch_norm_before (or 1), stream-ordered
 void launch_norm_before(State& st);
 void launch_renormalize(State& st, bool unit_before);

@@ -11,6 +11,13 @@
 // run are admitted as soon as a slot and the memory are free, and their
 // kernels overlap on the device.  Each request records its submission,
 // start and completion times.
+//
+// Scheduling: a request is large when 2^n * ops exceeds large_cost.  Small
+// requests wait in a FIFO and run on every slot at the highest stream
+// priority; large ones wait in a queue ordered by that cost (cheapest
+// first: under an offered load above capacity this completes the most
+// requests, and the biggest ones wait) and run only on the large slots, at
+// the lowest priority.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -39,6 +46,7 @@ struct ServedRequest {
   std::vector<std::vector<int32_t>> qubits;  // owned copies of op.qubits
   double t_submit = 0;
   bool large = false;
+  double cost = 0;  // 2^n * ops
   uint64_t bytes() const { return (1ull << n) * (dtype == BF_C128 ? 16 : 8); }
 };
 
@@ -47,8 +55,8 @@ struct Server {
   int device = 0;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
-  std::deque<ServedRequest*> queue;        // small requests, oldest first
-  std::deque<ServedRequest*> large_queue;  // large requests, oldest first
+  std::deque<ServedRequest*> queue;         // small requests, oldest first
+  std::vector<ServedRequest*> large_queue;  // large requests: a heap, cheapest on top
   std::vector<bf_result> done;
   uint64_t next_id = 1, bytes_in_use = 0, peak_bytes = 0, budget = 0;
   uint64_t submitted = 0, completed = 0, failed = 0, running = 0;
@@ -82,6 +90,12 @@ static ServedRequest* copy_request(int32_t n, int32_t dtype, const bf_op* ops, i
     }
   }
   return r;
+}
+
+// heap order: the cheapest request (then the oldest) on top
+static bool cheaper_last(const ServedRequest* a, const ServedRequest* b) {
+  if (a->cost != b->cost) return a->cost > b->cost;
+  return a->id > b->id;
 }
 
 static void serve_one(Server& sv, State& st, ServedRequest& r, bf_result& res) {
@@ -127,8 +141,8 @@ static void worker_main(Server* sv, int slot) {
   bool ready = true;
   try {
     init_state_runtime(st);
-    // a slot's cooperative loops take a quarter of the SMs at most
-    st.coop_ctas = std::max(8, st.num_sms / 4);
+    // the slot shares the GPU: no grid-wide persistent loops
+    st.shared_gpu = true;
     // small-request slots run at the highest stream priority, large-request
     // slots at the lowest: the block scheduler then hands SMs that free up to
     // the short requests first
@@ -148,15 +162,23 @@ static void worker_main(Server* sv, int slot) {
     const bool large_slot = slot < sv->opts.large_slots;
     {
       std::unique_lock<std::mutex> lk(sv->mu);
-      auto fits = [&](const std::deque<ServedRequest*>& q) {
-        return !q.empty() && sv->bytes_in_use + q.front()->bytes() <= sv->budget;
+      auto fits_small = [&]() {
+        return !sv->queue.empty() && sv->bytes_in_use + sv->queue.front()->bytes() <= sv->budget;
+      };
+      auto fits_large = [&]() {
+        return !sv->large_queue.empty() && sv->bytes_in_use + sv->large_queue.front()->bytes() <= sv->budget;
       };
       // large slots take large requests first and otherwise help with small ones
-      sv->cv_work.wait(lk, [&]() { return sv->stop || fits(sv->queue) || (large_slot && fits(sv->large_queue)); });
+      sv->cv_work.wait(lk, [&]() { return sv->stop || fits_small() || (large_slot && fits_large()); });
       if (sv->stop) break;
-      std::deque<ServedRequest*>& q = (large_slot && fits(sv->large_queue)) ? sv->large_queue : sv->queue;
-      r = q.front();
-      q.pop_front();
+      if (large_slot && fits_large()) {
+        std::pop_heap(sv->large_queue.begin(), sv->large_queue.end(), cheaper_last);
+        r = sv->large_queue.back();
+        sv->large_queue.pop_back();
+      } else {
+        r = sv->queue.front();
+        sv->queue.pop_front();
+      }
       sv->bytes_in_use += r->bytes();
       sv->peak_bytes = std::max(sv->peak_bytes, sv->bytes_in_use);
       sv->running++;
@@ -202,7 +224,7 @@ Server* server_create(const bf_server_opts& opts) {
   sv->opts = opts;
   if (sv->opts.slots <= 0) sv->opts.slots = 12;
   if (sv->opts.slots > 64) fail(BF_EINVAL, "at most 64 slots");
-  if (sv->opts.large_slots <= 0) sv->opts.large_slots = std::max(1, sv->opts.slots / 4);
+  if (sv->opts.large_slots <= 0) sv->opts.large_slots = std::max(1, sv->opts.slots - 2);
   if (sv->opts.large_slots > sv->opts.slots) fail(BF_EINVAL, "large_slots exceeds slots");
   if (sv->opts.large_cost == 0) sv->opts.large_cost = 1ull << 28;
   if (sv->opts.topk <= 0) sv->opts.topk = 16;
@@ -232,12 +254,18 @@ uint64_t server_submit(Server& sv, int32_t n, int32_t dtype, const bf_op* ops, i
     delete r;
     fail(BF_EBUSY, "a %d-qubit state needs more than the server's HBM budget", n);
   }
-  r->large = (double)(1ull << n) * (double)std::max<int64_t>(1, nops) > (double)sv.opts.large_cost;
+  r->cost = (double)(1ull << n) * (double)std::max<int64_t>(1, nops);
+  r->large = r->cost > (double)sv.opts.large_cost;
   {
     std::lock_guard<std::mutex> lk(sv.mu);
     r->id = sv.next_id++;
     r->t_submit = now_s();
-    (r->large ? sv.large_queue : sv.queue).push_back(r);
+    if (r->large) {
+      sv.large_queue.push_back(r);
+      std::push_heap(sv.large_queue.begin(), sv.large_queue.end(), cheaper_last);
+    } else {
+      sv.queue.push_back(r);
+    }
     sv.submitted++;
   }
   sv.cv_work.notify_all();

@@ -158,6 +158,100 @@ double reduce_norm2(State& st) {
   return hi + lo;
 }
 
+// ---- <a|b> ------------------------------------------------------------------
+// sum conj(a_i) b_i over two states of the same size and either dtype, in
+// double-float per thread; partials (re.hi, re.lo, im.hi, im.lo) per block
+// summed on the host in FP64.  Used for the fidelity of a complex64 result
+// against a complex128 one.
+template <class T>
+__device__ __forceinline__ void amp_df2(T a, dfl& re, dfl& im);
+template <>
+__device__ __forceinline__ void amp_df2<double2>(double2 a, dfl& re, dfl& im) {
+  re = df_from_double(a.x);
+  im = df_from_double(a.y);
+}
+template <>
+__device__ __forceinline__ void amp_df2<float2>(float2 a, dfl& re, dfl& im) {
+  re = dfl{a.x, 0.f};
+  im = dfl{a.y, 0.f};
+}
+
+template <class TA, class TB>
+__global__ void __launch_bounds__(256) k_inner(const TA* __restrict__ a, const TB* __restrict__ b, uint64_t N,
+                                               double* __restrict__ partial) {
+  __shared__ dfl wr[8], wi[8];
+  dfl sr{0.f, 0.f}, si{0.f, 0.f};
+  const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += step) {
+    dfl ar, ai, br, bi;
+    amp_df2<TA>(a[i], ar, ai);
+    amp_df2<TB>(b[i], br, bi);
+    sr = df_add(sr, df_dot2(ar, br, ai, bi));           // re(conj(a) b) = ar br + ai bi
+    si = df_add(si, df_dot2(ar, bi, df_neg(ai), br));   // im(conj(a) b) = ar bi - ai br
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    sr = df_shfl_add(sr, off);
+    si = df_shfl_add(si, off);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    wr[warp] = sr;
+    wi[warp] = si;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    sr = lane < (int)(blockDim.x >> 5) ? wr[lane] : dfl{0.f, 0.f};
+    si = lane < (int)(blockDim.x >> 5) ? wi[lane] : dfl{0.f, 0.f};
+    for (int off = 16; off > 0; off >>= 1) {
+      sr = df_shfl_add(sr, off);
+      si = df_shfl_add(si, off);
+    }
+    if (lane == 0) {
+      partial[4 * blockIdx.x] = (double)sr.hi;
+      partial[4 * blockIdx.x + 1] = (double)sr.lo;
+      partial[4 * blockIdx.x + 2] = (double)si.hi;
+      partial[4 * blockIdx.x + 3] = (double)si.lo;
+    }
+  }
+}
+
+void inner_product(State& a, State& b, double* re, double* im) {
+  if (a.n != b.n) fail(BF_EINVAL, "inner product of states with %d and %d qubits", a.n, b.n);
+  unsigned blocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((a.N + 255) / 256, (uint64_t)a.num_sms * 8));
+  ensure_partials(a, 2 * (size_t)blocks);
+  // b's pending work must finish before a's stream reads it
+  cudaEvent_t ev;
+  BF_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  BF_CUDA(cudaEventRecord(ev, b.stream));
+  BF_CUDA(cudaStreamWaitEvent(a.stream, ev, 0));
+  BF_CUDA(cudaEventDestroy(ev));
+  const bool a128 = a.dtype == BF_C128, b128 = b.dtype == BF_C128;
+  if (a128 && b128)
+    k_inner<double2, double2><<<blocks, 256, 0, a.stream>>>(static_cast<const double2*>(a.amp),
+                                                            static_cast<const double2*>(b.amp), a.N, a.d_partial);
+  else if (a128)
+    k_inner<double2, float2><<<blocks, 256, 0, a.stream>>>(static_cast<const double2*>(a.amp),
+                                                           static_cast<const float2*>(b.amp), a.N, a.d_partial);
+  else if (b128)
+    k_inner<float2, double2><<<blocks, 256, 0, a.stream>>>(static_cast<const float2*>(a.amp),
+                                                           static_cast<const double2*>(b.amp), a.N, a.d_partial);
+  else
+    k_inner<float2, float2><<<blocks, 256, 0, a.stream>>>(static_cast<const float2*>(a.amp),
+                                                          static_cast<const float2*>(b.amp), a.N, a.d_partial);
+  BF_CUDA(cudaGetLastError());
+  a.launches++;
+  BF_CUDA(cudaMemcpyAsync(a.h_partial, a.d_partial, 4 * (size_t)blocks * sizeof(double), cudaMemcpyDeviceToHost,
+                          a.stream));
+  sync_state(a);
+  double r = 0, i = 0;
+  for (unsigned k = 0; k < blocks; ++k) {
+    r += a.h_partial[4 * k] + a.h_partial[4 * k + 1];
+    i += a.h_partial[4 * k + 2] + a.h_partial[4 * k + 3];
+  }
+  *re = r;
+  *im = i;
+}
+
 // ---- renormalisation (complex64 states) -------------------------------------
 // FP32 gate matrices are unitary only to ~6e-8 and that error changes the
 // norm coherently at every gate, so the complex64 form restores the norm

@@ -12,9 +12,9 @@
 // R[2l+c][2j+d] built from U[j][l].  It runs as tcgen05.mma kind::tf32
 // (M=128, N=64, K=8 per instruction) with FP32 accumulation in tensor
 // memory, in 3xTF32 form: A = Ab + As and R = Rb + Rs with Ab, Rb rounded
-// to TF32 and As, Rs the rounded remainders, D = As*Rb + Ab*Rs + Ab*Rb
-// (the As*Rs term is below FP32 resolution).  Relative error per block is
-// about 2^-22, against 2^-11 for plain TF32.
+// to TF32 and As, Rs the remainders, D = As*Rb + Ab*Rs + Ab*Rb (the As*Rs
+// term is below FP32 resolution).  Relative error per block is about 2^-21,
+// against 2^-11 for plain TF32.
 //
 // Per tile: coalesced 16-byte loads -> split into the two A operands in
 // shared memory (K-major, 128-byte swizzle) -> per block: one thread issues
@@ -39,7 +39,11 @@
 
 namespace bf {
 
-constexpr int kBlkThreads = 256;
+constexpr int kBlkThreads = 512;
+constexpr int kColGroups = kBlkThreads / 128;      // warps sharing one 32-lane group of D
+constexpr int kColsPerWarp = 64 / kColGroups;      // FP32 columns of D per warp
+constexpr int kCplxPerThread = kColsPerWarp / 2;   // complex results per thread per block
+constexpr int kLoadIters = 4096 / (2 * kBlkThreads);  // 16-byte loads per thread per tile
 constexpr uint32_t kAOpBytes = 128 * 64 * 4;  // 32 KiB: 128 rows x 64 FP32
 constexpr uint32_t kSmemA0 = 0;               // Ab
 constexpr uint32_t kSmemA1 = kAOpBytes;       // As
@@ -126,22 +130,19 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
-// 32 lanes x 32 consecutive FP32 columns: thread `lane` of the warp gets
-// row (32 * (warp % 4) + lane), columns col..col+31
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
-  uint32_t r[32];
+// 32 lanes x 16 consecutive FP32 columns: thread `lane` of the warp gets
+// row (32 * (warp % 4) + lane), columns col..col+15
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
       : "r"(taddr));
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 // ---- operand layout ----------------------------------------------------------
@@ -159,10 +160,12 @@ __device__ __forceinline__ uint32_t a_off(uint32_t g, uint32_t j) {
   return ((j >> 4) << 14) + (g << 7) + (((((j & 15) >> 1)) ^ (g & 7)) << 4) + ((j & 1) << 3);
 }
 
+// The low part is the exact remainder x - tf32(x); the tensor cores read its
+// top 19 bits (|error| <= 2^-21 |x|, no bias: the remainder takes either sign).
 __device__ __forceinline__ void put_split(unsigned char* sm, uint32_t off, float re, float im) {
   const float rb = tf32_round(re), ib = tf32_round(im);
   *reinterpret_cast<float2*>(sm + kSmemA0 + off) = make_float2(rb, ib);
-  *reinterpret_cast<float2*>(sm + kSmemA1 + off) = make_float2(tf32_round(re - rb), tf32_round(im - ib));
+  *reinterpret_cast<float2*>(sm + kSmemA1 + off) = make_float2(re - rb, im - ib);
 }
 
 // staging slot of tile element i (pairs stay together; spreads banks when
@@ -245,8 +248,9 @@ __global__ void __launch_bounds__(kBlkThreads, 2) k_tblock(const BlkPassArgs a) 
   const uint32_t tmem = *tmem_slot;
   // this warp's rows and columns of D
   const uint32_t row = 32u * (warp & 3) + lane;
-  const uint32_t colh = (uint32_t)(warp >> 2);  // columns 32*colh .. +31
-  const uint32_t taddr = tmem + ((32u * (warp & 3)) << 16) + 32u * colh;
+  const uint32_t colh = (uint32_t)(warp >> 2);  // columns kColsPerWarp*colh ..
+  const uint32_t taddr = tmem + ((32u * (warp & 3)) << 16) + (uint32_t)kColsPerWarp * colh;
+  static_assert(kColsPerWarp == 16, "the epilogue reads 16 columns per warp");
 
   // instruction descriptor: D FP32, A and B TF32, both K-major, N = 64, M = 128
   const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
@@ -274,9 +278,9 @@ __global__ void __launch_bounds__(kBlkThreads, 2) k_tblock(const BlkPassArgs a) 
     const uint64_t obase = tile_base(tile);
     build_tables(tabs, a.blocks[0].tmask);
     __syncthreads();
-    // load: 8 x 16 bytes per thread, split into the block-0 operands
-#pragma unroll 4
-    for (int it = 0; it < 8; ++it) {
+    // load: 16 bytes at a time, split into the block-0 operands
+#pragma unroll
+    for (int it = 0; it < kLoadIters; ++it) {
       const uint32_t i0 = (uint32_t)(it * kBlkThreads + tid) * 2u;
       const uint64_t gi = obase | (i0 & 31u) | hoff[i0 >> 5];
       const float4 v = __ldcs(reinterpret_cast<const float4*>(a.s + gi));
@@ -342,13 +346,13 @@ __global__ void __launch_bounds__(kBlkThreads, 2) k_tblock(const BlkPassArgs a) 
         break;
       }
       tc_fence_after();
-      float d[32];
-      tmem_ld32(taddr, d);
+      float d[kColsPerWarp];
+      tmem_ld16(taddr, d);
       const uint32_t gpart = cur[128 + row];
       if (more) {
 #pragma unroll
-        for (int c = 0; c < 16; ++c) {
-          const uint32_t i = gpart | cur[256 + 16u * colh + c];
+        for (int c = 0; c < kCplxPerThread; ++c) {
+          const uint32_t i = gpart | cur[256 + (uint32_t)kCplxPerThread * colh + c];
           const uint32_t t = nxt[i & 63u] + nxt[64 + (i >> 6)];
           put_split(sm, a_off(t & 0xFFu, t >> 8), d[2 * c], d[2 * c + 1]);
         }
@@ -356,8 +360,8 @@ __global__ void __launch_bounds__(kBlkThreads, 2) k_tblock(const BlkPassArgs a) 
       } else {
         float2* stage = reinterpret_cast<float2*>(sm + kSmemA0);
 #pragma unroll
-        for (int c = 0; c < 16; ++c) {
-          const uint32_t i = gpart | cur[256 + 16u * colh + c];
+        for (int c = 0; c < kCplxPerThread; ++c) {
+          const uint32_t i = gpart | cur[256 + (uint32_t)kCplxPerThread * colh + c];
           stage[stage_slot(i)] = make_float2(d[2 * c], d[2 * c + 1]);
         }
       }
@@ -365,10 +369,10 @@ __global__ void __launch_bounds__(kBlkThreads, 2) k_tblock(const BlkPassArgs a) 
       __syncthreads();
     }
     if (failed) break;
-    // store the staged tile: 8 x 16 bytes per thread
+    // store the staged tile, 16 bytes at a time
     const float2* stage = reinterpret_cast<const float2*>(sm + kSmemA0);
-#pragma unroll 4
-    for (int it = 0; it < 8; ++it) {
+#pragma unroll
+    for (int it = 0; it < kLoadIters; ++it) {
       const uint32_t i0 = (uint32_t)(it * kBlkThreads + tid) * 2u;
       const uint64_t gi = obase | (i0 & 31u) | hoff[i0 >> 5];
       const float4 v = *reinterpret_cast<const float4*>(stage + stage_slot(i0));
@@ -415,9 +419,12 @@ void launch_block_pass(State& st, const Blk5* d_blocks, int nblocks, const unsig
     BF_CUDA(cudaFuncSetAttribute(k_tblock, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     configured = true;
   }
-  int per_sm = 0;
-  BF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tblock, kBlkThreads, kSmemAlloc));
-  per_sm = std::max(1, std::min(per_sm, 2));
+  // two CTAs per SM when the shared memory holds them (one CTA's MMAs then
+  // overlap the other's loads and conversions); the occupancy calculator
+  // can report one under the default carveout, so count from the SM's size
+  int smem_sm = 0;
+  BF_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, st.device));
+  int per_sm = std::max(1, std::min(2, smem_sm / (int)(kSmemAlloc + 1024)));
   uint64_t grid = std::min<uint64_t>(a.ntiles, (uint64_t)per_sm * st.num_sms);
   k_tblock<<<(unsigned)grid, kBlkThreads, kSmemAlloc, st.stream>>>(a);
   BF_CUDA(cudaGetLastError());

@@ -82,6 +82,10 @@ class Server:
             pass
 
 
+# the server's default threshold between small and large requests (2^n * ops)
+LARGE_COST = 1 << 28
+
+
 def request_mix(count: int, seed: int = 0, nmin: int = 10, nmax: int = 28) -> list[tuple[str, OA.OpArray]]:
     """The served mix: qubit counts log-uniform in [nmin, nmax]; kinds Grover
     search (random marked index, floor(pi/4 sqrt(2^n)) iterations), value
@@ -115,6 +119,7 @@ def poisson_run(server: Server, requests, rate: float, duration_s: float, drain_
     t0 = time.perf_counter()
     ids = []
     results = []
+    cost = {}
     for i, ta in enumerate(arrivals):
         while True:
             now = time.perf_counter() - t0
@@ -123,6 +128,7 @@ def poisson_run(server: Server, requests, rate: float, duration_s: float, drain_
             time.sleep(min(0.002, ta - now))
         kind, ops = requests[i % len(requests)]
         ids.append(server.submit(ops, dtype))
+        cost[ids[-1]] = (1 << ops.num_qubits) * max(1, len(ops))
         if i % 64 == 0:
             results += server.poll()
     submit_end = time.perf_counter() - t0
@@ -134,6 +140,15 @@ def poisson_run(server: Server, requests, rate: float, duration_s: float, drain_
     svc = np.array([r.latency_s - r.queue_s for r in ok]) * 1e3
     nq = np.array([r.num_qubits for r in ok])
     st = server.stats()
+
+    def split(pred):
+        sel = [r for r in ok if pred(cost[r.id])]
+        la = np.array([r.latency_s for r in sel]) * 1e3
+        sub = sum(1 for rid in ids if pred(cost[rid]))
+        return {"submitted": sub, "completed": len(sel),
+                "p50_ms": float(np.percentile(la, 50)) if len(la) else None,
+                "p99_ms": float(np.percentile(la, 99)) if len(la) else None}
+
     return {"dtype": dtype, "rate_per_s": rate, "submitted": len(ids), "completed": len(ok),
             "failed": len(results) - len(ok), "backlog_at_end": int(st["queued"] + st["running"]),
             "drained": drained, "wall_s": wall, "submit_window_s": submit_end,
@@ -143,4 +158,5 @@ def poisson_run(server: Server, requests, rate: float, duration_s: float, drain_
             "service_p50_ms": float(np.percentile(svc, 50)) if len(svc) else None,
             "service_p99_ms": float(np.percentile(svc, 99)) if len(svc) else None,
             "completed_by_qubits": {int(k): int(v) for k, v in zip(*np.unique(nq, return_counts=True))},
-            "peak_state_bytes": int(st["peak_bytes"])}
+            "peak_state_bytes": int(st["peak_bytes"]),
+            "small": split(lambda c: c <= LARGE_COST), "large": split(lambda c: c > LARGE_COST)}

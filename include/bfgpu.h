@@ -202,6 +202,12 @@ int bf_state_launch_count(const bf_state* st, uint64_t* launches, int32_t reset)
  * state's type). */
 int bf_norm2(bf_state* st, double* out);
 
+/* <a|b> = sum conj(a_i) b_i of two states with the same qubit count, either
+ * dtype, accumulated in double-float and summed in FP64; waits for both
+ * states' pending work.  No counterpart in the reference: the fidelity
+ * |<a|b>|^2 of a complex64 result against a complex128 one. */
+int bf_inner(bf_state* a, bf_state* b, double* re, double* im);
+
 /* ---- measurement and readout (apply_measure, state.mojo:447-553) ---------- */
 /* Outcome probabilities over `qubits`: values[k] = 0 or 1 restricts to
  * amplitudes whose qubit k reads that value, -1 leaves it free (values may be
@@ -255,14 +261,15 @@ int bf_batch_destroy(bf_batch* b);
  * statevector footprint 2^n * (8 | 16) B fits in the HBM budget left by the
  * running ones; states are allocated and freed stream-ordered, and requests
  * in different slots overlap on the device.  Requests whose estimated cost
- * (2^n * ops) is large wait in their own queue, served by `large_slots`
- * slots, so they never hold every slot while small requests queue. */
+ * (2^n * ops) is large wait in their own queue, cheapest first, served by
+ * `large_slots` slots at the lowest stream priority, so they never hold
+ * every slot while small requests queue. */
 typedef struct bf_server bf_server;
 typedef struct bf_server_opts {
   int32_t slots;              /* concurrent requests; 0 = 12, at most 64       */
   int32_t tile_qubits;        /* fusion width; 0 = default                     */
   int32_t topk;               /* outcomes returned per request, 1..16; 0 = 16 */
-  int32_t large_slots;        /* slots that run large requests; 0 = slots/4   */
+  int32_t large_slots;        /* slots that run large requests; 0 = slots-2   */
   uint64_t hbm_budget_bytes;  /* statevector bytes admitted at once;
                                  0 = 80 % of the free HBM at creation         */
   uint64_t large_cost;        /* a request is large when 2^n * ops exceeds
@@ -319,11 +326,14 @@ int bf_norm2_noalloc(const void* d_amps, uint64_t num_amps, int32_t dtype,
  * num_qubits qubits. */
 int bf_validate(int32_t num_qubits, const bf_op* ops, int64_t nops);
 /* Plans ops as bf_execute would and reports the launches it would issue and
- * the algorithmic bytes they move, in units of the state's size S. */
+ * the algorithmic bytes they move, in units of the state's size S.
+ * tile_passes counts every tile pass; block_passes of them run on the
+ * tensor cores (tensor_blocks set), with `blocks` 5-qubit blocks in all. */
 int bf_plan_stats(int32_t num_qubits, const bf_op* ops, int64_t nops,
                   const bf_exec_opts* opts, int64_t* tile_passes,
                   int64_t* gate_kernels, int64_t* other_passes,
-                  double* bytes_in_S);
+                  double* bytes_in_S, int64_t* block_passes,
+                  int64_t* blocks);
 
 #ifdef __cplusplus
 }

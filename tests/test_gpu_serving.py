@@ -98,3 +98,22 @@ def test_wait_idle_is_bounded():
     (r,) = srv.poll()
     assert r.status == 0 and int(r.top_index[0]) == 12345 and r.top_prob[0] > 0.99
     srv.close()
+
+
+def test_large_requests_run_cheapest_first():
+    """With one large slot busy, queued large requests start in order of
+    2^n * ops, not of arrival."""
+    srv = SV.Server(slots=2, large_slots=1, large_cost=1024)
+    srv.submit(OA.random_layered(22, 40, 1), "c64")  # occupies the large slot
+    reqs = [OA.random_layered(14, 30, 2), OA.random_layered(12, 10, 3), OA.random_layered(13, 20, 4),
+            OA.value_encoding(11, 5.0)]
+    ids = [srv.submit(ops, "c64") for ops in reqs]
+    assert srv.wait_idle(120)
+    res = {r.id: r for r in srv.poll()}
+    srv.close()
+    cost = {rid: (1 << ops.num_qubits) * len(ops) for rid, ops in zip(ids, reqs)}
+    assert all(res[rid].status == 0 for rid in ids)
+    # queue_s = t_start - t_submit; submissions are microseconds apart, so
+    # start order is queue order
+    order = sorted(ids, key=lambda rid: res[rid].queue_s)
+    assert order == sorted(ids, key=lambda rid: cost[rid])

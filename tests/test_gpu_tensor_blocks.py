@@ -73,8 +73,16 @@ def test_plan_uses_block_passes_only_when_asked():
     qc = W.random_layered_circuit(16, 6, seed=1)
     off = bfy.plan_stats(qc, ctx(False))
     on = bfy.plan_stats(qc, ctx(True))
-    assert on["tile_passes"] > 0 and off["tile_passes"] > 0
-    assert on["bytes_in_S"] > 0
+    assert off["block_passes"] == 0 and off["blocks"] == 0
+    assert on["block_passes"] > 0 and on["blocks"] >= on["block_passes"]
+    assert on["block_passes"] <= on["tile_passes"]
+
+
+def test_passes_of_diagonal_gates_stay_on_cuda_cores():
+    """A QFT's passes are mostly controlled phases: cheaper on the CUDA-core
+    tile kernel than as dense blocks."""
+    s = bfy.plan_stats(W.qft_circuit(20), ctx(True))
+    assert s["tile_passes"] > 0 and s["block_passes"] == 0
 
 
 @pytest.mark.gpu
@@ -168,3 +176,19 @@ def test_state_reuse_after_block_passes():
     second = st.to_complex()
     st.close()
     assert np.array_equal(first, second)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("da,db", [("c128", "c128"), ("c128", "c64"), ("c64", "c128"), ("c64", "c64")])
+def test_inner_product_matches_numpy(da, db):
+    n = 15
+    ra, ia = W.random_normal_state(n, 1)
+    rb, ib = W.random_normal_state(n, 2)
+    a = bfy.QuantumState.from_soa(ra, ia, da)
+    b = bfy.QuantumState.from_soa(rb, ib, db)
+    got = a.inner(b)
+    xa, xb = a.to_complex(), b.to_complex()
+    a.close()
+    b.close()
+    exp = np.vdot(xa, xb)
+    assert abs(got - exp) <= 1e-13
