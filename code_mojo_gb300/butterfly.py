@@ -65,6 +65,7 @@ class ExecContext:
         self.execution_strategy = ExecutionStrategy.GPU_FUSED
         self.gpu_tile_qubits = 0     # fusion width of a tile pass (0 = default)
         self.gpu_tensor_blocks = False  # complex64: 5-qubit blocks as 3xTF32 tensor-core GEMMs
+        self.gpu_renormalize = True  # complex64: restore the input norm after the circuit
         self.gpu_sync = True         # block until the device has finished
 
     def copy(self) -> "ExecContext":
@@ -635,6 +636,7 @@ def exec_opts(ctx: ExecContext) -> F.bf_exec_opts:
     o.tile_qubits = ctx.gpu_tile_qubits
     o.sync = 1 if ctx.gpu_sync else 0
     o.tensor_blocks = 1 if ctx.gpu_tensor_blocks else 0
+    o.renormalize = 0 if ctx.gpu_renormalize else -1
     return o
 
 
