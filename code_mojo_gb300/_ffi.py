@@ -20,7 +20,8 @@ BF_C128, BF_C64 = 0, 1
 BF_GATE_H, BF_GATE_P, BF_GATE_X, BF_GATE_Y, BF_GATE_Z, BF_GATE_RX, BF_GATE_RY, BF_GATE_RZ, BF_GATE_CUSTOM = range(9)
 # op kinds
 (BF_OP_GATE, BF_OP_SWAP, BF_OP_QREV, BF_OP_UNITARY, BF_OP_CUNITARY, BF_OP_BITREV, BF_OP_PERMUTE,
- BF_OP_CSWAP, BF_OP_MEASURE, BF_OP_GROVER_DIFFUSER, BF_OP_GROVER_INVERSION0, BF_OP_CLASSICAL_ORACLE) = range(12)
+ BF_OP_CSWAP, BF_OP_MEASURE, BF_OP_GROVER_DIFFUSER, BF_OP_GROVER_INVERSION0, BF_OP_CLASSICAL_ORACLE,
+ BF_OP_MODEXP, BF_OP_MODEXP_INV) = range(14)
 BF_OPF_FUSE_WITH_NEXT = 1
 BF_STRATEGY_GPU, BF_STRATEGY_GPU_FUSED = 8, 9
 BF_SPEC_ALL = 127
@@ -120,6 +121,12 @@ SIGNATURES = {
     "bf_batch_destroy": [C.c_void_p],
     "bf_server_create": [C.POINTER(bf_server_opts), C.POINTER(C.c_void_p)],
     "bf_server_submit": [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int64, C.POINTER(C.c_uint64)],
+    "bf_server_submit_serialized": [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int32, C.POINTER(C.c_uint64)],
+    "bf_qasm3_parse": [C.c_char_p, C.POINTER(C.c_void_p)],
+    "bf_ops_serialize": [C.c_int32, C.POINTER(bf_op), C.c_int64, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)],
+    "bf_ops_deserialize": [C.c_void_p, C.c_size_t, C.POINTER(C.c_void_p)],
+    "bf_oplist_view": [C.c_void_p, C.POINTER(C.POINTER(bf_op)), C.POINTER(C.c_int64), C.POINTER(C.c_int32)],
+    "bf_oplist_destroy": [C.c_void_p],
     "bf_server_poll": [C.c_void_p, C.POINTER(bf_result), C.c_int32, C.POINTER(C.c_int32)],
     "bf_server_wait_idle": [C.c_void_p, C.c_int64],
     "bf_server_stats": [C.c_void_p, C.POINTER(bf_server_counters)],

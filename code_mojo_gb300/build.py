@@ -21,7 +21,7 @@ LIB = LIBDIR / "libbfgpu.so"
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc" if Path("/usr/local/cuda/bin/nvcc").exists() else "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
-SOURCES = ["api.cpp", "planner.cpp", "server.cpp", "gates.cu", "tile.cu", "perm.cu", "state_ops.cu", "measure.cu", "grover.cu", "batch.cu", "noalloc.cu", "blocks.cpp", "tblock.cu"]
+SOURCES = ["api.cpp", "planner.cpp", "server.cpp", "gates.cu", "tile.cu", "perm.cu", "state_ops.cu", "measure.cu", "grover.cu", "batch.cu", "noalloc.cu", "blocks.cpp", "tblock.cu", "wire.cpp"]
 
 
 def _deps_mtime() -> float:

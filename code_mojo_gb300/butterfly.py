@@ -234,11 +234,14 @@ class ControlledUnitaryTransformation:
 
 class ClassicalTransformation:
     """The classical transforms on the hot path: BITREV, PERMUTE and SWAP
-    (quantum_circuit.mojo:99-123) and the Grover diffuser / inversion about
-    |0> (grover_classical.mojo:262-326)."""
+    (quantum_circuit.mojo:99-123), the Grover diffuser / inversion about
+    |0> (grover_classical.mojo:262-326) and Shor's modular exponentiation
+    MOD_EXP / MOD_EXP_INV with targets [n_exp, n_value, a, N]
+    (algos/shor.mojo:56-166)."""
 
     def __init__(self, name: str, targets: Sequence[int]):
-        if name not in ("BITREV", "PERMUTE", "SWAP", "GROVER_DIFFUSER", "GROVER_INVERSION_0"):
+        if name not in ("BITREV", "PERMUTE", "SWAP", "GROVER_DIFFUSER", "GROVER_INVERSION_0", "MOD_EXP",
+                        "MOD_EXP_INV"):
             raise ValueError(f"unsupported classical transform {name}")
         self.name = name
         self.targets = list(targets)
@@ -383,6 +386,13 @@ class QuantumCircuit:
                     ops.append(_list_op(F.BF_OP_GROVER_DIFFUSER, tr.targets, keep))
                 elif tr.name == "GROVER_INVERSION_0":
                     ops.append(_list_op(F.BF_OP_GROVER_INVERSION0, tr.targets, keep))
+                elif tr.name in ("MOD_EXP", "MOD_EXP_INV"):
+                    vals = np.array([float(v) for v in tr.targets], dtype=np.float64)
+                    keep.append(vals)
+                    o = _op(F.BF_OP_MODEXP if tr.name == "MOD_EXP" else F.BF_OP_MODEXP_INV)
+                    o.data = vals.ctypes.data_as(C.POINTER(C.c_double))
+                    o.nqubits = len(vals)
+                    ops.append(o)
                 else:
                     if len(tr.targets) != 2:
                         raise ValueError("SWAP expects 2 targets")
@@ -463,6 +473,9 @@ def _invert(tr):
         for i, v in enumerate(tr.targets):
             inv[v] = i
         return ClassicalTransformation("PERMUTE", inv)
+    if isinstance(tr, ClassicalTransformation) and tr.name in ("MOD_EXP", "MOD_EXP_INV"):
+        # add_classical registers apply_modexp_inverse as MOD_EXP's inverse (algos/shor.mojo:161-166)
+        return ClassicalTransformation("MOD_EXP_INV" if tr.name == "MOD_EXP" else "MOD_EXP", tr.targets)
     return tr  # swaps, reversals, bit reversal: self-inverse
 
 
@@ -494,6 +507,79 @@ def grover_inversion_0(circuit: QuantumCircuit, targets: Optional[Sequence[int]]
 
 def swap_tr(a: int, b: int) -> ClassicalTransformation:
     return ClassicalTransformation("SWAP", [a, b])
+
+
+def mod_exp(circuit: QuantumCircuit, n_exp: int, n_value: int, a: int, modulus: int) -> None:
+    """The MOD_EXP classical transform of modexp_circuit (algos/shor.mojo:156-166)."""
+    circuit.transformations.append(ClassicalTransformation("MOD_EXP", [n_exp, n_value, a, modulus]))
+
+
+# ---------------------------------------------------------------------------
+# wire formats
+def parse_qasm3_string(qasm: str) -> QuantumCircuit:
+    """parse_qasm3_string (butterfly/utils/qasm3_import.mojo:52-123), parsed
+    by the library (bf_qasm3_parse): a qubit declaration, then h, x, p(angle)
+    and cp(angle) lines."""
+    h = C.c_void_p()
+    F.check(F.lib().bf_qasm3_parse(qasm.encode(), C.byref(h)))
+    try:
+        ops, cnt, n = C.POINTER(F.bf_op)(), C.c_int64(), C.c_int32()
+        F.check(F.lib().bf_oplist_view(h, C.byref(ops), C.byref(cnt), C.byref(n)))
+        qc = QuantumCircuit(n.value)
+        for i in range(cnt.value):
+            o = ops[i]
+            gate = {F.BF_GATE_H: H_Gate, F.BF_GATE_X: X_Gate}.get(o.gate) or P_Gate(o.arg)
+            if o.ncontrols:
+                qc.add(int(o.controls).bit_length() - 1, o.target, gate)
+            else:
+                qc.add(o.target, gate)
+        return qc
+    finally:
+        F.lib().bf_oplist_destroy(h)
+
+
+def serialize(circuit) -> bytes:
+    """The binary op list of a circuit (bf_ops_serialize)."""
+    arr, n, keep = circuit.to_ops()
+    size = C.c_size_t()
+    F.check(F.lib().bf_ops_serialize(circuit.num_qubits, arr, n, None, 0, C.byref(size)))
+    buf = C.create_string_buffer(max(1, size.value))
+    F.check(F.lib().bf_ops_serialize(circuit.num_qubits, arr, n, buf, size.value, C.byref(size)))
+    del keep
+    return buf.raw[:size.value]
+
+
+class OpList:
+    """An op list owned by the library (bf_ops_deserialize / bf_qasm3_parse);
+    executable like a circuit."""
+
+    def __init__(self, blob: bytes):
+        self._h = C.c_void_p()
+        F.check(F.lib().bf_ops_deserialize(blob, len(blob), C.byref(self._h)))
+        ops, cnt, n = C.POINTER(F.bf_op)(), C.c_int64(), C.c_int32()
+        F.check(F.lib().bf_oplist_view(self._h, C.byref(ops), C.byref(cnt), C.byref(n)))
+        self._ops, self._count, self.num_qubits = ops, cnt.value, n.value
+
+    def __len__(self) -> int:
+        return self._count
+
+    def to_ops(self):
+        return self._ops, self._count, [self]
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            F.lib().bf_oplist_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def deserialize(blob: bytes) -> OpList:
+    return OpList(blob)
 
 
 # ---------------------------------------------------------------------------

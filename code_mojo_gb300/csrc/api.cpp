@@ -117,8 +117,10 @@ struct Program {
   std::vector<TileOp> ops;
   std::vector<Blk5> blocks;
   std::vector<unsigned char> images;
+  std::vector<uint16_t> offsets;
   size_t images_offset() const { return (blocks.size() * sizeof(Blk5) + 255) & ~(size_t)255; }
-  size_t aux_bytes() const { return blocks.empty() ? 0 : images_offset() + images.size(); }
+  size_t offsets_offset() const { return images_offset() + images.size(); }
+  size_t aux_bytes() const { return blocks.empty() ? 0 : offsets_offset() + offsets.size() * sizeof(uint16_t); }
 };
 
 static void upload_program(State& st, const Program& pg) {
@@ -145,6 +147,7 @@ static void upload_program(State& st, const Program& pg) {
     }
     std::memcpy(st.h_aux, pg.blocks.data(), pg.blocks.size() * sizeof(Blk5));
     std::memcpy(st.h_aux + pg.images_offset(), pg.images.data(), pg.images.size());
+    std::memcpy(st.h_aux + pg.offsets_offset(), pg.offsets.data(), pg.offsets.size() * sizeof(uint16_t));
     BF_CUDA(cudaMemcpyAsync(st.d_aux, st.h_aux, aux, cudaMemcpyHostToDevice, st.stream));
   }
   BF_CUDA(cudaEventRecord(st.prog_event, st.stream));
@@ -154,7 +157,10 @@ static void upload_program(State& st, const Program& pg) {
 // ---- execution -------------------------------------------------------------
 // A step is one launch (or a launch group) in op order.
 struct Step {
-  enum Kind { GATE, TILE, TBLOCK, BITREV, PERMUTE, SWAPBITS, UNITARY, MEASURE, DIFFUSER, INVERSION0, ORACLE, GROVER_LOOP } kind;
+  enum Kind {
+    GATE, TILE, TBLOCK, BITREV, PERMUTE, SWAPBITS, UNITARY, MEASURE, DIFFUSER, INVERSION0, ORACLE, GROVER_LOOP,
+    MODEXP
+  } kind;
   GateInstr gate;
   TilePass tile;            // ops moved into the program; tile.ops emptied
   size_t prog_off = 0;
@@ -170,7 +176,21 @@ struct Step {
   int reps = 0;                  // Grover loop: iterations
   size_t blk_off = 0;            // tensor-core pass: its blocks in the program
   int nblk = 0;
+  uint64_t base = 0, modulus = 0;  // modexp: a (or a^-1 mod N) and N; a = n_exp
 };
+
+// a^-1 mod N for gcd(a, N) = 1 (extended Euclid, as modinv in algos/shor.mojo:46-53)
+static int64_t modinv(int64_t a, int64_t N) {
+  int64_t r0 = N, r1 = a, t0 = 0, t1 = 1;
+  while (r1 != 0) {
+    int64_t q = r0 / r1, r = r0 - q * r1, t = t0 - q * t1;
+    r0 = r1;
+    r1 = r;
+    t0 = t1;
+    t1 = t;
+  }
+  return ((t0 % N) + N) % N;
+}
 
 // Grover loop detection: the number of consecutive (classical oracle with
 // the same index list, diffuser over every qubit) pairs starting at ops[i],
@@ -320,8 +340,8 @@ static void build_steps(int n, const bf_op* ops, int64_t nops, const bf_exec_opt
     for (auto& ps : plan_gates(n, run, K)) {
       Step s;
       if (ps.is_tile && tensor && ps.tile.K == kBlockTileQubits && ps.tile.L == kTileLowQubits) {
-        size_t b0 = pg.blocks.size(), i0 = pg.images.size();
-        if (plan_blocks(ps.tile, pg.blocks, pg.images) &&
+        size_t b0 = pg.blocks.size(), i0 = pg.images.size(), o0 = pg.offsets.size();
+        if (plan_blocks(ps.tile, pg.blocks, pg.images, pg.offsets) &&
             (double)(pg.blocks.size() - b0) * kBlockUnits < cuda_core_units(ps.tile)) {
           s.kind = Step::TBLOCK;
           s.tile = ps.tile;
@@ -333,6 +353,7 @@ static void build_steps(int n, const bf_op* ops, int64_t nops, const bf_exec_opt
         }
         pg.blocks.resize(b0);
         pg.images.resize(i0);
+        pg.offsets.resize(o0);
       }
       if (ps.is_tile) {
         s.kind = Step::TILE;
@@ -519,6 +540,19 @@ static void build_steps(int n, const bf_op* ops, int64_t nops, const bf_exec_opt
         steps.push_back(std::move(s));
         break;
       }
+      case BF_OP_MODEXP:
+      case BF_OP_MODEXP_INV: {  // apply_modexp(_inverse) (algos/shor.mojo:56-140)
+        flush();
+        Step s;
+        s.kind = Step::MODEXP;
+        s.a = (int)op.data[0];
+        const int64_t N = (int64_t)op.data[3];
+        const int64_t a = (((int64_t)op.data[2] % N) + N) % N;
+        s.modulus = (uint64_t)N;
+        s.base = (uint64_t)(op.kind == BF_OP_MODEXP ? a : modinv(a, N));
+        steps.push_back(std::move(s));
+        break;
+      }
       case BF_OP_UNITARY:
         emit_unitary(op.data, op.target, op.target2, -1);
         break;
@@ -540,7 +574,8 @@ static void run_steps(State& st, std::vector<Step>& steps, const Program& pg) {
       case Step::TILE: launch_tile_pass(st, st.d_prog + s.prog_off, s.nprog, s.tile); break;
       case Step::TBLOCK:
         launch_block_pass(st, reinterpret_cast<const Blk5*>(st.d_aux) + s.blk_off, s.nblk,
-                          st.d_aux + pg.images_offset(), s.tile);
+                          st.d_aux + pg.images_offset(),
+                          reinterpret_cast<const uint16_t*>(st.d_aux + pg.offsets_offset()), s.tile);
         break;
       case Step::BITREV: launch_bitrev_full(st); break;
       case Step::PERMUTE: launch_permute(st, s.src_of.data()); break;
@@ -553,6 +588,7 @@ static void run_steps(State& st, std::vector<Step>& steps, const Program& pg) {
       case Step::INVERSION0: launch_grover_inversion0(st, s.mq.data(), (int32_t)s.mq.size()); break;
       case Step::ORACLE: launch_classical_oracle(st, s.u.data(), (int64_t)s.u.size()); break;
       case Step::GROVER_LOOP: launch_grover_loop(st, s.marked.data(), (int)s.marked.size(), s.reps); break;
+      case Step::MODEXP: launch_modexp(st, s.a, s.base, s.modulus); break;
     }
   }
 }
@@ -1003,6 +1039,64 @@ int bf_plan_stats(int32_t n, const bf_op* ops, int64_t nops, const bf_exec_opts*
     if (bytes_in_S) *bytes_in_S = bytes;
     if (block_passes) *block_passes = bp;
     if (blocks) *blocks = nb;
+  });
+}
+
+// ---- wire formats ---------------------------------------------------------------
+static inline OpList* L_(bf_oplist* h) { return reinterpret_cast<OpList*>(h); }
+static inline const OpList* LC_(const bf_oplist* h) { return reinterpret_cast<const OpList*>(h); }
+
+int bf_qasm3_parse(const char* text, bf_oplist** out) {
+  return guarded([&]() {
+    if (!out) fail(BF_EINVAL, "out is null");
+    *out = reinterpret_cast<bf_oplist*>(qasm3_parse(text));
+  });
+}
+
+int bf_ops_serialize(int32_t n, const bf_op* ops, int64_t nops, void* buf, size_t cap, size_t* len) {
+  return guarded([&]() {
+    if (!len) fail(BF_EINVAL, "len is null");
+    std::vector<unsigned char> blob = ops_serialize(n, ops, nops);
+    *len = blob.size();
+    if (!buf) return;
+    if (cap < blob.size()) fail(BF_EINVAL, "buffer of %zu bytes is smaller than the %zu needed", cap, blob.size());
+    std::memcpy(buf, blob.data(), blob.size());
+  });
+}
+
+int bf_ops_deserialize(const void* buf, size_t len, bf_oplist** out) {
+  return guarded([&]() {
+    if (!out) fail(BF_EINVAL, "out is null");
+    *out = reinterpret_cast<bf_oplist*>(ops_deserialize(buf, len));
+  });
+}
+
+int bf_oplist_view(const bf_oplist* h, const bf_op** ops, int64_t* nops, int32_t* n) {
+  return guarded([&]() {
+    if (!h) fail(BF_EINVAL, "list is null");
+    oplist_view(*LC_(h), ops, nops, n);
+  });
+}
+
+int bf_oplist_destroy(bf_oplist* h) {
+  return guarded([&]() { oplist_destroy(L_(h)); });
+}
+
+int bf_server_submit_serialized(bf_server* h, const void* buf, size_t len, int32_t dtype, uint64_t* id) {
+  return guarded([&]() {
+    if (!h || !id) fail(BF_EINVAL, "null argument");
+    OpList* L = ops_deserialize(buf, len);
+    const bf_op* ops = nullptr;
+    int64_t nops = 0;
+    int32_t n = 0;
+    oplist_view(*L, &ops, &nops, &n);
+    try {
+      *id = server_submit(*V_(h), n, dtype, ops, nops);  // copies the ops
+    } catch (...) {
+      oplist_destroy(L);
+      throw;
+    }
+    oplist_destroy(L);
   });
 }
 

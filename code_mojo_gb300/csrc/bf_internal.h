@@ -88,18 +88,40 @@ struct TilePass {
 // consecutively, variant v for outside bits (bit k of v = qubit outpos[k]).
 constexpr int kBlockTileQubits = 12;
 constexpr uint32_t kBlockImageBytes = 32768;  // one matrix: TF32 hi and lo parts, swizzled
+constexpr int kBlockThreads = 512;            // threads of the block kernel
+constexpr int kBlockThreadElems = 8;          // amplitudes each thread moves per block
+constexpr int kMaxPassBlocks = 32;
 
 struct Blk5 {
   uint32_t tmask;     // the block's 5 local positions (bits of the 12-bit tile index)
   int32_t nout;
   int32_t outpos[3];
   uint32_t img;       // image index of variant 0
+  uint32_t offs;      // index (units of kBlockThreads * kBlockThreadElems) of the
+                      // shared-memory destinations of this block's results
+  uint32_t load_offs; // first block of a pass: destinations of the loaded tile
 };
 
 // Partitions the ops of a 12-qubit tile pass into blocks and appends their
-// matrix images; false when an op cannot be placed (more than 5 tile qubits
-// or more than 3 outside qubits on its own).
-bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsigned char>& images);
+// matrix images and destination tables (u16 per thread and element: the
+// next block's operand offset / 8, or after the last block the staging
+// slot); false when an op cannot be placed (more than 5 tile qubits or more
+// than 3 outside qubits on its own) or the pass needs more than
+// kMaxPassBlocks blocks.
+bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsigned char>& images,
+                 std::vector<uint16_t>& offsets);
+#ifdef __CUDACC__
+#define BF_HOST_DEVICE __host__ __device__
+#else
+#define BF_HOST_DEVICE
+#endif
+// operand layout shared by the planner and the kernel: byte offset of
+// complex element (row g, column j) in a K-major, 128-byte-swizzled operand
+BF_HOST_DEVICE inline uint32_t block_operand_offset(uint32_t g, uint32_t j) {
+  return ((j >> 4) << 14) + (g << 7) + ((((j & 15) >> 1) ^ (g & 7)) << 4) + ((j & 1) << 3);
+}
+// staging slot of tile element i after the last block (pairs stay adjacent)
+BF_HOST_DEVICE inline uint32_t block_stage_slot(uint32_t i) { return i ^ (((i >> 5) & 15u) << 1); }
 // The matrix image of a 32x32 complex matrix u (row-major, interleaved
 // re/im): the real 64x64 operand R^T, split into TF32 hi and lo parts, in
 // the swizzled K-major layout of the block kernel.
@@ -179,10 +201,12 @@ void sync_state(State& st);
 void launch_gate(State& s, const GateInstr& g);
 void launch_tile_pass(State& s, const TileOp* d_ops, int nops, const TilePass& p);
 void launch_block_pass(State& st, const Blk5* d_blocks, int nblocks, const unsigned char* d_images,
-                       const TilePass& p);
+                       const uint16_t* d_offsets, const TilePass& p);
 void launch_bitrev_full(State& s);
 void launch_permute(State& s, const int32_t* src_bit_of_dst);  // dst bit j <- src bit perm[j]
 void launch_swap_bits(State& s, int a, int b);
+// |x, y> -> |x, y * base^x mod N> (y < N) over the whole state, x the low n_exp bits
+void launch_modexp(State& s, int n_exp, uint64_t base, uint64_t modulus);
 void launch_unitary(State& s, const double* h_u, int target, int m, int control);
 void launch_set_basis(State& s, uint64_t idx);
 void launch_interleave(State& s, const double* d_re, const double* d_im, uint64_t off, uint64_t cnt);
@@ -239,6 +263,16 @@ void batch_destroy(Batch* b);
 void batch_stats(const Batch& b, int64_t* tasks, int64_t* passes, uint64_t* state_bytes, int32_t* graph,
                  uint64_t* launches);
 void* batch_stream(const Batch& b);
+
+// Wire formats (wire.cpp).
+struct OpList;
+size_t op_data_len(const bf_op& o);    // doubles behind op.data for its kind
+size_t op_qubits_len(const bf_op& o);  // int32s behind op.qubits for its kind
+OpList* qasm3_parse(const char* text);
+std::vector<unsigned char> ops_serialize(int32_t n, const bf_op* ops, int64_t nops);
+OpList* ops_deserialize(const void* blob, size_t len);
+void oplist_view(const OpList& L, const bf_op** ops, int64_t* nops, int32_t* n);
+void oplist_destroy(OpList* L);
 
 // Serving loop (server.cpp).
 struct Server;

@@ -67,7 +67,54 @@ uint64_t outside_set(const TileOp& t) { return t.cmask_out | (t.tloc < 0 ? (1ull
 
 }  // namespace
 
-bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsigned char>& images) {
+namespace {
+
+// Index maps of one block: the 5 block qubits T (ascending: column bit r =
+// the r-th lowest) and the row order R (row bit r = local position R[r]).
+struct BlockMap {
+  uint32_t T = 0;
+  int R[7] = {0, 0, 0, 0, 0, 0, 0};
+  uint32_t dep_g(uint32_t g) const {
+    uint32_t i = 0;
+    for (int r = 0; r < 7; ++r) i |= ((g >> r) & 1u) << R[r];
+    return i;
+  }
+  uint32_t dep_j(uint32_t j) const {
+    uint32_t i = 0;
+    int r = 0;
+    for (int pos = 0; pos < kBlockTileQubits; ++pos)
+      if ((T >> pos) & 1u) i |= ((j >> r++) & 1u) << pos;
+    return i;
+  }
+  void ext(uint32_t i, uint32_t& g, uint32_t& j) const {
+    g = 0;
+    j = 0;
+    for (int r = 0; r < 7; ++r) g |= ((i >> R[r]) & 1u) << r;
+    int r = 0;
+    for (int pos = 0; pos < kBlockTileQubits; ++pos)
+      if ((T >> pos) & 1u) j |= ((i >> pos) & 1u) << r++;
+  }
+};
+
+// Row order of a block: the non-block positions written by the lanes of one
+// warp come first, so that a warp's 32 operand stores fall on different
+// 16-byte chunks of the 128-byte swizzle (the swizzle XORs the chunk with
+// the row's low three bits).
+BlockMap make_map(uint32_t T, uint32_t lane_positions) {
+  BlockMap m;
+  m.T = T;
+  int r = 0;
+  for (int pos = 0; pos < kBlockTileQubits; ++pos)
+    if (!((T >> pos) & 1u) && ((lane_positions >> pos) & 1u)) m.R[r++] = pos;
+  for (int pos = 0; pos < kBlockTileQubits; ++pos)
+    if (!((T >> pos) & 1u) && !((lane_positions >> pos) & 1u)) m.R[r++] = pos;
+  return m;
+}
+
+}  // namespace
+
+bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsigned char>& images,
+                 std::vector<uint16_t>& offsets) {
   if (tp.K != kBlockTileQubits) return false;
   std::vector<BlockBuild> bl;
   // Each op goes into the earliest block at or after the last block that
@@ -97,10 +144,19 @@ bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsi
     bl[place].ops.push_back(&t);
   }
 
+  if ((int)bl.size() > kMaxPassBlocks) return false;
+  std::vector<BlockMap> maps;
+  const size_t first = blocks.size();
+  // the load phase writes block 0's operands: a warp's lanes walk local bits 1..5
+  uint32_t lanes = 0x3Eu;
   for (auto& b : bl) {
     // pad to exactly 5 positions with unused tile qubits (identity on them)
     uint32_t T = b.qset;
     for (int pos = 0; pos < kBlockTileQubits && __builtin_popcount(T) < 5; ++pos) T |= 1u << pos;
+    maps.push_back(make_map(T, lanes));
+    // this block's epilogue: a warp's lanes walk its row bits 0..4
+    lanes = 0;
+    for (int r = 0; r < 5; ++r) lanes |= 1u << maps.back().R[r];
     int rank_of[kBlockTileQubits];
     int r = 0;
     for (int pos = 0; pos < kBlockTileQubits; ++pos) rank_of[pos] = ((T >> pos) & 1u) ? r++ : -1;
@@ -159,6 +215,45 @@ bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsi
       block_image(flat.data(), images.data() + at);
     }
     blocks.push_back(d);
+  }
+
+  // destination tables, kBlockThreads x kBlockThreadElems u16 each
+  const size_t table = (size_t)kBlockThreads * kBlockThreadElems;
+  auto new_table = [&]() {
+    size_t at = offsets.size();
+    offsets.resize(at + table);
+    return at;
+  };
+  {  // load phase: thread t, element e = 2 * it + h holds tile element (it * threads + t) * 2 + h
+    size_t at = new_table();
+    blocks[first].load_offs = (uint32_t)(at / table);
+    for (int t = 0; t < kBlockThreads; ++t)
+      for (int e = 0; e < kBlockThreadElems; ++e) {
+        uint32_t i = (uint32_t)(((e >> 1) * kBlockThreads + t) * 2 + (e & 1)), g, j;
+        maps[0].ext(i, g, j);
+        offsets[at + (size_t)t * kBlockThreadElems + e] = (uint16_t)(block_operand_offset(g, j) >> 3);
+      }
+  }
+  for (size_t k = 0; k < maps.size(); ++k) {
+    // epilogue: thread t reads D row 32 (warp % 4) + lane, columns of
+    // complex elements 8 (warp / 4) + e
+    size_t at = new_table();
+    blocks[first + k].offs = (uint32_t)(at / table);
+    for (int t = 0; t < kBlockThreads; ++t)
+      for (int e = 0; e < kBlockThreadElems; ++e) {
+        const uint32_t w = (uint32_t)t >> 5, lane = (uint32_t)t & 31u;
+        const uint32_t g = 32u * (w & 3u) + lane, j = (uint32_t)kBlockThreadElems * (w >> 2) + (uint32_t)e;
+        const uint32_t i = maps[k].dep_g(g) | maps[k].dep_j(j);
+        uint16_t v;
+        if (k + 1 < maps.size()) {
+          uint32_t g2, j2;
+          maps[k + 1].ext(i, g2, j2);
+          v = (uint16_t)(block_operand_offset(g2, j2) >> 3);
+        } else {
+          v = (uint16_t)block_stage_slot(i);
+        }
+        offsets[at + (size_t)t * kBlockThreadElems + e] = v;
+      }
   }
   return true;
 }

@@ -135,4 +135,72 @@ void launch_permute(State& st, const int32_t* src_of) {
   std::swap(st.amp, st.scratch);
 }
 
+// ---- modular exponentiation (Shor's order finding) -----------------------------
+// apply_modexp / apply_modexp_inverse (algos/shor.mojo:56-140) as one
+// out-of-place gather: amplitude (x, y) moves to (x, y * base^x mod N) for
+// y < N, where x is the low n_exp bits and y the rest; y >= N stays.  For
+// gcd(base, N) = 1 this is a permutation.  base^x mod N comes from a table
+// built on the device (x < 2^22) or from square-and-multiply per amplitude.
+__device__ __forceinline__ uint64_t mulmod64(uint64_t a, uint64_t b, uint64_t m) {
+  return (uint64_t)(((unsigned __int128)a * b) % m);
+}
+
+__device__ __forceinline__ uint64_t powmod64(uint64_t base, uint64_t e, uint64_t m) {
+  uint64_t r = 1 % m, b = base % m;
+  while (e) {
+    if (e & 1) r = mulmod64(r, b, m);
+    b = mulmod64(b, b, m);
+    e >>= 1;
+  }
+  return r;
+}
+
+__global__ void k_powtable(uint64_t* __restrict__ table, uint64_t count, uint64_t base, uint64_t m) {
+  const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; x < count; x += step)
+    table[x] = powmod64(base, x, m);
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_modexp(const T* __restrict__ in, T* __restrict__ out, uint64_t N,
+                                                int n_exp, uint64_t base, uint64_t m,
+                                                const uint64_t* __restrict__ table) {
+  const uint64_t xmask = (1ull << n_exp) - 1;
+  const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N; idx += step) {
+    const uint64_t x = idx & xmask, y = idx >> n_exp;
+    uint64_t y_out = y;
+    if (y < m) y_out = mulmod64(y, table ? __ldg(table + x) : powmod64(base, x, m), m);
+    out[x | (y_out << n_exp)] = in[idx];
+  }
+}
+
+void launch_modexp(State& st, int n_exp, uint64_t base, uint64_t modulus) {
+  if (n_exp <= 0 || n_exp >= st.n) fail(BF_EINVAL, "internal: modexp register of %d qubits", n_exp);
+  if (modulus < 2) fail(BF_EINVAL, "internal: modexp modulus %llu", (unsigned long long)modulus);
+  ensure_scratch(st);
+  uint64_t* table = nullptr;
+  const uint64_t xcount = 1ull << n_exp;
+  if (n_exp <= 22) {
+    table = static_cast<uint64_t*>(dev_alloc(st, xcount * sizeof(uint64_t)));
+    unsigned tb = (unsigned)std::min<uint64_t>((xcount + 255) / 256, (uint64_t)st.num_sms * 16);
+    k_powtable<<<tb, 256, 0, st.stream>>>(table, xcount, base, modulus);
+    BF_CUDA(cudaGetLastError());
+    st.launches++;
+  }
+  uint64_t blocks = std::min<uint64_t>((st.N + 255) / 256, (uint64_t)st.num_sms * 16);
+  if (st.dtype == BF_C128)
+    k_modexp<double2><<<(unsigned)blocks, 256, 0, st.stream>>>(static_cast<const double2*>(st.amp),
+                                                               static_cast<double2*>(st.scratch), st.N, n_exp, base,
+                                                               modulus, table);
+  else
+    k_modexp<float2><<<(unsigned)blocks, 256, 0, st.stream>>>(static_cast<const float2*>(st.amp),
+                                                              static_cast<float2*>(st.scratch), st.N, n_exp, base,
+                                                              modulus, table);
+  BF_CUDA(cudaGetLastError());
+  st.launches++;
+  if (table) dev_free(st, table);  // stream-ordered: after the gather
+  std::swap(st.amp, st.scratch);
+}
+
 }  // namespace bf

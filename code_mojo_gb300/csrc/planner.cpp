@@ -79,6 +79,26 @@ void validate_ops(int n, const bf_op* ops, int64_t nops) {
         }
         break;
       }
+      case BF_OP_MODEXP:
+      case BF_OP_MODEXP_INV: {  // apply_modexp(_inverse) checks (algos/shor.mojo:60-76, 103-119)
+        const char* name = o.kind == BF_OP_MODEXP ? "MOD_EXP" : "MOD_EXP_INV";
+        if (o.nqubits < 4 || !o.data) fail(BF_EINVAL, "%s expects 4 parameters: n_exp, n_value, a, N", name);
+        for (int k = 0; k < 4; ++k)
+          if (o.data[k] != std::floor(o.data[k]) || std::fabs(o.data[k]) > 9.0e15)
+            fail(BF_EINVAL, "%s parameters must be integers", name);
+        const int64_t ne = (int64_t)o.data[0], nv = (int64_t)o.data[1], a = (int64_t)o.data[2], N = (int64_t)o.data[3];
+        if (ne <= 0 || nv <= 0) fail(BF_EINVAL, "%s expects positive register sizes", name);
+        if (N <= 1) fail(BF_EINVAL, "%s expects modulus > 1", name);
+        int64_t x = ((a % N) + N) % N, y = N;  // gcd(a, N)
+        while (y != 0) {
+          int64_t t = x % y;
+          x = y;
+          y = t;
+        }
+        if (x != 1) fail(BF_EINVAL, "%s expects a and modulus to be coprime", name);
+        if (ne + nv != n) fail(BF_EINVAL, "State size mismatch for %s", name);
+        break;
+      }
       case BF_OP_CLASSICAL_ORACLE: {
         if (o.nqubits < 0 || (o.nqubits > 0 && o.data == nullptr)) fail(BF_EINVAL, "oracle index list is null");
         double N = std::ldexp(1.0, n);

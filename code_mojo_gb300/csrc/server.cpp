@@ -64,10 +64,6 @@ struct Server {
   std::vector<std::thread> workers;
 };
 
-static size_t unitary_doubles(const bf_op& o) {
-  return o.target2 > 0 ? 2 * ((size_t)1 << (2 * o.target2)) : 0;
-}
-
 static ServedRequest* copy_request(int32_t n, int32_t dtype, const bf_op* ops, int64_t nops) {
   auto* r = new ServedRequest();
   r->n = n;
@@ -77,13 +73,12 @@ static ServedRequest* copy_request(int32_t n, int32_t dtype, const bf_op* ops, i
   r->qubits.resize(nops);
   for (int64_t i = 0; i < nops; ++i) {
     bf_op& o = r->ops[i];
-    if (o.qubits && o.nqubits > 0) {
-      r->qubits[i].assign(o.qubits, o.qubits + o.nqubits);
+    const size_t nq = op_qubits_len(o);
+    if (o.qubits && nq > 0) {
+      r->qubits[i].assign(o.qubits, o.qubits + nq);
       o.qubits = r->qubits[i].data();
     }
-    size_t nd = 0;
-    if (o.kind == BF_OP_UNITARY || o.kind == BF_OP_CUNITARY) nd = unitary_doubles(o);
-    else if (o.kind == BF_OP_MEASURE || o.kind == BF_OP_CLASSICAL_ORACLE) nd = (size_t)std::max<int64_t>(0, o.nqubits);
+    const size_t nd = op_data_len(o);
     if (o.data && nd > 0) {
       r->data[i].assign(o.data, o.data + nd);
       o.data = r->data[i].data();

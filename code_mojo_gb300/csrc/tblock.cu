@@ -21,7 +21,10 @@
 // 24 MMAs and commits them to an mbarrier, the epilogue reads D from tensor
 // memory (tcgen05.ld 32x32b), and writes it either as the next block's A
 // operands (a bit permutation of the tile index) or, after the last block,
-// into a staging copy of the tile -> coalesced 16-byte stores.  The block
+// into a staging copy of the tile -> coalesced 16-byte stores.  Where each
+// thread's 8 results go is a per-block table computed by the planner (one
+// 16-byte load per thread per block), which also orders each block's rows so
+// that a warp's operand stores spread over the swizzled 16-byte chunks.  The block
 // matrices (pre-split and pre-swizzled on the host, 32 KiB each) stream in
 // with cp.async.bulk behind the MMAs of the previous block.  Gates with
 // controls (or diagonal targets) outside the tile select one of up to 8
@@ -39,7 +42,7 @@
 
 namespace bf {
 
-constexpr int kBlkThreads = 512;
+constexpr int kBlkThreads = kBlockThreads;
 constexpr int kColGroups = kBlkThreads / 128;      // warps sharing one 32-lane group of D
 constexpr int kColsPerWarp = 64 / kColGroups;      // FP32 columns of D per warp
 constexpr int kCplxPerThread = kColsPerWarp / 2;   // complex results per thread per block
@@ -48,9 +51,7 @@ constexpr uint32_t kAOpBytes = 128 * 64 * 4;  // 32 KiB: 128 rows x 64 FP32
 constexpr uint32_t kSmemA0 = 0;               // Ab
 constexpr uint32_t kSmemA1 = kAOpBytes;       // As
 constexpr uint32_t kSmemB = 2 * kAOpBytes;    // Rb (2 x 8 KiB), Rs (2 x 8 KiB)
-constexpr uint32_t kSmemTab = kSmemB + kBlockImageBytes;
-constexpr uint32_t kTabWords = 288;           // ext_lo 64, ext_hi 64, dep_g 128, dep_j 32
-constexpr uint32_t kSmemHoff = kSmemTab + 2 * kTabWords * 4;
+constexpr uint32_t kSmemHoff = kSmemB + kBlockImageBytes;
 constexpr uint32_t kSmemBar = kSmemHoff + 128 * 8;
 constexpr uint32_t kSmemUsed = kSmemBar + 32;
 constexpr uint32_t kSmemAlloc = kSmemUsed + 1024;  // slack for 1024-byte alignment
@@ -63,6 +64,7 @@ struct BlkPassArgs {
   uint64_t ntiles;
   int32_t nblocks;
   int32_t q[kBlockTileQubits];  // tile qubits; q[j] = j for j < 5
+  const uint16_t* offsets;      // destination tables (kBlkThreads x 8 per table)
   int* flag;
   uint32_t spin_limit;
 };
@@ -152,14 +154,6 @@ __device__ __forceinline__ float tf32_round(float x) {
   return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
 }
 
-// Byte offset of complex element (row g, column j) inside an A operand: the
-// real part at k = 2j, the imaginary part at k = 2j + 1, K-major rows of
-// 64 FP32 split into two 128-byte spans of 16 KiB each, 16-byte chunks
-// swizzled by the row's low three bits.
-__device__ __forceinline__ uint32_t a_off(uint32_t g, uint32_t j) {
-  return ((j >> 4) << 14) + (g << 7) + (((((j & 15) >> 1)) ^ (g & 7)) << 4) + ((j & 1) << 3);
-}
-
 // The low part is the exact remainder x - tf32(x); the tensor cores read its
 // top 19 bits (|error| <= 2^-21 |x|, no bias: the remainder takes either sign).
 __device__ __forceinline__ void put_split(unsigned char* sm, uint32_t off, float re, float im) {
@@ -168,43 +162,14 @@ __device__ __forceinline__ void put_split(unsigned char* sm, uint32_t off, float
   *reinterpret_cast<float2*>(sm + kSmemA1 + off) = make_float2(re - rb, im - ib);
 }
 
-// staging slot of tile element i (pairs stay together; spreads banks when
-// the epilogue's lanes walk the tile at a power-of-two stride)
-__device__ __forceinline__ uint32_t stage_slot(uint32_t i) { return i ^ (((i >> 5) & 15u) << 1); }
+// this thread's 8 destinations in a table: operand byte offset / 8, or staging slot
+__device__ __forceinline__ uint4 my_dests(const uint16_t* offsets, uint32_t table) {
+  return __ldg(reinterpret_cast<const uint4*>(offsets + ((size_t)table * kBlkThreads + threadIdx.x) * 8));
+}
 
-// Index tables of one block (target mask T over the 12 local bits):
-//   ext_lo[x], ext_hi[y]: (g | j << 8) contributions of local bits 0..5 / 6..11
-//   dep_g[g], dep_j[j]:   local index bits of row g / column j
-__device__ __forceinline__ void build_tables(uint32_t* tab, uint32_t T) {
-  const uint32_t G = ~T & 0xFFFu;
-  const int glo = __popc(G & 63u), jlo = __popc(T & 63u);
-  for (int e = threadIdx.x; e < (int)kTabWords; e += kBlkThreads) {
-    uint32_t v = 0;
-    if (e < 128) {
-      const int x = e & 63;
-      const int base = (e < 64) ? 0 : 6;
-      uint32_t g = 0, j = 0;
-      int gr = (e < 64) ? 0 : glo, jr = (e < 64) ? 0 : jlo;
-      for (int b = 0; b < 6; ++b) {
-        const int pos = base + b;
-        const uint32_t bit = (x >> b) & 1u;
-        if ((G >> pos) & 1u) g |= bit << gr++;
-        else j |= bit << jr++;
-      }
-      v = g | (j << 8);
-    } else if (e < 256) {
-      const uint32_t g = e - 128;
-      int r = 0;
-      for (int pos = 0; pos < 12; ++pos)
-        if ((G >> pos) & 1u) v |= ((g >> r++) & 1u) << pos;
-    } else {
-      const uint32_t j = e - 256;
-      int r = 0;
-      for (int pos = 0; pos < 12; ++pos)
-        if ((T >> pos) & 1u) v |= ((j >> r++) & 1u) << pos;
-    }
-    tab[e] = v;
-  }
+__device__ __forceinline__ uint32_t dest_at(const uint4& d, int e) {
+  const uint32_t w = e < 2 ? d.x : (e < 4 ? d.y : (e < 6 ? d.z : d.w));
+  return (e & 1) ? (w >> 16) : (w & 0xFFFFu);
 }
 
 __device__ __forceinline__ uint32_t variant_of(const Blk5& b, uint64_t obase) {
@@ -217,13 +182,12 @@ __global__ void __launch_bounds__(kBlkThreads, 2) k_tblock(const BlkPassArgs a) 
   extern __shared__ unsigned char smem_raw[];
   // 1024-byte alignment for the swizzled operands
   unsigned char* sm = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
-  uint32_t* tabs = reinterpret_cast<uint32_t*>(sm + kSmemTab);
   uint64_t* hoff = reinterpret_cast<uint64_t*>(sm + kSmemHoff);
   uint64_t* bars = reinterpret_cast<uint64_t*>(sm + kSmemBar);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + kSmemBar + 16);
   int* ok_slot = reinterpret_cast<int*>(sm + kSmemBar + 20);
   const uint32_t bar_b = smem_u32(&bars[0]), bar_mma = smem_u32(&bars[1]);
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tid = threadIdx.x, warp = tid >> 5;
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
@@ -247,7 +211,6 @@ __global__ void __launch_bounds__(kBlkThreads, 2) k_tblock(const BlkPassArgs a) 
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   // this warp's rows and columns of D
-  const uint32_t row = 32u * (warp & 3) + lane;
   const uint32_t colh = (uint32_t)(warp >> 2);  // columns kColsPerWarp*colh ..
   const uint32_t taddr = tmem + ((32u * (warp & 3)) << 16) + (uint32_t)kColsPerWarp * colh;
   static_assert(kColsPerWarp == 16, "the epilogue reads 16 columns per warp");
@@ -274,29 +237,28 @@ __global__ void __launch_bounds__(kBlkThreads, 2) k_tblock(const BlkPassArgs a) 
     b_in_flight = true;
   }
 
+  static_assert(kLoadIters * 2 == kBlockThreadElems, "one destination table entry per loaded amplitude");
+  const uint4 load_dest = my_dests(a.offsets, a.blocks[0].load_offs);
   for (; tile < a.ntiles && !failed; tile += gridDim.x) {
     const uint64_t obase = tile_base(tile);
-    build_tables(tabs, a.blocks[0].tmask);
-    __syncthreads();
     // load: 16 bytes at a time, split into the block-0 operands
+    float4 v[kLoadIters];
 #pragma unroll
     for (int it = 0; it < kLoadIters; ++it) {
       const uint32_t i0 = (uint32_t)(it * kBlkThreads + tid) * 2u;
-      const uint64_t gi = obase | (i0 & 31u) | hoff[i0 >> 5];
-      const float4 v = __ldcs(reinterpret_cast<const float4*>(a.s + gi));
-      uint32_t t = tabs[i0 & 63u] + tabs[64 + (i0 >> 6)];
-      put_split(sm, a_off(t & 0xFFu, t >> 8), v.x, v.y);
-      t = tabs[(i0 + 1) & 63u] + tabs[64 + ((i0 + 1) >> 6)];
-      put_split(sm, a_off(t & 0xFFu, t >> 8), v.z, v.w);
+      v[it] = __ldcs(reinterpret_cast<const float4*>(a.s + (obase | (i0 & 31u) | hoff[i0 >> 5])));
+    }
+#pragma unroll
+    for (int it = 0; it < kLoadIters; ++it) {
+      put_split(sm, dest_at(load_dest, 2 * it) << 3, v[it].x, v[it].y);
+      put_split(sm, dest_at(load_dest, 2 * it + 1) << 3, v[it].z, v[it].w);
     }
     fence_proxy_async();
     __syncthreads();
 
     for (int bi = 0; bi < a.nblocks; ++bi) {
-      const uint32_t* cur = tabs + (bi & 1) * kTabWords;
-      uint32_t* nxt = tabs + ((bi + 1) & 1) * kTabWords;
       const bool more = bi + 1 < a.nblocks;
-      if (more) build_tables(nxt, a.blocks[bi + 1].tmask);
+      const uint4 dest = my_dests(a.offsets, a.blocks[bi].offs);
       if (tid == 0) {
         int ok = mbar_wait(bar_b, ph_b, a.spin_limit) ? 1 : 0;
         if (ok) {
@@ -348,22 +310,14 @@ __global__ void __launch_bounds__(kBlkThreads, 2) k_tblock(const BlkPassArgs a) 
       tc_fence_after();
       float d[kColsPerWarp];
       tmem_ld16(taddr, d);
-      const uint32_t gpart = cur[128 + row];
       if (more) {
 #pragma unroll
-        for (int c = 0; c < kCplxPerThread; ++c) {
-          const uint32_t i = gpart | cur[256 + (uint32_t)kCplxPerThread * colh + c];
-          const uint32_t t = nxt[i & 63u] + nxt[64 + (i >> 6)];
-          put_split(sm, a_off(t & 0xFFu, t >> 8), d[2 * c], d[2 * c + 1]);
-        }
+        for (int c = 0; c < kCplxPerThread; ++c) put_split(sm, dest_at(dest, c) << 3, d[2 * c], d[2 * c + 1]);
         fence_proxy_async();
       } else {
         float2* stage = reinterpret_cast<float2*>(sm + kSmemA0);
 #pragma unroll
-        for (int c = 0; c < kCplxPerThread; ++c) {
-          const uint32_t i = gpart | cur[256 + (uint32_t)kCplxPerThread * colh + c];
-          stage[stage_slot(i)] = make_float2(d[2 * c], d[2 * c + 1]);
-        }
+        for (int c = 0; c < kCplxPerThread; ++c) stage[dest_at(dest, c)] = make_float2(d[2 * c], d[2 * c + 1]);
       }
       tc_fence_before();
       __syncthreads();
@@ -375,7 +329,7 @@ __global__ void __launch_bounds__(kBlkThreads, 2) k_tblock(const BlkPassArgs a) 
     for (int it = 0; it < kLoadIters; ++it) {
       const uint32_t i0 = (uint32_t)(it * kBlkThreads + tid) * 2u;
       const uint64_t gi = obase | (i0 & 31u) | hoff[i0 >> 5];
-      const float4 v = *reinterpret_cast<const float4*>(stage + stage_slot(i0));
+      const float4 v = *reinterpret_cast<const float4*>(stage + block_stage_slot(i0));
       __stcs(reinterpret_cast<float4*>(a.s + gi), v);
     }
     __syncthreads();
@@ -394,7 +348,7 @@ __global__ void __launch_bounds__(kBlkThreads, 2) k_tblock(const BlkPassArgs a) 
 }
 
 void launch_block_pass(State& st, const Blk5* d_blocks, int nblocks, const unsigned char* d_images,
-                       const TilePass& p) {
+                       const uint16_t* d_offsets, const TilePass& p) {
   if (st.dtype != BF_C64) fail(BF_EINVAL, "internal: tensor-core blocks need a complex64 state");
   if (p.K != kBlockTileQubits || st.n < kBlockTileQubits) fail(BF_EINVAL, "internal: block pass needs a 12-qubit tile");
   if (nblocks < 1) fail(BF_EINVAL, "internal: empty block pass");
@@ -408,6 +362,8 @@ void launch_block_pass(State& st, const Blk5* d_blocks, int nblocks, const unsig
   a.s = static_cast<float2*>(st.amp);
   a.blocks = d_blocks;
   a.images = d_images;
+  a.offsets = d_offsets;
+  if (((uintptr_t)d_offsets & 15u) != 0) fail(BF_EINVAL, "internal: block tables must be 16-byte aligned");
   a.nblocks = nblocks;
   a.ntiles = st.N >> kBlockTileQubits;
   a.flag = state_flag(st);

@@ -47,6 +47,13 @@ class Server:
         F.check(_lib().bf_server_submit(self._h, ops.num_qubits, code, ops.ops.ctypes.data, len(ops), C.byref(rid)))
         return rid.value
 
+    def submit_serialized(self, blob: bytes, dtype: str = "c64") -> int:
+        """Submits a circuit in the binary op-list form (bf_server_submit_serialized)."""
+        rid = C.c_uint64()
+        code = F.BF_C64 if dtype == "c64" else F.BF_C128
+        F.check(_lib().bf_server_submit_serialized(self._h, blob, len(blob), code, C.byref(rid)))
+        return rid.value
+
     def poll(self, max_results: int = 4096) -> list[Result]:
         buf = (bf_result * max_results)()
         cnt = C.c_int32()

@@ -19,7 +19,7 @@ from typing import Sequence
 
 import numpy as np
 
-from .butterfly import QuantumCircuit, bit_reverse, grover_diffuser
+from .butterfly import QuantumCircuit, bit_reverse, grover_diffuser, mod_exp
 
 
 def iqft_circuit(qc: QuantumCircuit, targets: Sequence[int], swap: bool = False) -> None:
@@ -169,3 +169,22 @@ def random_normal_state(n: int, seed: int = 0) -> tuple[np.ndarray, np.ndarray]:
     im = rng.standard_normal(1 << n)
     s = math.sqrt(float(np.sum(re * re) + np.sum(im * im)))
     return re / s, im / s
+
+
+def modexp_circuit(n_exp: int, n_value: int, a: int, modulus: int) -> QuantumCircuit:
+    """modexp_circuit (algos/shor.mojo:143-167): H on the exponent register
+    (qubits 0..n_exp-1), |1> in the value register, then MOD_EXP."""
+    qc = QuantumCircuit(n_exp + n_value)
+    for i in range(n_exp):
+        qc.h(i)
+    qc.x(n_exp)
+    mod_exp(qc, n_exp, n_value, a, modulus)
+    return qc
+
+
+def order_finding_circuit(n_exp: int, n_value: int, a: int, modulus: int, swap: bool = False) -> QuantumCircuit:
+    """order_finding_circuit (algos/shor.mojo:334-380): modexp_circuit, then
+    the inverse QFT on the exponent register."""
+    qc = modexp_circuit(n_exp, n_value, a, modulus)
+    iqft_circuit(qc, [n_exp - 1 - j for j in range(n_exp)], swap=swap)
+    return qc

@@ -85,9 +85,16 @@ enum {
                                   x <- 2 mean - x over each target block      */
   BF_OP_GROVER_INVERSION0 = 10, /* classical apply_grover_inversion_0(qubits; none =
                                   all): negate the all-zero target amplitude  */
-  BF_OP_CLASSICAL_ORACLE = 11  /* classical_oracle (grover.mojo:64-66): negate the
+  BF_OP_CLASSICAL_ORACLE = 11, /* classical_oracle (grover.mojo:64-66): negate the
                                   amplitudes at the basis indices data[0..nqubits)
                                   (integers held exactly as doubles)          */
+  BF_OP_MODEXP = 12,           /* apply_modexp (algos/shor.mojo:56-96): data =
+                                  {n_exp, n_value, a, N} (nqubits = 4); the state
+                                  has n_exp + n_value qubits, x = the low n_exp
+                                  bits, y = the rest; |x, y> -> |x, y a^x mod N>
+                                  for y < N, unchanged for y >= N              */
+  BF_OP_MODEXP_INV = 13        /* apply_modexp_inverse (algos/shor.mojo:99-140):
+                                  the same with a^-x mod N                    */
 };
 
 /* bf_op.flags */
@@ -320,6 +327,29 @@ int bf_server_destroy(bf_server* s);
  * the array, so calls that overlap on the GPU race: serialise them. */
 int bf_norm2_noalloc(const void* d_amps, uint64_t num_amps, int32_t dtype,
                      double* d_out, void* stream);
+
+/* ---- circuit wire formats ------------------------------------------------
+ * An op list owns its records and the data / qubit arrays they point to.
+ * bf_qasm3_parse reads the QASM3 subset of parse_qasm3_string
+ * (butterfly/utils/qasm3_import.mojo:52-123: a qubit declaration, h, x,
+ * p(angle), cp(angle); angles as numbers, pi, -pi, k*pi, pi/k, k/pi) with the
+ * same error messages.  bf_ops_serialize writes a self-contained binary form
+ * of any op array (little-endian: "BFOP", version 1, num_qubits, op count,
+ * then per op its 104 fixed bytes, nqubits, and its data and qubit arrays);
+ * with buf NULL it only reports the size.  bf_ops_deserialize reads it back.
+ * No counterpart in the reference for the binary form. */
+typedef struct bf_oplist bf_oplist;
+int bf_qasm3_parse(const char* text, bf_oplist** out);
+int bf_ops_serialize(int32_t num_qubits, const bf_op* ops, int64_t nops,
+                     void* buf, size_t cap, size_t* len);
+int bf_ops_deserialize(const void* buf, size_t len, bf_oplist** out);
+/* the list's ops (valid until bf_oplist_destroy) and its qubit count */
+int bf_oplist_view(const bf_oplist* list, const bf_op** ops, int64_t* nops,
+                   int32_t* num_qubits);
+int bf_oplist_destroy(bf_oplist* list);
+/* submits a serialized op list (see bf_server_submit) */
+int bf_server_submit_serialized(bf_server* server, const void* buf, size_t len,
+                                int32_t dtype, uint64_t* id);
 
 /* ---- host-only entry points (no device needed) --------------------------- */
 /* validate_circuit (butterfly/core/executors.mojo:129-185) for a state of

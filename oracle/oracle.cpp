@@ -536,6 +536,61 @@ void permute_qubits(St& s, const int32_t* order, int64_t cnt) {
   }
 }
 
+// ---- modular exponentiation (algos/shor.mojo:11-140) ------------------------
+int64_t gcd64(int64_t a, int64_t b) {  // gcd (:11-18)
+  int64_t x = a, y = b;
+  while (y != 0) {
+    int64_t t = x % y;
+    x = y;
+    y = t;
+  }
+  return x < 0 ? -x : x;
+}
+
+uint64_t mulmod_u64(uint64_t a, uint64_t b, uint64_t m) { return (uint64_t)(((unsigned __int128)a * b) % m); }
+
+int64_t modexp64(int64_t base, int64_t e, int64_t m) {  // modexp (:21-32)
+  if (m <= 1) return 0;
+  uint64_t r = 1 % (uint64_t)m, b = (uint64_t)(((base % m) + m) % m);
+  while (e > 0) {
+    if (e & 1) r = mulmod_u64(r, b, (uint64_t)m);
+    b = mulmod_u64(b, b, (uint64_t)m);
+    e >>= 1;
+  }
+  return (int64_t)r;
+}
+
+int64_t modinv64(int64_t a, int64_t m) {  // modinv via egcd (:39-53)
+  int64_t r0 = m, r1 = ((a % m) + m) % m, t0 = 0, t1 = 1;
+  while (r1 != 0) {
+    int64_t q = r0 / r1, r = r0 - q * r1, t = t0 - q * t1;
+    r0 = r1;
+    r1 = r;
+    t0 = t1;
+    t1 = t;
+  }
+  return r0 != 1 ? 0 : ((t0 % m) + m) % m;
+}
+
+// out[x | y_out << n_exp] = in[idx], y_out = y * a^x mod N (or a^-x) for y < N
+void apply_modexp(St& s, int n_exp, int n_value, int64_t a, int64_t N, bool inverse) {
+  std::vector<double> ore(s.N, 0.0), oim(s.N, 0.0);
+  const size_t xm = ((size_t)1 << n_exp) - 1, ym = ((size_t)1 << n_value) - 1;
+  for (size_t idx = 0; idx < s.N; ++idx) {
+    size_t x = idx & xm, y = (idx >> n_exp) & ym, y_out = y;
+    if ((int64_t)y < N) {
+      int64_t ax = modexp64(a, (int64_t)x, N);
+      if (inverse) ax = modinv64(ax, N);
+      y_out = (size_t)mulmod_u64(y, (uint64_t)ax, (uint64_t)N);
+    }
+    size_t out = x | (y_out << n_exp);
+    ore[out] = s.re[idx];
+    oim[out] = s.im[idx];
+  }
+  std::memcpy(s.re, ore.data(), s.N * sizeof(double));
+  std::memcpy(s.im, oim.data(), s.N * sizeof(double));
+}
+
 // ---- validation (executors.mojo:78-185) -----------------------------------
 void check_qubit(int idx, int n, const char* label) {
   if (idx < 0 || idx >= n) fail(BF_EINVAL, "%s out of bounds: %d", label, idx);
@@ -576,6 +631,17 @@ void validate(const St& s, const bf_op* ops, int64_t nops) {
           if (!(o.data[k] >= 0 && o.data[k] < (double)s.N) || o.data[k] != floor(o.data[k]))
             fail(BF_EINVAL, "Oracle index out of range: %.17g", o.data[k]);
         break;
+      case BF_OP_MODEXP:
+      case BF_OP_MODEXP_INV: {  // algos/shor.mojo:60-76
+        const char* name = o.kind == BF_OP_MODEXP ? "MOD_EXP" : "MOD_EXP_INV";
+        if (o.nqubits < 4 || !o.data) fail(BF_EINVAL, "%s expects 4 parameters: n_exp, n_value, a, N", name);
+        int64_t ne = (int64_t)o.data[0], nv = (int64_t)o.data[1], a = (int64_t)o.data[2], N = (int64_t)o.data[3];
+        if (ne <= 0 || nv <= 0) fail(BF_EINVAL, "%s expects positive register sizes", name);
+        if (N <= 1) fail(BF_EINVAL, "%s expects modulus > 1", name);
+        if (gcd64(a, N) != 1) fail(BF_EINVAL, "%s expects a and modulus to be coprime", name);
+        if (ne + nv != n) fail(BF_EINVAL, "State size mismatch for %s", name);
+        break;
+      }
       case BF_OP_UNITARY:
       case BF_OP_CUNITARY: {
         int m = o.target2;
@@ -712,6 +778,11 @@ void run(St& s, const Ctx& c, const bf_op* ops, int64_t nops, bool do_validate) 
         }
         break;
       }
+      case BF_OP_MODEXP:       // apply_modexp (algos/shor.mojo:56-96)
+      case BF_OP_MODEXP_INV:   // apply_modexp_inverse (algos/shor.mojo:99-140)
+        apply_modexp(s, (int)o.data[0], (int)o.data[1], (int64_t)o.data[2], (int64_t)o.data[3],
+                     o.kind == BF_OP_MODEXP_INV);
+        break;
       case BF_OP_CLASSICAL_ORACLE:  // classical_oracle (grover.mojo:64-66)
         for (int64_t k = 0; k < o.nqubits; ++k) {
           size_t i = (size_t)o.data[k];
