@@ -306,9 +306,9 @@ constexpr int kLoopAlwaysQubits = 22;
 // Tensor cores or CUDA cores for one 12-qubit pass: the CUDA-core tile
 // kernel's work in units of one dense gate over the tile, against the blocks
 // the pass needs (one block costs about kBlockUnits dense gates: measured on
-// the 30-qubit complex64 layered circuit, 4.2 ms per block against 0.81 ms
+// the 30-qubit complex64 layered circuit, 2.6 ms per block against 0.81 ms
 // per dense gate, beyond the 2.6 ms that moving the state costs either way).
-constexpr double kBlockUnits = 5.0;
+constexpr double kBlockUnits = 3.3;
 
 static double cuda_core_units(const TilePass& tp) {
   double u = 0;

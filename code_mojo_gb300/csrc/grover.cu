@@ -636,17 +636,6 @@ void launch_grover_loop(State& st, const uint64_t* marked, int nmarked, int iter
       if (try_grover_cluster<PolF32>(st, a)) return;
       break;
   }
-  if (st.shared_gpu) {
-    // a server slot: no grid-wide persistent loop (its CTAs would hold SMs
-    // for the whole search while other slots' kernels wait); the iterations
-    // run as short per-op kernels that the block scheduler interleaves
-    std::vector<double> idx(marked, marked + nmarked);
-    for (int it = 0; it < iters; ++it) {
-      if (nmarked > 0) launch_classical_oracle(st, idx.data(), nmarked);
-      launch_grover_diffuser(st, nullptr, 0);
-    }
-    return;
-  }
   a.spin_limit = 1u << 25;  // x 64 ns sleeps: about 2 s
   // chunks of at least 4096 amplitudes
   int per_sm = 0;
@@ -658,7 +647,12 @@ void launch_grover_loop(State& st, const uint64_t* marked, int nmarked, int iter
   }
   BF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, 0));
   uint64_t resident = (uint64_t)std::max(1, per_sm) * (uint64_t)st.num_sms;
-  const uint64_t cap = (uint64_t)2 * st.num_sms;
+  // a server slot shares the GPU: its loop holds at most kSharedLoopCtas
+  // SMs' worth of CTAs for the whole search, so the other slots keep the rest
+  // (per-op kernels instead would issue four launches per iteration from
+  // every slot at once)
+  constexpr uint64_t kSharedLoopCtas = 16;
+  const uint64_t cap = st.shared_gpu ? kSharedLoopCtas : (uint64_t)2 * st.num_sms;
   uint64_t G = std::max<uint64_t>(1, std::min<uint64_t>(std::min(cap, resident), st.N >> 12));
   a.chunk = (st.N + G - 1) / G;
   a.chunk = (a.chunk + 255) & ~255ull;

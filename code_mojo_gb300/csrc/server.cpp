@@ -17,7 +17,9 @@
 // priority; large ones wait in a queue ordered by that cost (cheapest
 // first: under an offered load above capacity this completes the most
 // requests, and the biggest ones wait) and run only on the large slots, at
-// the lowest priority.
+// the lowest priority.  A large slot takes a small request first once the
+// oldest one has waited 20 ms, so that a backlog of large work cannot hold
+// small requests behind the few small-only slots.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -60,6 +62,7 @@ struct Server {
   std::vector<bf_result> done;
   uint64_t next_id = 1, bytes_in_use = 0, peak_bytes = 0, budget = 0;
   uint64_t submitted = 0, completed = 0, failed = 0, running = 0;
+  double small_wait_s = 0.020;
   bool stop = false;
   std::vector<std::thread> workers;
 };
@@ -123,7 +126,8 @@ static void serve_one(Server& sv, State& st, ServedRequest& r, bf_result& res) {
   o.validate = 1;
   o.specialized = BF_SPEC_ALL;
   o.tile_qubits = sv.opts.tile_qubits;
-  o.renormalize = 2;  // starts from |0...0>: unit norm
+  o.tensor_blocks = 1;  // complex64 requests of 12+ qubits: 5-qubit blocks on the tensor cores
+  o.renormalize = 2;    // starts from |0...0>: unit norm
   execute_ops(st, r.ops.data(), (int64_t)r.ops.size(), o);
   int k = std::min<int>(sv.opts.topk, (int)std::min<uint64_t>(16, st.N));
   res.k = k;
@@ -163,10 +167,17 @@ static void worker_main(Server* sv, int slot) {
       auto fits_large = [&]() {
         return !sv->large_queue.empty() && sv->bytes_in_use + sv->large_queue.front()->bytes() <= sv->budget;
       };
+      // a small request that has waited longer than small_wait_s is served
+      // by any slot before large work
+      auto small_overdue = [&]() {
+        return fits_small() && now_s() - sv->queue.front()->t_submit > sv->small_wait_s;
+      };
       // large slots take large requests first and otherwise help with small ones
-      sv->cv_work.wait(lk, [&]() { return sv->stop || fits_small() || (large_slot && fits_large()); });
+      sv->cv_work.wait_for(lk, std::chrono::milliseconds(5),
+                           [&]() { return sv->stop || fits_small() || (large_slot && fits_large()); });
       if (sv->stop) break;
-      if (large_slot && fits_large()) {
+      if (!fits_small() && !(large_slot && fits_large())) continue;
+      if (large_slot && fits_large() && !small_overdue()) {
         std::pop_heap(sv->large_queue.begin(), sv->large_queue.end(), cheaper_last);
         r = sv->large_queue.back();
         sv->large_queue.pop_back();
