@@ -79,10 +79,19 @@ def test_plan_uses_block_passes_only_when_asked():
 
 
 def test_passes_of_diagonal_gates_stay_on_cuda_cores():
-    """A QFT's passes are mostly controlled phases: cheaper on the CUDA-core
-    tile kernel than as dense blocks."""
-    s = bfy.plan_stats(W.qft_circuit(20), ctx(True))
-    assert s["tile_passes"] > 0 and s["block_passes"] == 0
+    """Controlled phases on many qubit pairs need many blocks but are cheap on
+    the CUDA-core tile kernel: such a pass stays there."""
+    rng = np.random.Generator(np.random.PCG64(3))
+    qc = bfy.QuantumCircuit(16)
+    for q in range(16):
+        qc.h(q)
+    for _ in range(120):
+        c, t = (int(x) for x in rng.permutation(12)[:2])
+        qc.cp(c, t, float(rng.uniform(0, 2 * math.pi)))
+    s = bfy.plan_stats(qc, ctx(True))
+    assert s["tile_passes"] >= 1 and s["block_passes"] < s["tile_passes"]
+    q = bfy.plan_stats(W.qft_circuit(20), ctx(True))
+    assert q["block_passes"] < q["tile_passes"]
 
 
 @pytest.mark.gpu
