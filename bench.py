@@ -115,27 +115,32 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def dist_setup(n_gpus: int):
-    """Returns (rank, world, local_rank); initialises torch.distributed for N>1."""
+def dist_setup(n_gpus: int, backend: str | None = None):
+    """Returns (rank, world, local_rank); initialises torch.distributed for N>1
+    (NCCL with one GPU per rank; gloo where there is no GPU)."""
     if n_gpus > 1 or "RANK" in os.environ:
         import torch
         import torch.distributed as dist
         rank = int(os.environ.get("RANK", 0))
         world = int(os.environ.get("WORLD_SIZE", 1))
         local = int(os.environ.get("LOCAL_RANK", 0))
-        if world > 1:
-            torch.cuda.set_device(local)
-            dist.init_process_group("nccl")
+        if world > 1 and not dist.is_initialized():
+            backend = backend or ("nccl" if torch.cuda.is_available() else "gloo")
+            if backend == "nccl":
+                torch.cuda.set_device(local)
+            dist.init_process_group(backend)
         return rank, world, local
     return 0, 1, 0
 
 
 def barrier_max(value: float, world: int) -> float:
+    """The maximum of `value` over the ranks (each replica's step time)."""
     if world <= 1:
         return value
     import torch
     import torch.distributed as dist
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -311,6 +316,22 @@ def run_precision_bench(n_big: int, n_cmp: int, layers: int) -> dict:
     st.close()
     out["tensor_over_cuda_core_speed"] = ((out["cuda_cores"]["layered_ms"] + out["cuda_cores"]["qft_ms"]) /
                                           (out["tensor_cores"]["layered_ms"] + out["tensor_cores"]["qft_ms"]))
+    # the tensor-core pass as a roofline: 2S per block pass over the layered run's average pass time
+    # (every pass of the layered plan is a block pass or a CUDA-core tile pass of similar length)
+    tp = out["tensor_cores"]["plan_layered"]
+    passes = max(1, tp["tile_passes"] + tp["gate_kernels"])
+    S = float(8 << n_big)
+    peak, src = measured_peaks()
+    launch_ms = out["tensor_cores"]["layered_ms"] / passes
+    blocks = max(1, tp["blocks"])
+    out["roofline_k_tblock"] = {
+        "bound": "tensor", "kernel": "bf::k_tblock", "avg_launch_ms": launch_ms,
+        "hbm": {"achieved": 2 * S / (launch_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                "frac": 2 * S / (launch_ms * 1e-3) / 1e9 / peak, "peak_source": f"{src} hbm_gbs"},
+        # 3 TF32 GEMMs of 128 x 64 x 64 per 128-row tile and block: 3 * 2 * 64 * 64 / 32 flop per amplitude
+        "tensor": {"achieved": 3 * 2 * 64 * 64 / 32 * (1 << n_big) * blocks / passes / (launch_ms * 1e-3) / 1e12,
+                   "unit": "TFLOP/s (TF32)"},
+        "blocks_per_pass": blocks / passes}
     # fidelity at n_cmp qubits against complex128
     qc, qft = W.random_layered_circuit(n_cmp, layers, SEED), W.qft_circuit(n_cmp)
     ref = bfy.QuantumState(n_cmp, "c128")

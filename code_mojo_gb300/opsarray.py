@@ -121,3 +121,25 @@ def grover(n: int, marked: int, iterations: int | None = None) -> OpArray:
     body["nqubits"][0::2] = 1
     body["kind"][1::2] = F.BF_OP_GROVER_DIFFUSER
     return OpArray(n, a, [idx])
+
+
+def adjoint(ops: OpArray) -> OpArray:
+    """The inverse of a circuit of gate records: reversed order, each 2x2
+    matrix conjugate-transposed (X and other self-inverse gates unchanged in
+    effect; P/RX/RY/RZ angles negated)."""
+    a = ops.ops[::-1].copy()
+    gates = a["kind"] == F.BF_OP_GATE
+    if not np.all(gates):
+        raise ValueError("adjoint() takes gate records only")
+    custom = a["gate"] == F.BF_GATE_CUSTOM
+    m = a["mat"][custom]
+    # [[m00, m01], [m10, m11]]^dagger = [[m00*, m10*], [m01*, m11*]]
+    out = np.empty_like(m)
+    out[:, 0], out[:, 1] = m[:, 0], -m[:, 1]
+    out[:, 2], out[:, 3] = m[:, 4], -m[:, 5]
+    out[:, 4], out[:, 5] = m[:, 2], -m[:, 3]
+    out[:, 6], out[:, 7] = m[:, 6], -m[:, 7]
+    a["mat"][custom] = out
+    angled = np.isin(a["gate"], [F.BF_GATE_P, F.BF_GATE_RX, F.BF_GATE_RY, F.BF_GATE_RZ])
+    a["arg"][angled] = -a["arg"][angled]
+    return OpArray(ops.num_qubits, a, list(ops.keep))

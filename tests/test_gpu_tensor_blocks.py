@@ -201,3 +201,27 @@ def test_inner_product_matches_numpy(da, db):
     b.close()
     exp = np.vdot(xa, xb)
     assert abs(got - exp) <= 1e-13
+
+
+def test_adjoint_op_array_inverts_on_the_oracle():
+    from code_mojo_gb300 import opsarray as OA
+    ops = OA.random_layered(8, 6, 3)
+    both = OA.OpArray(8, np.concatenate([ops.ops, OA.adjoint(ops).ops]), [])
+    r, i = O.run(both, *O.basis(8))
+    assert abs(r[0] - 1) <= 1e-12 and np.max(np.abs(r[1:])) <= 1e-12 and np.max(np.abs(i)) <= 1e-12
+
+
+@pytest.mark.gpu
+def test_30q_layered_round_trip_on_tensor_cores():
+    """Full size: the 40-layer circuit then its adjoint returns |0> on the
+    tensor-core path (complex64, 8 GiB)."""
+    from code_mojo_gb300 import opsarray as OA
+    n = 30
+    ops = OA.random_layered(n, 40, 0)
+    assert bfy.plan_stats(ops, ctx(True))["block_passes"] > 0
+    st = bfy.QuantumState(n, "c64")
+    bfy.execute(st, ops, ctx(True))
+    bfy.execute(st, OA.adjoint(ops), ctx(True))
+    top_idx, top_p = st.topk(1)
+    st.close()
+    assert int(top_idx[0]) == 0 and top_p[0] >= 1 - 1e-5
