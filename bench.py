@@ -483,6 +483,7 @@ def run_ours(args) -> None:
         "per_gate_path": per_gate,
         "gpu_launches": launches,
         "norm_after": norm,
+        "norm_after_circuits": args.warmup + args.steps,  # applications of the circuit to the state since |0>
         "clocks": clk.summary(),
         "e2e": e2e,
         "cpu_baseline": cpu,

@@ -92,6 +92,21 @@ __device__ __forceinline__ dfl df_dot4(dfl a0, dfl b0, dfl a1, dfl b1, dfl a2,
   return df_norm(s, err);
 }
 
+// a0*b0 + a1*b1 + a2*b2, as df_dot4
+__device__ __forceinline__ dfl df_dot3(dfl a0, dfl b0, dfl a1, dfl b1, dfl a2, dfl b2) {
+  float p0 = __fmul_rn(a0.hi, b0.hi), e0 = fmaf(a0.hi, b0.hi, -p0);
+  float p1 = __fmul_rn(a1.hi, b1.hi), e1 = fmaf(a1.hi, b1.hi, -p1);
+  float p2 = __fmul_rn(a2.hi, b2.hi), e2 = fmaf(a2.hi, b2.hi, -p2);
+  e0 = fmaf(a0.hi, b0.lo, fmaf(a0.lo, b0.hi, e0));
+  e1 = fmaf(a1.hi, b1.lo, fmaf(a1.lo, b1.hi, e1));
+  e2 = fmaf(a2.hi, b2.lo, fmaf(a2.lo, b2.hi, e2));
+  float s, t1, t2;
+  two_sum(p0, p1, s, t1);
+  two_sum(s, p2, s, t2);
+  float err = __fadd_rn(__fadd_rn(e0, e1), __fadd_rn(e2, __fadd_rn(t1, t2)));
+  return df_norm(s, err);
+}
+
 // a0*b0 + a1*b1
 __device__ __forceinline__ dfl df_dot2(dfl a0, dfl b0, dfl a1, dfl b1) {
   float p0 = __fmul_rn(a0.hi, b0.hi), e0 = fmaf(a0.hi, b0.hi, -p0);
@@ -214,6 +229,7 @@ struct PolF64 {
     v.re = a.re * m[4] - a.im * m[5] + b.re * m[6] - b.im * m[7];
     v.im = a.re * m[5] + a.im * m[4] + b.re * m[7] + b.im * m[6];
   }
+  __device__ static __forceinline__ void dense_r(R& u, R& v, const Coef& g) { dense(u, v, g); }
   __device__ static __forceinline__ void hadamard(R& u, R& v) {
     R a = u, b = v;
     u.re = (a.re + b.re) * kSqHalf;
@@ -281,6 +297,15 @@ struct PolDF {
     v.re = df_dot4(a.re, m[4], df_neg(a.im), m[5], b.re, m[6], df_neg(b.im), m[7]);
     v.im = df_dot4(a.re, m[5], a.im, m[4], b.re, m[7], b.im, m[6]);
   }
+  // m00 real (m[1] == 0): the a-terms of u need one product each
+  __device__ static __forceinline__ void dense_r(R& u, R& v, const Coef& g) {
+    const dfl* m = g.v;
+    R a = u, b = v;
+    u.re = df_dot3(a.re, m[0], b.re, m[2], df_neg(b.im), m[3]);
+    u.im = df_dot3(a.im, m[0], b.re, m[3], b.im, m[2]);
+    v.re = df_dot4(a.re, m[4], df_neg(a.im), m[5], b.re, m[6], df_neg(b.im), m[7]);
+    v.im = df_dot4(a.re, m[5], a.im, m[4], b.re, m[7], b.im, m[6]);
+  }
   __device__ static __forceinline__ void hadamard(R& u, R& v) {
     const dfl s = dfl{kSqHalfHi, kSqHalfLo};
     R a = u, b = v;
@@ -344,6 +369,7 @@ struct PolF32 {
   // the norm at every H.  x*hi + x*lo with one FMA keeps the product within
   // half an ulp of x*sqrt(0.5), so no bias builds up.
   __device__ static __forceinline__ float mul_sq_half(float x) { return fmaf(x, kSqHalfHi, x * kSqHalfLo); }
+  __device__ static __forceinline__ void dense_r(R& u, R& v, const Coef& g) { dense(u, v, g); }
   __device__ static __forceinline__ void hadamard(R& u, R& v) {
     R a = u, b = v;
     u.re = mul_sq_half(a.re + b.re);
@@ -382,6 +408,7 @@ __device__ __forceinline__ void apply_pair(int kind, typename P::R& u,
     case 2: { typename P::R t = u; u = v; v = t; break; }  // GK_SWAP
     case 3: P::cmul(v, g, 6); break;             // GK_PHASE
     case 4: P::cmul(u, g, 0); P::cmul(v, g, 6); break;  // GK_DIAG
+    case 6: P::dense_r(u, v, g); break;          // GK_DENSE_R
     default: P::ry(u, v, g); break;              // GK_RY
   }
 }

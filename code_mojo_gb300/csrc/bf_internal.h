@@ -39,7 +39,8 @@ enum GKind : int32_t {
   GK_SWAP = 2,   // X: exchange the pair
   GK_PHASE = 3,  // diag(1, e^{i theta}): m[6], m[7] = cos, sin (P, Z, CP, CZ, MCP)
   GK_DIAG = 4,   // diag(d0, d1): m[0..1] = d0, m[6..7] = d1 (RZ)
-  GK_RY = 5      // real rotation [[c,-s],[s,c]]: m[0] = c, m[4] = s
+  GK_RY = 5,     // real rotation [[c,-s],[s,c]]: m[0] = c, m[4] = s
+  GK_DENSE_R = 6 // full 2x2 matrix whose m00 is real (m[1] == 0), as in every U3
 };
 
 struct GateInstr {

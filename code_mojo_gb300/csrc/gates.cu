@@ -98,6 +98,7 @@ static void launch_gate_p(State& st, const GateInstr& g) {
     case GK_PHASE: k_gate<P, GK_PHASE><<<(unsigned)blocks, 256, 0, st.stream>>>(s, a); break;
     case GK_DIAG: k_gate<P, GK_DIAG><<<(unsigned)blocks, 256, 0, st.stream>>>(s, a); break;
     case GK_RY: k_gate<P, GK_RY><<<(unsigned)blocks, 256, 0, st.stream>>>(s, a); break;
+    case GK_DENSE_R: k_gate<P, GK_DENSE_R><<<(unsigned)blocks, 256, 0, st.stream>>>(s, a); break;
     default: fail(BF_EINVAL, "internal: unknown lowered gate kind %d", g.kind);
   }
   BF_CUDA(cudaGetLastError());

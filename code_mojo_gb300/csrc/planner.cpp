@@ -192,7 +192,7 @@ GateInstr lower_gate(const bf_op& o, uint32_t spec) {
              (m[1] == 0 && m[3] == 0 && m[5] == 0 && m[7] == 0 && m[0] == m[6] && m[2] == -m[4])) {
     g.kind = GK_RY;  // real rotation [[c, -s], [s, c]]
   } else {
-    g.kind = GK_DENSE;
+    g.kind = m[1] == 0 ? GK_DENSE_R : GK_DENSE;  // U3: m00 = cos(theta/2) is real
   }
   split_pairs(g);
   return g;

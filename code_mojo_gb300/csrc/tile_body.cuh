@@ -15,6 +15,51 @@ struct TileGeom {
   int32_t q[kMaxTileQubits];
 };
 
+// One in-tile gate over all its pairs: the gate kind and whether it has
+// controls inside the tile are compile-time, so the pair loop carries no
+// dispatch; indices are 32-bit (a tile has at most 2^13 amplitudes).
+template <class P, int KIND, bool kCtl>
+__device__ __forceinline__ void tile_pairs(typename P::Smem* amp, int TS, int tloc, uint32_t cml,
+                                           const typename P::Coef& g) {
+  using R = typename P::R;
+  using S = typename P::Smem;
+  const uint32_t low = (1u << tloc) - 1u, tb = 1u << tloc;
+#pragma unroll 2
+  for (int p = threadIdx.x; p < (TS >> 1); p += kTileThreads) {
+    const uint32_t i0 = (((uint32_t)p & ~low) << 1) | ((uint32_t)p & low);
+    if (kCtl && (i0 & cml) != cml) continue;
+    const uint32_t i1 = i0 | tb;
+    if (KIND == GK_SWAP) {
+      S t = amp[i0];
+      amp[i0] = amp[i1];
+      amp[i1] = t;
+    } else if (KIND == GK_PHASE) {
+      R v = P::from_smem(amp[i1]);
+      P::cmul(v, g, 6);
+      amp[i1] = P::to_smem(v);
+    } else {
+      R u = P::from_smem(amp[i0]), v = P::from_smem(amp[i1]);
+      apply_pair<P>(KIND, u, v, g);
+      amp[i0] = P::to_smem(u);
+      amp[i1] = P::to_smem(v);
+    }
+  }
+}
+
+template <class P, bool kCtl>
+__device__ __forceinline__ void tile_gate(int kind, typename P::Smem* amp, int TS, int tloc, uint32_t cml,
+                                          const typename P::Coef& g) {
+  switch (kind) {
+    case GK_DENSE: tile_pairs<P, GK_DENSE, kCtl>(amp, TS, tloc, cml, g); break;
+    case GK_H: tile_pairs<P, GK_H, kCtl>(amp, TS, tloc, cml, g); break;
+    case GK_SWAP: tile_pairs<P, GK_SWAP, kCtl>(amp, TS, tloc, cml, g); break;
+    case GK_PHASE: tile_pairs<P, GK_PHASE, kCtl>(amp, TS, tloc, cml, g); break;
+    case GK_DIAG: tile_pairs<P, GK_DIAG, kCtl>(amp, TS, tloc, cml, g); break;
+    case GK_DENSE_R: tile_pairs<P, GK_DENSE_R, kCtl>(amp, TS, tloc, cml, g); break;
+    default: tile_pairs<P, GK_RY, kCtl>(amp, TS, tloc, cml, g); break;
+  }
+}
+
 // One tile: load the 2^K amplitudes of tile `tile` (the non-tile qubits set
 // to the bits of `tile`), apply ops[0..nops) in shared memory, store.  Called
 // by every thread of a CTA of kTileThreads threads; `smem_raw` holds
@@ -63,26 +108,8 @@ __device__ __forceinline__ void run_tile(typename P::Glob* __restrict__ s, const
     const uint32_t cml = __ldg(&op->cmask_loc);
     const typename P::Coef g = P::coef(op->m, op->mhl);
     if (tloc >= 0) {
-      const int tb = 1 << tloc;
-      for (int p = tid; p < (TS >> 1); p += kTileThreads) {
-        int i0 = (int)insert_zero_bit((uint64_t)p, tloc);
-        if ((i0 & cml) != cml) continue;
-        int i1 = i0 | tb;
-        if (kind == GK_SWAP) {
-          S t = amp[i0];
-          amp[i0] = amp[i1];
-          amp[i1] = t;
-        } else if (kind == GK_PHASE) {
-          R v = P::from_smem(amp[i1]);
-          P::cmul(v, g, 6);
-          amp[i1] = P::to_smem(v);
-        } else {
-          R u = P::from_smem(amp[i0]), v = P::from_smem(amp[i1]);
-          apply_pair<P>(kind, u, v, g);
-          amp[i0] = P::to_smem(u);
-          amp[i1] = P::to_smem(v);
-        }
-      }
+      if (cml) tile_gate<P, true>(kind, amp, TS, tloc, cml, g);
+      else tile_gate<P, false>(kind, amp, TS, tloc, 0u, g);
     } else {
       // diagonal gate, target outside the tile: one entry for the whole CTA
       const int tg = __ldg(&op->tglob);
