@@ -2,6 +2,7 @@
 // and bf_execute, the GPU counterpart of execute_with_handlers
 // (butterfly/core/executors.mojo:268-319).
 #include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -138,6 +139,7 @@ static void upload_program(State& st, const Program& pg) {
       size_t cap = std::max(aux, 2 * st.aux_cap);
       host_retire(st, st.h_aux);
       dev_free(st, st.d_aux);
+    dev_free(st, st.d_scale);
       st.h_aux = nullptr;
       st.d_aux = nullptr;
       st.aux_cap = 0;
@@ -177,6 +179,7 @@ struct Step {
   size_t blk_off = 0;            // tensor-core pass: its blocks in the program
   int nblk = 0;
   uint64_t base = 0, modulus = 0;  // modexp: a (or a^-1 mod N) and N; a = n_exp
+  bool digits = false;             // tensor-core pass in the complex128 digit form
 };
 
 // a^-1 mod N for gcd(a, N) = 1 (extended Euclid, as modinv in algos/shor.mojo:46-53)
@@ -327,12 +330,52 @@ static double cuda_core_units(const TilePass& tp) {
   return u;
 }
 
-// tensor: complex64 tile passes as tensor-core block passes (12-qubit tiles)
+// complex128 digit blocks against the double-float tile kernel: one block
+// costs about this many double-float dense gates
+constexpr double kDigitBlockUnits = 2.5;
+
+// True when every op keeps the state's norm (unitary gates and unitaries to
+// 1e-12, permutations and the classical Grover and modexp passes; not
+// measurement): the digit form's scale, taken from the norm before the
+// circuit, then holds for every pass.
+static bool norm_preserving(const bf_op* ops, int64_t nops) {
+  auto unitary = [](const double* m, int dim) {
+    for (int r = 0; r < dim; ++r)
+      for (int c = 0; c < dim; ++c) {
+        double re = 0, im = 0;
+        for (int k = 0; k < dim; ++k) {
+          const double ar = m[2 * (k * dim + r)], ai = -m[2 * (k * dim + r) + 1];  // conj(m[k][r])
+          const double br = m[2 * (k * dim + c)], bi = m[2 * (k * dim + c) + 1];
+          re += ar * br - ai * bi;
+          im += ar * bi + ai * br;
+        }
+        if (std::fabs(re - (r == c ? 1.0 : 0.0)) > 1e-12 || std::fabs(im) > 1e-12) return false;
+      }
+    return true;
+  };
+  for (int64_t i = 0; i < nops; ++i) {
+    const bf_op& op = ops[i];
+    if (op.kind == BF_OP_MEASURE) return false;
+    if (op.kind == BF_OP_GATE) {
+      GateInstr g = lower_gate(op, 0);
+      if (!unitary(g.m, 2)) return false;
+    } else if (op.kind == BF_OP_UNITARY || op.kind == BF_OP_CUNITARY) {
+      if (op.target2 <= 0 || op.target2 > 6 || !op.data || !unitary(op.data, 1 << op.target2)) return false;
+    }
+  }
+  return true;
+}
+
+// tensor: tile passes as tensor-core block passes (12-qubit tiles), in
+// `format` (BLOCK_TF32 for complex64, BLOCK_DIGITS for complex128)
 static void build_steps(int n, const bf_op* ops, int64_t nops, const bf_exec_opts& o, std::vector<Step>& steps,
-                        Program& pg, bool grover_loop_large = true, bool tensor = false) {
+                        Program& pg, bool grover_loop_large = true, bool tensor = false,
+                        BlockFormat format = BLOCK_TF32) {
   std::vector<TileOp>& prog = pg.ops;
   const bool fused = o.strategy == BF_STRATEGY_GPU_FUSED;
   tensor = tensor && fused && n >= kBlockTileQubits;
+  if (tensor && format == BLOCK_DIGITS) tensor = norm_preserving(ops, nops);
+  const double block_units = format == BLOCK_DIGITS ? kDigitBlockUnits : kBlockUnits;
   const int K = tensor ? kBlockTileQubits : (o.tile_qubits > 0 ? o.tile_qubits : 11);
   std::vector<GateInstr> run;
   auto flush = [&]() {
@@ -341,9 +384,10 @@ static void build_steps(int n, const bf_op* ops, int64_t nops, const bf_exec_opt
       Step s;
       if (ps.is_tile && tensor && ps.tile.K == kBlockTileQubits && ps.tile.L == kTileLowQubits) {
         size_t b0 = pg.blocks.size(), i0 = pg.images.size(), o0 = pg.offsets.size();
-        if (plan_blocks(ps.tile, pg.blocks, pg.images, pg.offsets) &&
-            (double)(pg.blocks.size() - b0) * kBlockUnits < cuda_core_units(ps.tile)) {
+        if (plan_blocks(ps.tile, pg.blocks, pg.images, pg.offsets, format) &&
+            (double)(pg.blocks.size() - b0) * block_units < cuda_core_units(ps.tile)) {
           s.kind = Step::TBLOCK;
+          s.digits = format == BLOCK_DIGITS;
           s.tile = ps.tile;
           s.tile.ops.clear();
           s.blk_off = b0;
@@ -568,14 +612,27 @@ static void build_steps(int n, const bf_op* ops, int64_t nops, const bf_exec_opt
 
 static void run_steps(State& st, std::vector<Step>& steps, const Program& pg) {
   upload_program(st, pg);
+  bool scaled = false;
   for (auto& s : steps) {
     switch (s.kind) {
       case Step::GATE: launch_gate(st, s.gate); break;
       case Step::TILE: launch_tile_pass(st, st.d_prog + s.prog_off, s.nprog, s.tile); break;
       case Step::TBLOCK:
-        launch_block_pass(st, reinterpret_cast<const Blk5*>(st.d_aux) + s.blk_off, s.nblk,
-                          st.d_aux + pg.images_offset(),
-                          reinterpret_cast<const uint16_t*>(st.d_aux + pg.offsets_offset()), s.tile);
+        if (s.digits) {
+          if (!scaled) {  // the digit scale, from the norm before the first digit pass
+            if (!st.d_scale) st.d_scale = static_cast<int*>(dev_alloc(st, 16));
+            launch_digit_scale(st, st.d_scale);
+            scaled = true;
+          }
+          launch_block_pass_digits(st, reinterpret_cast<const Blk5*>(st.d_aux) + s.blk_off, s.nblk,
+                                   st.d_aux + pg.images_offset(),
+                                   reinterpret_cast<const uint16_t*>(st.d_aux + pg.offsets_offset()), s.tile,
+                                   st.d_scale);
+        } else {
+          launch_block_pass(st, reinterpret_cast<const Blk5*>(st.d_aux) + s.blk_off, s.nblk,
+                            st.d_aux + pg.images_offset(),
+                            reinterpret_cast<const uint16_t*>(st.d_aux + pg.offsets_offset()), s.tile);
+        }
         break;
       case Step::BITREV: launch_bitrev_full(st); break;
       case Step::PERMUTE: launch_permute(st, s.src_of.data()); break;
@@ -606,7 +663,8 @@ void execute_ops(State& st, const bf_op* ops, int64_t nops, bf_exec_opts o) {
   if (o.validate) validate_ops(st.n, ops, nops);
   std::vector<Step> steps;
   Program prog;
-  build_steps(st.n, ops, nops, o, steps, prog, !st.shared_gpu, o.tensor_blocks != 0 && st.dtype == BF_C64);
+  build_steps(st.n, ops, nops, o, steps, prog, !st.shared_gpu, o.tensor_blocks != 0,
+              st.dtype == BF_C128 ? BLOCK_DIGITS : BLOCK_TF32);
   // FP32 matrices are unitary only to ~6e-8, and that error changes the norm
   // coherently at every gate; the complex64 form restores the input norm.
   // renormalize == 2 (internal): the input is known to have unit norm.

@@ -103,14 +103,26 @@ struct Blk5 {
   uint32_t load_offs; // first block of a pass: destinations of the loaded tile
 };
 
+// Two operand formats for the blocks:
+//   BLOCK_TF32   complex64: FP32 operands split into TF32 hi and lo (3xTF32);
+//                a matrix image is 32 KiB.
+//   BLOCK_DIGITS complex128: values as 6 signed base-256 digits held exactly
+//                in bf16 (x / scale = 2^-8 sum_i d_i 2^-8i); the digit
+//                products accumulate exactly in FP32 per digit level; a
+//                matrix image is 6 digit planes of 8 KiB.
+enum BlockFormat { BLOCK_TF32 = 0, BLOCK_DIGITS = 1 };
+constexpr int kDigits = 6;
+constexpr uint32_t kDigitImageBytes = kDigits * 8192;
+
 // Partitions the ops of a 12-qubit tile pass into blocks and appends their
 // matrix images and destination tables (u16 per thread and element: the
-// next block's operand offset / 8, or after the last block the staging
-// slot); false when an op cannot be placed (more than 5 tile qubits or more
-// than 3 outside qubits on its own) or the pass needs more than
-// kMaxPassBlocks blocks.
+// next block's operand offset in the format's units, or after the last
+// block the staging slot); false when an op cannot be placed (more than 5
+// tile qubits or more than 3 outside qubits on its own), the pass needs more
+// than kMaxPassBlocks blocks, or (BLOCK_DIGITS) a block's matrix is not
+// unitary to 1e-12.
 bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsigned char>& images,
-                 std::vector<uint16_t>& offsets);
+                 std::vector<uint16_t>& offsets, BlockFormat format = BLOCK_TF32);
 #ifdef __CUDACC__
 #define BF_HOST_DEVICE __host__ __device__
 #else
@@ -120,6 +132,12 @@ bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsi
 // complex element (row g, column j) in a K-major, 128-byte-swizzled operand
 BF_HOST_DEVICE inline uint32_t block_operand_offset(uint32_t g, uint32_t j) {
   return ((j >> 4) << 14) + (g << 7) + ((((j & 15) >> 1) ^ (g & 7)) << 4) + ((j & 1) << 3);
+}
+// byte offset of complex element (row g, column j) in one bf16 digit plane:
+// K-major rows of 64 bf16 (re, im interleaved), 16-byte chunks swizzled by
+// the row's low three bits; 16 KiB per plane
+BF_HOST_DEVICE inline uint32_t digit_operand_offset(uint32_t g, uint32_t j) {
+  return (g << 7) + ((((j >> 2) ^ (g & 7))) << 4) + ((j & 3) << 2);
 }
 // staging slot of tile element i after the last block (pairs stay adjacent)
 BF_HOST_DEVICE inline uint32_t block_stage_slot(uint32_t i) { return i ^ (((i >> 5) & 15u) << 1); }
@@ -171,6 +189,8 @@ struct State {
   unsigned char* d_aux = nullptr;
   unsigned char* h_aux = nullptr;
   size_t aux_cap = 0;
+  // scale exponent of the complex128 digit passes (device int)
+  int* d_scale = nullptr;
 
   // pinned host buffers outgrown while copies from them may be in flight;
   // freed with the state (cudaFreeHost can synchronise the device)
@@ -203,6 +223,12 @@ void launch_gate(State& s, const GateInstr& g);
 void launch_tile_pass(State& s, const TileOp* d_ops, int nops, const TilePass& p);
 void launch_block_pass(State& st, const Blk5* d_blocks, int nblocks, const unsigned char* d_images,
                        const uint16_t* d_offsets, const TilePass& p);
+// complex128 digit blocks (BLOCK_DIGITS); d_exp holds the scale exponent
+// that launch_digit_scale computed from the state's norm
+void launch_block_pass_digits(State& st, const Blk5* d_blocks, int nblocks, const unsigned char* d_images,
+                              const uint16_t* d_offsets, const TilePass& p, const int* d_exp);
+void launch_digit_scale(State& st, int* d_exp);
+void launch_norm2_partials(State& st, unsigned blocks);  // into st.d_partial (ensure_partials first)
 void launch_bitrev_full(State& s);
 void launch_permute(State& s, const int32_t* src_bit_of_dst);  // dst bit j <- src bit perm[j]
 void launch_swap_bits(State& s, int a, int b);

@@ -54,6 +54,46 @@ void block_image(const double* u, unsigned char* img) {
     }
 }
 
+// Digits of a value v with |v| <= 1 as r = 2^-8 sum_j e_j 2^-8j: balanced
+// base-256 digits e_1..e_5 in [-128, 127] and the leading e_0 in [-256, 256],
+// from the nearest integer to v * 2^48.
+static void value_digits(double v, int* e) {
+  long long V = std::llround(std::ldexp(v, 48));
+  for (int j = kDigits - 1; j >= 1; --j) {
+    long long d = ((V & 255) ^ 128) - 128;
+    e[j] = (int)d;
+    V = (V - d) >> 8;
+  }
+  e[0] = (int)V;
+}
+
+static uint16_t bf16_of_int(int d) {  // exact for |d| <= 256
+  float f = (float)d;
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  return (uint16_t)(u >> 16);
+}
+
+// The digit image of a 32x32 complex matrix: R^T as in block_image, each
+// entry as 6 bf16 digit planes (plane j holds e_j), K-major with the
+// 128-byte swizzle, 8 KiB per plane.
+void block_image_digits(const double* u, unsigned char* img) {
+  std::memset(img, 0, kDigitImageBytes);
+  for (int n = 0; n < 64; ++n)
+    for (int k = 0; k < 64; ++k) {
+      const int j = n >> 1, d = n & 1, l = k >> 1, c = k & 1;
+      const double re = u[2 * (j * 32 + l)], im = u[2 * (j * 32 + l) + 1];
+      const double v = c == 0 ? (d == 0 ? re : im) : (d == 0 ? -im : re);
+      int e[kDigits];
+      value_digits(v, e);
+      const size_t off = (size_t)n * 128 + (size_t)((((2 * k) >> 4) ^ (n & 7)) << 4) + (size_t)((2 * k) & 15);
+      for (int p = 0; p < kDigits; ++p) {
+        uint16_t h = bf16_of_int(e[p]);
+        std::memcpy(img + (size_t)p * 8192 + off, &h, 2);
+      }
+    }
+}
+
 namespace {
 
 struct BlockBuild {
@@ -114,7 +154,14 @@ BlockMap make_map(uint32_t T, uint32_t lane_positions) {
 }  // namespace
 
 bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsigned char>& images,
-                 std::vector<uint16_t>& offsets) {
+                 std::vector<uint16_t>& offsets, BlockFormat format) {
+  const uint32_t image_bytes = format == BLOCK_DIGITS ? kDigitImageBytes : kBlockImageBytes;
+  // destination of complex element (g, j) of a block's operands, in the
+  // units of the kernel's table (TF32: bytes / 8; digits: bytes / 4 in a plane)
+  auto dest = [&](uint32_t g, uint32_t j) {
+    return format == BLOCK_DIGITS ? (uint16_t)(digit_operand_offset(g, j) >> 2)
+                                  : (uint16_t)(block_operand_offset(g, j) >> 3);
+  };
   if (tp.K != kBlockTileQubits) return false;
   std::vector<BlockBuild> bl;
   // Each op goes into the earliest block at or after the last block that
@@ -165,7 +212,7 @@ bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsi
     d.tmask = T;
     for (int q = 0; q < 64; ++q)
       if ((b.outs >> q) & 1ull) d.outpos[d.nout++] = q;
-    d.img = (uint32_t)(images.size() / kBlockImageBytes);
+    d.img = (uint32_t)(images.size() / image_bytes);
     const int variants = 1 << d.nout;
     std::vector<cd> U(32 * 32);
     std::vector<double> flat(2 * 32 * 32);
@@ -210,9 +257,21 @@ bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsi
         flat[2 * i] = U[i].real();
         flat[2 * i + 1] = U[i].imag();
       }
+      if (format == BLOCK_DIGITS) {
+        // the digit form is exact only for entries of modulus <= 1: unitary blocks
+        double worst = 0;
+        for (int r = 0; r < 32; ++r)
+          for (int c = 0; c < 32; ++c) {
+            cd acc(0.0, 0.0);
+            for (int k = 0; k < 32; ++k) acc += std::conj(U[k * 32 + r]) * U[k * 32 + c];
+            worst = std::max(worst, std::abs(acc - (r == c ? cd(1.0, 0.0) : cd(0.0, 0.0))));
+          }
+        if (worst > 1e-12) return false;
+      }
       size_t at = images.size();
-      images.resize(at + kBlockImageBytes);
-      block_image(flat.data(), images.data() + at);
+      images.resize(at + image_bytes);
+      if (format == BLOCK_DIGITS) block_image_digits(flat.data(), images.data() + at);
+      else block_image(flat.data(), images.data() + at);
     }
     blocks.push_back(d);
   }
@@ -231,7 +290,7 @@ bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsi
       for (int e = 0; e < kBlockThreadElems; ++e) {
         uint32_t i = (uint32_t)(((e >> 1) * kBlockThreads + t) * 2 + (e & 1)), g, j;
         maps[0].ext(i, g, j);
-        offsets[at + (size_t)t * kBlockThreadElems + e] = (uint16_t)(block_operand_offset(g, j) >> 3);
+        offsets[at + (size_t)t * kBlockThreadElems + e] = dest(g, j);
       }
   }
   for (size_t k = 0; k < maps.size(); ++k) {
@@ -248,7 +307,7 @@ bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsi
         if (k + 1 < maps.size()) {
           uint32_t g2, j2;
           maps[k + 1].ext(i, g2, j2);
-          v = (uint16_t)(block_operand_offset(g2, j2) >> 3);
+          v = dest(g2, j2);
         } else {
           v = (uint16_t)block_stage_slot(i);
         }

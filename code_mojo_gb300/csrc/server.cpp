@@ -126,8 +126,10 @@ static void serve_one(Server& sv, State& st, ServedRequest& r, bf_result& res) {
   o.validate = 1;
   o.specialized = BF_SPEC_ALL;
   o.tile_qubits = sv.opts.tile_qubits;
-  o.tensor_blocks = 1;  // complex64 requests of 12+ qubits: 5-qubit blocks on the tensor cores
-  o.renormalize = 2;    // starts from |0...0>: unit norm
+  // no tensor-core passes: their persistent grids take every SM's shared
+  // memory for the whole pass, which the other slots' kernels then wait for
+  o.tensor_blocks = 0;
+  o.renormalize = 2;  // starts from |0...0>: unit norm
   execute_ops(st, r.ops.data(), (int64_t)r.ops.size(), o);
   int k = std::min<int>(sv.opts.topk, (int)std::min<uint64_t>(16, st.N));
   res.k = k;

@@ -315,6 +315,16 @@ static void ensure_renorm(State& st, unsigned blocks) {
   st.renorm_cap = need;
 }
 
+// sum |amp|^2 partials (hi, lo per CTA) into st.d_partial, stream-ordered
+void launch_norm2_partials(State& st, unsigned blocks) {
+  if (st.dtype == BF_C128)
+    k_norm2<double2><<<blocks, 256, 0, st.stream>>>(static_cast<const double2*>(st.amp), st.N, st.d_partial);
+  else
+    k_norm2<float2><<<blocks, 256, 0, st.stream>>>(static_cast<const float2*>(st.amp), st.N, st.d_partial);
+  BF_CUDA(cudaGetLastError());
+  st.launches++;
+}
+
 void launch_norm_before(State& st) {
   if (st.dtype != BF_C64) return;
   unsigned blocks = renorm_blocks(st);

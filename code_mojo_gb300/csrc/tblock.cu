@@ -347,6 +347,387 @@ __global__ void __launch_bounds__(kBlkThreads, 2) k_tblock(const BlkPassArgs a) 
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
 }
 
+// ---- complex128: digit blocks on the bf16 tensor cores -----------------------
+// A complex128 value x becomes 6 signed base-256 digits, x / scale =
+// 2^-8 sum_i d_i 2^-8i with d_i integers of at most 8 bits plus sign, each
+// exact in bf16; the matrix likewise (r = 2^-8 sum_j e_j 2^-8j).  For every
+// digit level s = i + j <= 6 the 4 MMAs of each pair (i, j) (kind::f16, bf16
+// inputs, K = 16) accumulate sum_K d_i e_j into one FP32 accumulator; every
+// product and partial sum is an integer below 2^24, so the accumulation is
+// exact whatever the order.  The epilogue turns the 7 level sums back into
+// the next block's digits by carries between levels (FP32 on exact
+// integers), or after the last block into the FP64 result.  scale is a power
+// of two at least twice the state's norm, so every amplitude of a unitary
+// circuit stays below scale / 2; a pass runs in this form only when all its
+// blocks are unitary.  Dropping the levels s >= 7 and rounding below the
+// sixth digit leave errors of about 2^-48 scale per block.
+constexpr uint32_t kDgPlane = 16384;                       // 128 rows x 64 bf16
+constexpr uint32_t kDgSmemB = kDigits * kDgPlane;          // 6 A planes, then B
+constexpr uint32_t kDgSmemHoff = kDgSmemB + kDigitImageBytes;
+constexpr uint32_t kDgSmemBar = kDgSmemHoff + 128 * 8;
+constexpr uint32_t kDgSmemUsed = kDgSmemBar + 32;
+constexpr uint32_t kDgSmemAlloc = kDgSmemUsed + 1024;
+constexpr uint32_t kDgTmemCols = 512;                      // 7 levels x 64 columns
+constexpr int kDgLevels = 7;
+
+struct DgPassArgs {
+  double2* s;
+  const Blk5* blocks;
+  const unsigned char* images;  // kDigitImageBytes per image
+  const uint16_t* offsets;
+  uint64_t ntiles;
+  int32_t nblocks;
+  int32_t q[kBlockTileQubits];
+  const int* scale_exp;         // device: scale = 2^scale_exp
+  int* flag;
+  uint32_t spin_limit;
+};
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void load_image_bytes(uint32_t dst, const void* src, uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+
+// rint for |x| < 2^22 on the FP32 pipe
+__device__ __forceinline__ float rint_small(float x) {
+  return __fsub_rn(__fadd_rn(x, 12582912.0f), 12582912.0f);
+}
+__device__ __forceinline__ int int_of_small(float x) {  // exact integer-valued |x| < 2^22
+  return __float_as_int(__fadd_rn(x, 12582912.0f)) - 0x4B400000;
+}
+__device__ __forceinline__ float float_of_small(int v) {  // |v| < 2^22
+  return __fsub_rn(__int_as_float(0x4B400000 + v), 12582912.0f);
+}
+// two exact small-integer floats -> (bf16 lo | bf16 hi << 16)
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632);
+}
+
+// round(x * 2^sh) as an integer of at most 48 bits and its 6 digits; false
+// when |x * 2^sh| >= 2^47 (the scale does not cover x)
+__device__ __forceinline__ bool digits_of(double x, int sh, float* d) {
+  const long long b = __double_as_longlong(x);
+  const int ex = (int)((b >> 52) & 0x7ff);
+  const long long m = (b & 0x000FFFFFFFFFFFFFll) | 0x0010000000000000ll;
+  const int k = ex - 1075 + sh;  // |x| 2^sh = m 2^k
+  long long V = 0;
+  bool ok = true;
+  if (ex != 0 && k > -64) {
+    if (k > -6) {
+      ok = false;
+    } else {
+      V = (m + (1ll << (-k - 1))) >> (-k);
+    }
+  }
+  if (b < 0) V = -V;
+#pragma unroll
+  for (int j = kDigits - 1; j >= 1; --j) {
+    const long long t = ((V & 255) ^ 128) - 128;
+    d[j] = float_of_small((int)t);
+    V = (V - t) >> 8;
+  }
+  d[0] = float_of_small((int)V);
+  return ok;
+}
+
+// V * 2^e as a double, |V| < 2^53 (exact)
+__device__ __forceinline__ double double_of(long long V, int e) {
+  if (V == 0) return 0.0;
+  const unsigned long long sgn = V < 0 ? 0x8000000000000000ull : 0ull;
+  const unsigned long long a = (unsigned long long)(V < 0 ? -V : V);
+  const int lz = __clzll(a);
+  const unsigned long long mant = (a << (lz - 11)) & 0x000FFFFFFFFFFFFFull;
+  const long long E = (long long)(63 - lz) + 1023 + e;
+  if (E <= 0) return 0.0;
+  return __longlong_as_double((long long)(sgn | ((unsigned long long)E << 52) | mant));
+}
+
+__global__ void __launch_bounds__(kBlkThreads, 1) k_tblock_dg(const DgPassArgs a) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* sm = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+  uint64_t* hoff = reinterpret_cast<uint64_t*>(sm + kDgSmemHoff);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + kDgSmemBar);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + kDgSmemBar + 16);
+  int* ok_slot = reinterpret_cast<int*>(sm + kDgSmemBar + 20);
+  const uint32_t bar_b = smem_u32(&bars[0]), bar_mma = smem_u32(&bars[1]);
+  const int tid = threadIdx.x, warp = tid >> 5;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(kDgTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 32) {
+    mbar_init(bar_b, 1);
+    mbar_init(bar_mma, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  for (int h = tid; h < 128; h += kBlkThreads) {
+    uint64_t off = 0;
+    for (int j = 0; j < 7; ++j)
+      if ((h >> j) & 1) off |= 1ull << a.q[5 + j];
+    hoff[h] = off;
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t colh = (uint32_t)(warp >> 2);
+  const uint32_t tlane = tmem + ((32u * (warp & 3)) << 16) + (uint32_t)kColsPerWarp * colh;
+  const int e_scale = *a.scale_exp;
+  const int sh = 48 - e_scale;  // x / scale * 2^48 = x * 2^sh
+
+  // kind::f16: D FP32, A and B BF16, both K-major, N = 64, M = 128
+  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+  const uint32_t sA = smem_u32(sm), sB = smem_u32(sm + kDgSmemB);
+
+  uint32_t ph_b = 0, ph_mma = 0;
+  bool b_in_flight = false;
+  int mma_lost_phase = -1;
+  bool failed = false;
+  bool range_ok = true;
+
+  auto tile_base = [&](uint64_t tile) {
+    uint64_t ob = tile;
+    for (int j = 0; j < kBlockTileQubits; ++j) ob = insert_zero_bit(ob, a.q[j]);
+    return ob;
+  };
+
+  uint64_t tile = blockIdx.x;
+  if (tid == 0 && tile < a.ntiles) {
+    const Blk5& b0 = a.blocks[0];
+    load_image_bytes(sB, a.images + (size_t)(b0.img + variant_of(b0, tile_base(tile))) * kDigitImageBytes, bar_b,
+                     kDigitImageBytes);
+    b_in_flight = true;
+  }
+  const uint4 load_dest = my_dests(a.offsets, a.blocks[0].load_offs);
+
+  for (; tile < a.ntiles && !failed; tile += gridDim.x) {
+    const uint64_t obase = tile_base(tile);
+    // load: 8 amplitudes per thread, each as 6 digit pairs (re, im) into the planes
+#pragma unroll
+    for (int it = 0; it < kLoadIters; ++it) {
+      const uint32_t i0 = (uint32_t)(it * kBlkThreads + tid) * 2u;
+      const double2* src = a.s + (obase | (i0 & 31u) | hoff[i0 >> 5]);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const double2 v = __ldcs(src + h);
+        float dr[kDigits], di[kDigits];
+        range_ok &= digits_of(v.x, sh, dr);
+        range_ok &= digits_of(v.y, sh, di);
+        const uint32_t off = dest_at(load_dest, 2 * it + h) << 2;
+#pragma unroll
+        for (int p = 0; p < kDigits; ++p)
+          *reinterpret_cast<uint32_t*>(sm + (uint32_t)p * kDgPlane + off) = pack_bf16(dr[p], di[p]);
+      }
+    }
+    fence_proxy_async();
+    __syncthreads();
+
+    for (int bi = 0; bi < a.nblocks; ++bi) {
+      const bool more = bi + 1 < a.nblocks;
+      const uint4 dest = my_dests(a.offsets, a.blocks[bi].offs);
+      if (tid == 0) {
+        int ok = mbar_wait(bar_b, ph_b, a.spin_limit) ? 1 : 0;
+        if (ok) {
+          b_in_flight = false;
+          tc_fence_after();
+#pragma unroll
+          for (int s = 0; s < kDgLevels; ++s) {
+            uint32_t acc = 0;
+            const int ilo = s > kDigits - 1 ? s - (kDigits - 1) : 0;
+            const int ihi = s < kDigits - 1 ? s : kDigits - 1;
+            for (int i = ilo; i <= ihi; ++i) {
+              const int j = s - i;
+#pragma unroll
+              for (int ks = 0; ks < 4; ++ks) {
+                const uint64_t ad = sdesc(sA + (uint32_t)i * kDgPlane + (uint32_t)ks * 32u);
+                const uint64_t bd = sdesc(sB + (uint32_t)j * 8192u + (uint32_t)ks * 32u);
+                mma_bf16(tmem + 64u * (uint32_t)s, ad, bd, idesc, acc);
+                acc = 1;
+              }
+            }
+          }
+          mma_commit(bar_mma);
+          ok = mbar_wait(bar_mma, ph_mma, a.spin_limit) ? 1 : 0;
+          if (!ok) mma_lost_phase = (int)ph_mma;
+        }
+        if (!ok) atomicExch(a.flag, 1);
+        *ok_slot = ok;
+        if (ok) {
+          const Blk5* nb = nullptr;
+          uint64_t nbase = obase;
+          if (more) {
+            nb = &a.blocks[bi + 1];
+          } else if (tile + gridDim.x < a.ntiles) {
+            nb = &a.blocks[0];
+            nbase = tile_base(tile + gridDim.x);
+          }
+          if (nb) {
+            load_image_bytes(sB, a.images + (size_t)(nb->img + variant_of(*nb, nbase)) * kDigitImageBytes, bar_b,
+                             kDigitImageBytes);
+            b_in_flight = true;
+          }
+        }
+      }
+      ph_b ^= 1u;
+      ph_mma ^= 1u;
+      __syncthreads();
+      if (!*ok_slot) {
+        failed = true;
+        break;
+      }
+      tc_fence_after();
+      // Level s holds digit position s + 1 of the result.  From the lowest
+      // level up: t = sum + carry, digit = t - 256 round(t / 256), carry the
+      // rest; positions 6 and 7 only round; position 0 is the last carry.
+      float carry[kColsPerWarp];
+      long long V[kColsPerWarp];
+#pragma unroll
+      for (int v = 0; v < kColsPerWarp; ++v) {
+        carry[v] = 0.f;
+        V[v] = 0;
+      }
+#pragma unroll
+      for (int s = kDgLevels - 1; s >= 0; --s) {
+        float d[kColsPerWarp];
+        tmem_ld16(tlane + 64u * (uint32_t)s, d);
+        const int pos = s + 1;
+#pragma unroll
+        for (int v = 0; v < kColsPerWarp; ++v) {
+          const float t = __fadd_rn(d[v], carry[v]);
+          const float q = rint_small(__fmul_rn(t, 0.00390625f));
+          d[v] = fmaf(q, -256.0f, t);
+          carry[v] = q;
+        }
+        if (pos <= kDigits - 1) {
+          if (more) {
+#pragma unroll
+            for (int c = 0; c < kCplxPerThread; ++c)
+              *reinterpret_cast<uint32_t*>(sm + (uint32_t)pos * kDgPlane + (dest_at(dest, c) << 2)) =
+                  pack_bf16(d[2 * c], d[2 * c + 1]);
+          } else {
+#pragma unroll
+            for (int v = 0; v < kColsPerWarp; ++v) V[v] += (long long)int_of_small(d[v]) << (8 * (kDigits - 1 - pos));
+          }
+        }
+      }
+      // position 0: the remaining carry
+      if (more) {
+#pragma unroll
+        for (int c = 0; c < kCplxPerThread; ++c)
+          *reinterpret_cast<uint32_t*>(sm + (dest_at(dest, c) << 2)) = pack_bf16(carry[2 * c], carry[2 * c + 1]);
+        fence_proxy_async();
+      } else {
+        double2* stage = reinterpret_cast<double2*>(sm);
+#pragma unroll
+        for (int c = 0; c < kCplxPerThread; ++c) {
+          const long long vr = V[2 * c] + ((long long)int_of_small(carry[2 * c]) << (8 * (kDigits - 1)));
+          const long long vi = V[2 * c + 1] + ((long long)int_of_small(carry[2 * c + 1]) << (8 * (kDigits - 1)));
+          stage[dest_at(dest, c)] = make_double2(double_of(vr, e_scale - 48), double_of(vi, e_scale - 48));
+        }
+      }
+      tc_fence_before();
+      __syncthreads();
+    }
+    if (failed) break;
+    const double2* stage = reinterpret_cast<const double2*>(sm);
+#pragma unroll
+    for (int it = 0; it < kLoadIters; ++it) {
+      const uint32_t i0 = (uint32_t)(it * kBlkThreads + tid) * 2u;
+      double2* dst = a.s + (obase | (i0 & 31u) | hoff[i0 >> 5]);
+      const uint32_t sl = block_stage_slot(i0);
+      __stcs(dst, stage[sl]);
+      __stcs(dst + 1, stage[sl + 1]);
+    }
+    __syncthreads();
+  }
+  if (!range_ok) atomicExch(a.flag, 2);
+
+  if (tid == 0) {
+    if (b_in_flight && !mbar_wait(bar_b, ph_b, a.spin_limit)) atomicExch(a.flag, 1);
+    if (mma_lost_phase >= 0 && !mbar_wait(bar_mma, (uint32_t)mma_lost_phase, a.spin_limit)) atomicExch(a.flag, 1);
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kDgTmemCols) : "memory");
+}
+
+// scale exponent e (scale = 2^e >= 2 * norm) from norm-squared partials
+__global__ void k_digit_scale(const double* __restrict__ partial, int blocks, int* __restrict__ out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double hi = 0, lo = 0;
+  for (int b = 0; b < blocks; ++b) {
+    hi += partial[2 * b];
+    lo += partial[2 * b + 1];
+  }
+  const double nrm = sqrt(hi + lo) * (1.0 + 1e-6);
+  int e = 1;
+  if (nrm > 0) {
+    int k = 0;
+    frexp(nrm, &k);  // nrm < 2^k
+    e = k + 1;
+  }
+  *out = e;
+}
+
+void launch_digit_scale(State& st, int* d_exp) {
+  const unsigned blocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((st.N + 255) / 256, (uint64_t)st.num_sms * 8));
+  ensure_partials(st, blocks);
+  launch_norm2_partials(st, blocks);
+  k_digit_scale<<<1, 32, 0, st.stream>>>(st.d_partial, (int)blocks, d_exp);
+  BF_CUDA(cudaGetLastError());
+  st.launches++;
+}
+
+void launch_block_pass_digits(State& st, const Blk5* d_blocks, int nblocks, const unsigned char* d_images,
+                              const uint16_t* d_offsets, const TilePass& p, const int* d_exp) {
+  if (st.dtype != BF_C128) fail(BF_EINVAL, "internal: digit blocks need a complex128 state");
+  if (p.K != kBlockTileQubits || st.n < kBlockTileQubits) fail(BF_EINVAL, "internal: block pass needs a 12-qubit tile");
+  if (nblocks < 1) fail(BF_EINVAL, "internal: empty block pass");
+  if (((uintptr_t)d_images & 15u) != 0 || ((uintptr_t)d_offsets & 15u) != 0)
+    fail(BF_EINVAL, "internal: block images and tables must be 16-byte aligned");
+  DgPassArgs a;
+  std::memset(&a, 0, sizeof a);
+  for (int j = 0; j < kBlockTileQubits; ++j) {
+    a.q[j] = p.q[j];
+    if (j < 5 && p.q[j] != j) fail(BF_EINVAL, "internal: block tile must hold qubits 0..4");
+  }
+  a.s = static_cast<double2*>(st.amp);
+  a.blocks = d_blocks;
+  a.images = d_images;
+  a.offsets = d_offsets;
+  a.nblocks = nblocks;
+  a.ntiles = st.N >> kBlockTileQubits;
+  a.scale_exp = d_exp;
+  a.flag = state_flag(st);
+  a.spin_limit = 1u << 24;
+  static bool configured = false;
+  if (!configured) {
+    BF_CUDA(cudaFuncSetAttribute(k_tblock_dg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDgSmemAlloc));
+    BF_CUDA(cudaFuncSetAttribute(k_tblock_dg, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    configured = true;
+  }
+  uint64_t grid = std::min<uint64_t>(a.ntiles, (uint64_t)st.num_sms);
+  k_tblock_dg<<<(unsigned)grid, kBlkThreads, kDgSmemAlloc, st.stream>>>(a);
+  BF_CUDA(cudaGetLastError());
+  st.launches++;
+}
+
 void launch_block_pass(State& st, const Blk5* d_blocks, int nblocks, const unsigned char* d_images,
                        const uint16_t* d_offsets, const TilePass& p) {
   if (st.dtype != BF_C64) fail(BF_EINVAL, "internal: tensor-core blocks need a complex64 state");

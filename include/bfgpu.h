@@ -160,10 +160,12 @@ typedef struct bf_exec_opts {
                                 norm it had before the circuit (double-float
                                 norms, FP64 factor); -1: never.  complex128
                                 states are never rescaled.                    */
-  int32_t tensor_blocks;     /* non-zero: complex64 tile passes group their
-                                gates into 5-qubit blocks applied as 3xTF32
-                                tensor-core GEMMs (states of >= 12 qubits;
-                                ignored for complex128)                       */
+  int32_t tensor_blocks;     /* non-zero: tile passes group their gates into
+                                5-qubit blocks applied as tensor-core GEMMs
+                                (states of >= 12 qubits): 3xTF32 for
+                                complex64; for complex128 exact products of
+                                6 base-256 digits in bf16 (circuits of
+                                norm-preserving ops only)                     */
   int32_t reserved;
 } bf_exec_opts;
 
