@@ -661,6 +661,7 @@ void execute_ops(State& st, const bf_op* ops, int64_t nops, bf_exec_opts o) {
     fail(BF_EINVAL, "tile_qubits must be in [0, %d]", kMaxTileQubits);
   if (o.tile_qubits == 0) o.tile_qubits = env_int("BFGPU_TILE_QUBITS", default_tile_qubits(st));
   if (o.validate) validate_ops(st.n, ops, nops);
+  if (!o.tensor_blocks && env_int("BFGPU_TENSOR_BLOCKS", 0) && !st.shared_gpu) o.tensor_blocks = 1;
   std::vector<Step> steps;
   Program prog;
   build_steps(st.n, ops, nops, o, steps, prog, !st.shared_gpu, o.tensor_blocks != 0,

@@ -89,8 +89,10 @@ struct TilePass {
 // consecutively, variant v for outside bits (bit k of v = qubit outpos[k]).
 constexpr int kBlockTileQubits = 12;
 constexpr uint32_t kBlockImageBytes = 32768;  // one matrix: TF32 hi and lo parts, swizzled
-constexpr int kBlockThreads = 512;            // threads of the block kernel
-constexpr int kBlockThreadElems = 8;          // amplitudes each thread moves per block
+constexpr int kBlockThreads = 512;            // threads of the 3xTF32 block kernel
+constexpr int kBlockThreadElems = 8;          // amplitudes each of its threads moves per block
+constexpr int kDigitThreads = 1024;           // threads of the digit block kernel (4 amplitudes each)
+constexpr int kBlockTableEntries = 4096;      // one destination table: threads x amplitudes
 constexpr int kMaxPassBlocks = 32;
 
 struct Blk5 {
@@ -98,7 +100,7 @@ struct Blk5 {
   int32_t nout;
   int32_t outpos[3];
   uint32_t img;       // image index of variant 0
-  uint32_t offs;      // index (units of kBlockThreads * kBlockThreadElems) of the
+  uint32_t offs;      // index (units of kBlockTableEntries) of the
                       // shared-memory destinations of this block's results
   uint32_t load_offs; // first block of a pass: destinations of the loaded tile
 };

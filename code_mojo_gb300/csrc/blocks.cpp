@@ -276,32 +276,34 @@ bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsi
     blocks.push_back(d);
   }
 
-  // destination tables, kBlockThreads x kBlockThreadElems u16 each
-  const size_t table = (size_t)kBlockThreads * kBlockThreadElems;
+  // destination tables: u16 per (thread, amplitude) of the format's kernel
+  const int T = format == BLOCK_DIGITS ? kDigitThreads : kBlockThreads;
+  const int E = kBlockTableEntries / T;
+  const size_t table = (size_t)kBlockTableEntries;
   auto new_table = [&]() {
     size_t at = offsets.size();
     offsets.resize(at + table);
     return at;
   };
-  {  // load phase: thread t, element e = 2 * it + h holds tile element (it * threads + t) * 2 + h
+  {  // load phase: thread t, element e = 2 * it + h holds tile element (it * T + t) * 2 + h
     size_t at = new_table();
     blocks[first].load_offs = (uint32_t)(at / table);
-    for (int t = 0; t < kBlockThreads; ++t)
-      for (int e = 0; e < kBlockThreadElems; ++e) {
-        uint32_t i = (uint32_t)(((e >> 1) * kBlockThreads + t) * 2 + (e & 1)), g, j;
+    for (int t = 0; t < T; ++t)
+      for (int e = 0; e < E; ++e) {
+        uint32_t i = (uint32_t)(((e >> 1) * T + t) * 2 + (e & 1)), g, j;
         maps[0].ext(i, g, j);
-        offsets[at + (size_t)t * kBlockThreadElems + e] = dest(g, j);
+        offsets[at + (size_t)t * E + e] = dest(g, j);
       }
   }
   for (size_t k = 0; k < maps.size(); ++k) {
     // epilogue: thread t reads D row 32 (warp % 4) + lane, columns of
-    // complex elements 8 (warp / 4) + e
+    // complex elements E (warp / 4) + e
     size_t at = new_table();
     blocks[first + k].offs = (uint32_t)(at / table);
-    for (int t = 0; t < kBlockThreads; ++t)
-      for (int e = 0; e < kBlockThreadElems; ++e) {
+    for (int t = 0; t < T; ++t)
+      for (int e = 0; e < E; ++e) {
         const uint32_t w = (uint32_t)t >> 5, lane = (uint32_t)t & 31u;
-        const uint32_t g = 32u * (w & 3u) + lane, j = (uint32_t)kBlockThreadElems * (w >> 2) + (uint32_t)e;
+        const uint32_t g = 32u * (w & 3u) + lane, j = (uint32_t)E * (w >> 2) + (uint32_t)e;
         const uint32_t i = maps[k].dep_g(g) | maps[k].dep_j(j);
         uint16_t v;
         if (k + 1 < maps.size()) {
@@ -311,7 +313,7 @@ bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsi
         } else {
           v = (uint16_t)block_stage_slot(i);
         }
-        offsets[at + (size_t)t * kBlockThreadElems + e] = v;
+        offsets[at + (size_t)t * E + e] = v;
       }
   }
   return true;

@@ -164,7 +164,7 @@ __device__ __forceinline__ void put_split(unsigned char* sm, uint32_t off, float
 
 // this thread's 8 destinations in a table: operand byte offset / 8, or staging slot
 __device__ __forceinline__ uint4 my_dests(const uint16_t* offsets, uint32_t table) {
-  return __ldg(reinterpret_cast<const uint4*>(offsets + ((size_t)table * kBlkThreads + threadIdx.x) * 8));
+  return __ldg(reinterpret_cast<const uint4*>(offsets + (size_t)table * kBlockTableEntries + threadIdx.x * 8));
 }
 
 __device__ __forceinline__ uint32_t dest_at(const uint4& d, int e) {
@@ -363,12 +363,50 @@ __global__ void __launch_bounds__(kBlkThreads, 2) k_tblock(const BlkPassArgs a) 
 // sixth digit leave errors of about 2^-48 scale per block.
 constexpr uint32_t kDgPlane = 16384;                       // 128 rows x 64 bf16
 constexpr uint32_t kDgSmemB = kDigits * kDgPlane;          // 6 A planes, then B
-constexpr uint32_t kDgSmemHoff = kDgSmemB + kDigitImageBytes;
-constexpr uint32_t kDgSmemBar = kDgSmemHoff + 128 * 8;
-constexpr uint32_t kDgSmemUsed = kDgSmemBar + 32;
+constexpr uint32_t kDgSmemHoff = kDgSmemB + 2 * kDigitImageBytes;  // two image buffers
+constexpr uint32_t kDgSmemBar = kDgSmemHoff + 128 * 8;  // 2 image barriers, 7 level barriers, tmem slot
+constexpr uint32_t kDgSmemUsed = kDgSmemBar + 88;
 constexpr uint32_t kDgSmemAlloc = kDgSmemUsed + 1024;
 constexpr uint32_t kDgTmemCols = 512;                      // 7 levels x 64 columns
 constexpr int kDgLevels = 7;
+constexpr int kDgThreads = kDigitThreads;                  // 32 warps: 8 per 32-lane group of D
+constexpr int kDgCols = 64 / (kDgThreads / 128);           // FP32 columns of a level per warp
+constexpr int kDgCplx = kDgCols / 2;                       // complex results per thread per block
+constexpr int kDgLoadIters = 4096 / (2 * kDgThreads);      // amplitude pairs per thread per tile
+static_assert(kDgCols == 8 && kDgLoadIters * 2 == kBlockTableEntries / kDgThreads, "digit kernel thread layout");
+
+// The MMA groups of one block: A plane i against B planes j0 .. j0+nj-1
+// (i + j <= 6: the 26 digit pairs kept), in issue order.
+struct DgGroup {
+  int i, j0, nj, init;
+};
+#define BF_DG_GROUPS                                                                                  \
+  {                                                                                                   \
+    {0, 0, 4, 1}, {0, 4, 2, 1}, /* levels 0..5 first written */                                       \
+        {1, 5, 1, 1},           /* level 6 first written */                                           \
+        {1, 0, 4, 0}, {1, 4, 1, 0}, {2, 0, 4, 0}, {2, 4, 1, 0}, {3, 0, 4, 0}, {4, 0, 3, 0}, {5, 0, 2, 0} \
+  }
+constexpr int kDgGroups = 10;
+
+// 8 columns of the thread's TMEM lane
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// this thread's 4 destinations in a table
+__device__ __forceinline__ uint2 my_dests4(const uint16_t* offsets, uint32_t table) {
+  return __ldg(reinterpret_cast<const uint2*>(offsets + (size_t)table * kBlockTableEntries + threadIdx.x * 4));
+}
+__device__ __forceinline__ uint32_t dest_at4(const uint2& d, int e) {
+  const uint32_t w = e < 2 ? d.x : d.y;
+  return (e & 1) ? (w >> 16) : (w & 0xFFFFu);
+}
 
 struct DgPassArgs {
   double2* s;
@@ -453,14 +491,15 @@ __device__ __forceinline__ double double_of(long long V, int e) {
   return __longlong_as_double((long long)(sgn | ((unsigned long long)E << 52) | mant));
 }
 
-__global__ void __launch_bounds__(kBlkThreads, 1) k_tblock_dg(const DgPassArgs a) {
+__global__ void __launch_bounds__(kDgThreads, 1) k_tblock_dg(const DgPassArgs a) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* sm = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
   uint64_t* hoff = reinterpret_cast<uint64_t*>(sm + kDgSmemHoff);
   uint64_t* bars = reinterpret_cast<uint64_t*>(sm + kDgSmemBar);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + kDgSmemBar + 16);
-  int* ok_slot = reinterpret_cast<int*>(sm + kDgSmemBar + 20);
-  const uint32_t bar_b = smem_u32(&bars[0]), bar_mma = smem_u32(&bars[1]);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + kDgSmemBar + 72);
+  // bar_b + 8 k: image buffer k; bar_lvl + 8 s: the MMAs of level s (issued
+  // from level 6 down, so a level's completion implies every higher level's)
+  const uint32_t bar_b = smem_u32(&bars[0]), bar_lvl = smem_u32(&bars[2]);
   const int tid = threadIdx.x, warp = tid >> 5;
 
   if (warp == 0) {
@@ -471,10 +510,11 @@ __global__ void __launch_bounds__(kBlkThreads, 1) k_tblock_dg(const DgPassArgs a
   }
   if (tid == 32) {
     mbar_init(bar_b, 1);
-    mbar_init(bar_mma, 1);
+    mbar_init(bar_b + 8u, 1);
+    for (int l = 0; l < kDgLevels; ++l) mbar_init(bar_lvl + 8u * (uint32_t)l, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  for (int h = tid; h < 128; h += kBlkThreads) {
+  for (int h = tid; h < 128; h += kDgThreads) {
     uint64_t off = 0;
     for (int j = 0; j < 7; ++j)
       if ((h >> j) & 1) off |= 1ull << a.q[5 + j];
@@ -484,18 +524,20 @@ __global__ void __launch_bounds__(kBlkThreads, 1) k_tblock_dg(const DgPassArgs a
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const uint32_t colh = (uint32_t)(warp >> 2);
-  const uint32_t tlane = tmem + ((32u * (warp & 3)) << 16) + (uint32_t)kColsPerWarp * colh;
+  const uint32_t colh = (uint32_t)(warp >> 2);  // 8 column groups of 8
+  const uint32_t tlane = tmem + ((32u * (warp & 3)) << 16) + (uint32_t)kDgCols * colh;
   const int e_scale = *a.scale_exp;
   const int sh = 48 - e_scale;  // x / scale * 2^48 = x * 2^sh
 
-  // kind::f16: D FP32, A and B BF16, both K-major, N = 64, M = 128
-  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+  // kind::f16: D FP32, A and B BF16, both K-major, M = 128 (N set per MMA)
+  const uint32_t idesc_base = (1u << 4) | (1u << 7) | (1u << 10) | ((128u >> 4) << 24);
   const uint32_t sA = smem_u32(sm), sB = smem_u32(sm + kDgSmemB);
 
-  uint32_t ph_b = 0, ph_mma = 0;
-  bool b_in_flight = false;
-  int mma_lost_phase = -1;
+  uint32_t ph_b0 = 0, ph_b1 = 0, ph_mma = 0;
+  uint32_t kimg = 0;          // blocks this CTA has run: image buffer kimg & 1
+  int b_in_flight = 0;        // thread 0: image loads not yet waited for (by buffer bit)
+  bool issued = false;        // thread 0: MMAs issued for the current block
+  int mma_lost_phase = -1;    // thread 0: level-0 phase whose wait expired
   bool failed = false;
   bool range_ok = true;
 
@@ -510,16 +552,16 @@ __global__ void __launch_bounds__(kBlkThreads, 1) k_tblock_dg(const DgPassArgs a
     const Blk5& b0 = a.blocks[0];
     load_image_bytes(sB, a.images + (size_t)(b0.img + variant_of(b0, tile_base(tile))) * kDigitImageBytes, bar_b,
                      kDigitImageBytes);
-    b_in_flight = true;
+    b_in_flight |= 1;
   }
-  const uint4 load_dest = my_dests(a.offsets, a.blocks[0].load_offs);
+  const uint2 load_dest = my_dests4(a.offsets, a.blocks[0].load_offs);
 
   for (; tile < a.ntiles && !failed; tile += gridDim.x) {
     const uint64_t obase = tile_base(tile);
     // load: 8 amplitudes per thread, each as 6 digit pairs (re, im) into the planes
 #pragma unroll
-    for (int it = 0; it < kLoadIters; ++it) {
-      const uint32_t i0 = (uint32_t)(it * kBlkThreads + tid) * 2u;
+    for (int it = 0; it < kDgLoadIters; ++it) {
+      const uint32_t i0 = (uint32_t)(it * kDgThreads + tid) * 2u;
       const double2* src = a.s + (obase | (i0 & 31u) | hoff[i0 >> 5]);
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
@@ -527,7 +569,7 @@ __global__ void __launch_bounds__(kBlkThreads, 1) k_tblock_dg(const DgPassArgs a
         float dr[kDigits], di[kDigits];
         range_ok &= digits_of(v.x, sh, dr);
         range_ok &= digits_of(v.y, sh, di);
-        const uint32_t off = dest_at(load_dest, 2 * it + h) << 2;
+        const uint32_t off = dest_at4(load_dest, 2 * it + h) << 2;
 #pragma unroll
         for (int p = 0; p < kDigits; ++p)
           *reinterpret_cast<uint32_t*>(sm + (uint32_t)p * kDgPlane + off) = pack_bf16(dr[p], di[p]);
@@ -538,35 +580,34 @@ __global__ void __launch_bounds__(kBlkThreads, 1) k_tblock_dg(const DgPassArgs a
 
     for (int bi = 0; bi < a.nblocks; ++bi) {
       const bool more = bi + 1 < a.nblocks;
-      const uint4 dest = my_dests(a.offsets, a.blocks[bi].offs);
+      const uint2 dest = my_dests4(a.offsets, a.blocks[bi].offs);
+      bool lost = false;
+      const uint32_t kb = kimg & 1u;
+      const uint32_t sBk = sB + kb * kDigitImageBytes;
       if (tid == 0) {
-        int ok = mbar_wait(bar_b, ph_b, a.spin_limit) ? 1 : 0;
-        if (ok) {
-          b_in_flight = false;
+        if (mbar_wait(bar_b + 8u * kb, kb ? ph_b1 : ph_b0, a.spin_limit)) {
+          b_in_flight &= ~(1 << kb);
           tc_fence_after();
+          issued = true;
+          // A plane i against nj stacked B planes j0.. (N = 64 nj) writes
+          // levels i + j0 .. i + j0 + nj - 1, which are consecutive 64-column
+          // ranges of tensor memory; the first group to reach a level
+          // initialises it (at K step 0), the others accumulate.
+          constexpr DgGroup groups[kDgGroups] = BF_DG_GROUPS;
 #pragma unroll
-          for (int s = 0; s < kDgLevels; ++s) {
-            uint32_t acc = 0;
-            const int ilo = s > kDigits - 1 ? s - (kDigits - 1) : 0;
-            const int ihi = s < kDigits - 1 ? s : kDigits - 1;
-            for (int i = ilo; i <= ihi; ++i) {
-              const int j = s - i;
+          for (int gi = 0; gi < kDgGroups; ++gi) {
+            const DgGroup gr = groups[gi];
+            const uint32_t idn = idesc_base | ((uint32_t)(8 * gr.nj) << 17);
 #pragma unroll
-              for (int ks = 0; ks < 4; ++ks) {
-                const uint64_t ad = sdesc(sA + (uint32_t)i * kDgPlane + (uint32_t)ks * 32u);
-                const uint64_t bd = sdesc(sB + (uint32_t)j * 8192u + (uint32_t)ks * 32u);
-                mma_bf16(tmem + 64u * (uint32_t)s, ad, bd, idesc, acc);
-                acc = 1;
-              }
+            for (int ks = 0; ks < 4; ++ks) {
+              const uint64_t ad = sdesc(sA + (uint32_t)gr.i * kDgPlane + (uint32_t)ks * 32u);
+              const uint64_t bd = sdesc(sBk + (uint32_t)gr.j0 * 8192u + (uint32_t)ks * 32u);
+              mma_bf16(tmem + 64u * (uint32_t)(gr.i + gr.j0), ad, bd, idn, (gr.init && ks == 0) ? 0u : 1u);
             }
           }
-          mma_commit(bar_mma);
-          ok = mbar_wait(bar_mma, ph_mma, a.spin_limit) ? 1 : 0;
-          if (!ok) mma_lost_phase = (int)ph_mma;
-        }
-        if (!ok) atomicExch(a.flag, 1);
-        *ok_slot = ok;
-        if (ok) {
+          mma_commit(bar_lvl);
+          // the next block's image into the other buffer, whose last reader
+          // (the previous block's MMAs) has completed
           const Blk5* nb = nullptr;
           uint64_t nbase = obase;
           if (more) {
@@ -576,37 +617,36 @@ __global__ void __launch_bounds__(kBlkThreads, 1) k_tblock_dg(const DgPassArgs a
             nbase = tile_base(tile + gridDim.x);
           }
           if (nb) {
-            load_image_bytes(sB, a.images + (size_t)(nb->img + variant_of(*nb, nbase)) * kDigitImageBytes, bar_b,
-                             kDigitImageBytes);
-            b_in_flight = true;
+            load_image_bytes(sB + (kb ^ 1u) * kDigitImageBytes,
+                             a.images + (size_t)(nb->img + variant_of(*nb, nbase)) * kDigitImageBytes,
+                             bar_b + 8u * (kb ^ 1u), kDigitImageBytes);
+            b_in_flight |= 1 << (kb ^ 1u);
           }
+        } else {
+          lost = true;  // the image never arrived: no MMAs; every level wait below expires
         }
       }
-      ph_b ^= 1u;
-      ph_mma ^= 1u;
-      __syncthreads();
-      if (!*ok_slot) {
-        failed = true;
-        break;
-      }
-      tc_fence_after();
+      if (kb) ph_b1 ^= 1u; else ph_b0 ^= 1u;
+      ++kimg;
       // Level s holds digit position s + 1 of the result.  From the lowest
       // level up: t = sum + carry, digit = t - 256 round(t / 256), carry the
       // rest; positions 6 and 7 only round; position 0 is the last carry.
-      float carry[kColsPerWarp];
-      long long V[kColsPerWarp];
+      float carry[kDgCols];
+      long long V[kDgCols];
 #pragma unroll
-      for (int v = 0; v < kColsPerWarp; ++v) {
+      for (int v = 0; v < kDgCols; ++v) {
         carry[v] = 0.f;
         V[v] = 0;
       }
+      if (!mbar_wait(bar_lvl, ph_mma, a.spin_limit)) lost = true;
+      tc_fence_after();
 #pragma unroll
       for (int s = kDgLevels - 1; s >= 0; --s) {
-        float d[kColsPerWarp];
-        tmem_ld16(tlane + 64u * (uint32_t)s, d);
+        float d[kDgCols];
+        tmem_ld8(tlane + 64u * (uint32_t)s, d);
         const int pos = s + 1;
 #pragma unroll
-        for (int v = 0; v < kColsPerWarp; ++v) {
+        for (int v = 0; v < kDgCols; ++v) {
           const float t = __fadd_rn(d[v], carry[v]);
           const float q = rint_small(__fmul_rn(t, 0.00390625f));
           d[v] = fmaf(q, -256.0f, t);
@@ -615,38 +655,44 @@ __global__ void __launch_bounds__(kBlkThreads, 1) k_tblock_dg(const DgPassArgs a
         if (pos <= kDigits - 1) {
           if (more) {
 #pragma unroll
-            for (int c = 0; c < kCplxPerThread; ++c)
-              *reinterpret_cast<uint32_t*>(sm + (uint32_t)pos * kDgPlane + (dest_at(dest, c) << 2)) =
+            for (int c = 0; c < kDgCplx; ++c)
+              *reinterpret_cast<uint32_t*>(sm + (uint32_t)pos * kDgPlane + (dest_at4(dest, c) << 2)) =
                   pack_bf16(d[2 * c], d[2 * c + 1]);
           } else {
 #pragma unroll
-            for (int v = 0; v < kColsPerWarp; ++v) V[v] += (long long)int_of_small(d[v]) << (8 * (kDigits - 1 - pos));
+            for (int v = 0; v < kDgCols; ++v) V[v] += (long long)int_of_small(d[v]) << (8 * (kDigits - 1 - pos));
           }
         }
       }
       // position 0: the remaining carry
       if (more) {
 #pragma unroll
-        for (int c = 0; c < kCplxPerThread; ++c)
-          *reinterpret_cast<uint32_t*>(sm + (dest_at(dest, c) << 2)) = pack_bf16(carry[2 * c], carry[2 * c + 1]);
+        for (int c = 0; c < kDgCplx; ++c)
+          *reinterpret_cast<uint32_t*>(sm + (dest_at4(dest, c) << 2)) = pack_bf16(carry[2 * c], carry[2 * c + 1]);
         fence_proxy_async();
       } else {
         double2* stage = reinterpret_cast<double2*>(sm);
 #pragma unroll
-        for (int c = 0; c < kCplxPerThread; ++c) {
+        for (int c = 0; c < kDgCplx; ++c) {
           const long long vr = V[2 * c] + ((long long)int_of_small(carry[2 * c]) << (8 * (kDigits - 1)));
           const long long vi = V[2 * c + 1] + ((long long)int_of_small(carry[2 * c + 1]) << (8 * (kDigits - 1)));
-          stage[dest_at(dest, c)] = make_double2(double_of(vr, e_scale - 48), double_of(vi, e_scale - 48));
+          stage[dest_at4(dest, c)] = make_double2(double_of(vr, e_scale - 48), double_of(vi, e_scale - 48));
         }
       }
+      if (tid == 0 && lost && issued) mma_lost_phase = (int)ph_mma;
+      ph_mma ^= 1u;
       tc_fence_before();
-      __syncthreads();
+      if (__syncthreads_or(lost ? 1 : 0)) {
+        if (tid == 0) atomicExch(a.flag, 1);
+        failed = true;
+        break;
+      }
     }
     if (failed) break;
     const double2* stage = reinterpret_cast<const double2*>(sm);
 #pragma unroll
-    for (int it = 0; it < kLoadIters; ++it) {
-      const uint32_t i0 = (uint32_t)(it * kBlkThreads + tid) * 2u;
+    for (int it = 0; it < kDgLoadIters; ++it) {
+      const uint32_t i0 = (uint32_t)(it * kDgThreads + tid) * 2u;
       double2* dst = a.s + (obase | (i0 & 31u) | hoff[i0 >> 5]);
       const uint32_t sl = block_stage_slot(i0);
       __stcs(dst, stage[sl]);
@@ -657,8 +703,9 @@ __global__ void __launch_bounds__(kBlkThreads, 1) k_tblock_dg(const DgPassArgs a
   if (!range_ok) atomicExch(a.flag, 2);
 
   if (tid == 0) {
-    if (b_in_flight && !mbar_wait(bar_b, ph_b, a.spin_limit)) atomicExch(a.flag, 1);
-    if (mma_lost_phase >= 0 && !mbar_wait(bar_mma, (uint32_t)mma_lost_phase, a.spin_limit)) atomicExch(a.flag, 1);
+    if ((b_in_flight & 1) && !mbar_wait(bar_b, ph_b0, a.spin_limit)) atomicExch(a.flag, 1);
+    if ((b_in_flight & 2) && !mbar_wait(bar_b + 8u, ph_b1, a.spin_limit)) atomicExch(a.flag, 1);
+    if (mma_lost_phase >= 0 && !mbar_wait(bar_lvl, (uint32_t)mma_lost_phase, a.spin_limit)) atomicExch(a.flag, 1);
   }
   tc_fence_before();
   __syncthreads();
@@ -723,7 +770,7 @@ void launch_block_pass_digits(State& st, const Blk5* d_blocks, int nblocks, cons
     configured = true;
   }
   uint64_t grid = std::min<uint64_t>(a.ntiles, (uint64_t)st.num_sms);
-  k_tblock_dg<<<(unsigned)grid, kBlkThreads, kDgSmemAlloc, st.stream>>>(a);
+  k_tblock_dg<<<(unsigned)grid, kDgThreads, kDgSmemAlloc, st.stream>>>(a);
   BF_CUDA(cudaGetLastError());
   st.launches++;
 }
