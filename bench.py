@@ -9,8 +9,11 @@ A step applies the whole circuit once to a state resident in HBM (16 GiB,
 larger than L2, so no flush is needed between steps).  `value` is effective
 HBM GB/s under the per-gate byte accounting (each dense 1-qubit gate reads and
 writes the state once, 2S; each CX touches half of it, S): 3000 S per
-circuit.  `roofline` is the tile kernel's own traffic (2S per tile pass)
-over its average launch time.  `e2e` repeats the step through host SoA
+circuit.  `roofline` is the pass class with the largest share of the step,
+timed with CUDA events around every pass on the state's stream: by default
+the complex128 digit block pass (tensor-bound: its bf16 digit products over
+the measured bf16 peak, with its 2S of HBM traffic beside it), or the
+double-float tile pass (2S per launch) with --no-tensor-blocks.  `e2e` repeats the step through host SoA
 buffers (pinned), the upload and the download inside the timed region.
 `cpu_baseline` times the restated SIMD_PARALLEL strategy on this host's
 cores on a bounded sample of the same circuit.
@@ -34,10 +37,15 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "30q HBM GB/s vs peak; served circuits/s, p50/p99 ms at fidelity≥1-1e-6"
-# DRAM bytes (read + write) of one double-float tile launch per amplitude,
-# from an ncu capture of the same kernel at 26 qubits (2.153 GB / 2^26);
-# traffic grows in proportion to the amplitudes a launch processes.
+# DRAM bytes (read + write) per amplitude of one launch, from ncu captures of
+# the same kernels at 26 qubits; traffic grows in proportion to the amplitudes
+# a launch processes.  Double-float tile pass: 2.153 GB / 2^26.
 TILE_TRAFFIC_BYTES_PER_AMP = 32.08
+# complex128 digit block pass (k_tblock_dg), per launch
+DIGIT_TRAFFIC_BYTES_PER_AMP = None
+# Tensor work of one complex128 digit block on one 128-row tile (4096
+# amplitudes): 26 digit-pair products of 128 x 64 x 64, 2 flops each.
+DIGIT_FLOPS_PER_AMP_BLOCK = 26 * 2 * 128 * 64 * 64 / 4096
 N_QUBITS = 30
 LAYERS = 40
 SEED = 0
@@ -49,6 +57,47 @@ def per_gate_bytes_in_S(qc) -> float:
     ctx = bfy.ExecContext()
     ctx.execution_strategy = bfy.ExecutionStrategy.GPU
     return bfy.plan_stats(qc, ctx)["bytes_in_S"]
+
+
+def measured_tensor_peak(sustained: bool) -> tuple[float, str]:
+    """Dense bf16 TFLOP/s of this machine's GPUs (cuBLAS), burst or sustained."""
+    key = "bf16_tflops_sustained" if sustained else "bf16_tflops"
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())[key]), f"measured {key}"
+        except Exception:
+            pass
+    return (1700.0 if sustained else 1900.0), "fallback bf16"
+
+
+def roofline_of(times: dict, plan: dict, n: int, S: float) -> dict:
+    """Roofline of the pass class with the largest share of the timed region
+    (CUDA events around each pass on the state's stream)."""
+    cls, (count, total_ms) = max(times.items(), key=lambda kv: kv[1][1])
+    share = total_ms / sum(t for _, t in times.values())
+    avg_ms = total_ms / count
+    hbm_peak, hbm_src = measured_peaks()
+    hbm = 2 * S / (avg_ms * 1e-3) / 1e9
+    if cls == "block_digits":
+        # the plan's block count over the timed passes (each step runs the plan once)
+        blocks = plan["blocks"] * count / max(1, plan["block_passes"])
+        tflops = DIGIT_FLOPS_PER_AMP_BLOCK * (1 << n) * blocks / (total_ms * 1e-3) / 1e12
+        peak, src = measured_tensor_peak(sustained=True)
+        traffic = DIGIT_TRAFFIC_BYTES_PER_AMP * (1 << n) if DIGIT_TRAFFIC_BYTES_PER_AMP else None
+        return {"bound": "tensor", "achieved": tflops, "peak": peak, "unit": "TFLOP/s", "frac": tflops / peak,
+                "traffic": traffic, "kernel": "bf::k_tblock_dg", "avg_launch_ms": avg_ms,
+                "flops_per_launch": DIGIT_FLOPS_PER_AMP_BLOCK * (1 << n) * blocks / count,
+                "blocks_per_launch": blocks / count, "share_of_step": share, "launches": count,
+                "peak_source": f"{src} (bf16 tensor; digit products are bf16 x bf16 -> fp32)",
+                "hbm": {"achieved": hbm, "peak": hbm_peak, "unit": "GB/s", "frac": hbm / hbm_peak,
+                        "bytes_per_launch": 2 * S, "peak_source": f"{hbm_src} hbm_gbs"}}
+    kernel = {"tile": "bf::k_tile<bf::PolDF>", "gate": "bf::k_gate<bf::PolDF>",
+              "block_tf32": "bf::k_tblock"}.get(cls, cls)
+    traffic = TILE_TRAFFIC_BYTES_PER_AMP * (1 << n) if cls == "tile" else None
+    return {"bound": "hbm", "achieved": hbm, "peak": hbm_peak, "unit": "GB/s", "frac": hbm / hbm_peak,
+            "traffic": traffic, "kernel": kernel, "bytes_per_launch": 2 * S, "avg_launch_ms": avg_ms,
+            "share_of_step": share, "launches": count, "peak_source": f"{hbm_src} hbm_gbs"}
 
 
 def measured_peaks() -> tuple[float, str]:
@@ -371,11 +420,15 @@ def run_ours(args) -> None:
     st = bfy.QuantumState(n)
     stream = torch.cuda.ExternalStream(st.stream_ptr())
 
-    K, tune = autotune_width(st, qc, [int(k) for k in args.widths.split(",")])
     ctx = bfy.ExecContext()
     ctx.execution_strategy = bfy.ExecutionStrategy.GPU_FUSED
-    ctx.gpu_tile_qubits = K
+    ctx.gpu_tensor_blocks = not args.no_tensor_blocks
     ctx.gpu_sync = False
+    if bfy.plan_stats(qc, ctx)["block_passes"] > 0:
+        K, tune = 12, "not run: tensor-core block passes fix 12-qubit tiles"
+    else:
+        K, tune = autotune_width(st, qc, [int(k) for k in args.widths.split(",")])
+    ctx.gpu_tile_qubits = K
     plan = bfy.plan_stats(qc, ctx)
 
     st.set_basis(0)
@@ -384,6 +437,8 @@ def run_ours(args) -> None:
     st.sync()
     barrier(world)
     st.launch_count(reset=True)
+    st.pass_timing(True)
+    st.pass_times()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
         st.sync()
@@ -393,6 +448,8 @@ def run_ours(args) -> None:
         e1.record(stream)
         e1.synchronize()
     launches = st.launch_count()
+    pass_times = st.pass_times()
+    st.pass_timing(False)
     ms = e0.elapsed_time(e1)
     ms = barrier_max(ms, world)
     ms_step = ms / args.steps
@@ -459,26 +516,25 @@ def run_ours(args) -> None:
     if rank != 0:
         st.close()
         return
-    peak, peak_src = measured_peaks()
     value = pg_bytes * world / (ms_step * 1e-3) / 1e9
-    tile_launch_ms = ms_step / max(1, plan["tile_passes"] + plan["gate_kernels"])
-    achieved = 2 * S / (tile_launch_ms * 1e-3) / 1e9
+    digits = plan["block_passes"] > 0
+    arith = ("exact base-256 digit products on bf16 tensor cores (48-bit fixed point per block pass) and "
+             "double-float tile passes" if digits else "double-float arithmetic")
     line = {
         "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "df64", "data": "synthetic",
+        "vs_baseline": None, "dtype": "fixed48+df64" if digits else "df64", "data": "synthetic",
         "config": {"workload": f"random layered circuit, {n} qubits, {LAYERS} layers (U3 on every qubit + CX on a "
-                               f"random perfect matching), complex128 (FP64 storage, double-float arithmetic), "
-                               f"from |0>; fused tile passes, fusion width autotuned",
+                               f"random perfect matching), complex128 (FP64 storage; {arith}), from |0>",
                    "qubits": n, "layers": LAYERS, "seed": SEED, "state_bytes": int(S), "tile_qubits": K,
+                   "tensor_blocks": digits,
                    "l2": "state (16 GiB) larger than L2; no flush", "parallelism": f"replicas x{world}"},
         "gate_passes_per_s": len(qc.transformations) * world / (ms_step * 1e-3),
         "circuits_per_s": world / (ms_step * 1e-3),
         "per_gate_bytes_per_circuit": pg_bytes,
         "fused_plan": plan,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": TILE_TRAFFIC_BYTES_PER_AMP * (1 << n), "kernel": "bf::k_tile<bf::PolDF>",
-                     "bytes_per_launch": 2 * S, "avg_launch_ms": tile_launch_ms, "peak_source": f"{peak_src} hbm_gbs"},
+        "roofline": roofline_of(pass_times, plan, n, S),
+        "pass_times_ms": {k: {"passes": c, "ms": t} for k, (c, t) in pass_times.items()},
         "autotune": tune,
         "per_gate_path": per_gate,
         "gpu_launches": launches,
@@ -502,6 +558,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--widths", default="10,11,12,13")
+    ap.add_argument("--no-tensor-blocks", action="store_true",
+                    help="CUDA-core tile passes only (double-float complex128)")
     ap.add_argument("--per-gate-steps", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-gates", type=int, default=45)

@@ -56,7 +56,7 @@ class bf_exec_opts(C.Structure):
         ("sync", C.c_int32),
         ("renormalize", C.c_int32),
         ("tensor_blocks", C.c_int32),
-        ("reserved", C.c_int32),
+        ("plan_dtype", C.c_int32),
     ]
 
 
@@ -104,6 +104,8 @@ SIGNATURES = {
     "bf_state_stream": [C.c_void_p, C.POINTER(C.c_void_p)],
     "bf_execute": [C.c_void_p, C.POINTER(bf_op), C.c_int64, C.POINTER(bf_exec_opts)],
     "bf_state_launch_count": [C.c_void_p, C.POINTER(C.c_uint64), C.c_int32],
+    "bf_state_pass_timing": [C.c_void_p, C.c_int32],
+    "bf_state_pass_times": [C.c_void_p, C.c_void_p, C.c_void_p],
     "bf_norm2": [C.c_void_p, C.POINTER(C.c_double)],
     "bf_inner": [C.c_void_p, C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)],
     "bf_probabilities": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p],

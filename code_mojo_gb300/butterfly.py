@@ -64,7 +64,7 @@ class ExecContext:
         self.validate_circuit = True
         self.execution_strategy = ExecutionStrategy.GPU_FUSED
         self.gpu_tile_qubits = 0     # fusion width of a tile pass (0 = default)
-        self.gpu_tensor_blocks = False  # complex64: 5-qubit blocks as 3xTF32 tensor-core GEMMs
+        self.gpu_tensor_blocks = True   # 5-qubit blocks on the tensor cores where cheaper (3xTF32 / bf16 digits)
         self.gpu_renormalize = True  # complex64: restore the input norm after the circuit
         self.gpu_sync = True         # block until the device has finished
 
@@ -701,6 +701,22 @@ class QuantumState:
         F.check(F.lib().bf_state_launch_count(self.handle, C.byref(v), 1 if reset else 0))
         return v.value
 
+    PASS_CLASSES = ("gate", "tile", "block_tf32", "block_digits", "other")
+
+    def pass_timing(self, enable: bool) -> None:
+        """Bracket every pass of later executes with CUDA events on the
+        state's stream (read with pass_times)."""
+        F.check(F.lib().bf_state_pass_timing(self.handle, 1 if enable else 0))
+
+    def pass_times(self) -> dict:
+        """{class: (passes, summed device ms)} of the passes timed since the
+        last call; waits for the state's stream."""
+        n = len(self.PASS_CLASSES)
+        cnt = np.zeros(n, dtype=np.int64)
+        ms = np.zeros(n, dtype=np.float64)
+        F.check(F.lib().bf_state_pass_times(self.handle, cnt.ctypes.data, ms.ctypes.data))
+        return {k: (int(cnt[i]), float(ms[i])) for i, k in enumerate(self.PASS_CLASSES) if cnt[i]}
+
     def close(self) -> None:
         if getattr(self, "_h", None):
             F.lib().bf_state_destroy(self._h)
@@ -739,11 +755,13 @@ def execute(state: QuantumState, circuit: QuantumCircuit, ctx: Optional[ExecCont
     del keep
 
 
-def plan_stats(circuit: QuantumCircuit, ctx: Optional[ExecContext] = None) -> dict:
-    """Host-only plan of a circuit: launches and algorithmic bytes (units of S)."""
+def plan_stats(circuit: QuantumCircuit, ctx: Optional[ExecContext] = None, dtype: str = "c128") -> dict:
+    """Host-only plan of a circuit for a state of `dtype`: launches and
+    algorithmic bytes (units of S)."""
     ctx = ctx or ExecContext()
     arr, n, keep = circuit.to_ops()
     opts = exec_opts(ctx)
+    opts.plan_dtype = F.BF_C64 if dtype == "c64" else F.BF_C128
     t, g, x, bp, nb = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
     b = C.c_double()
     F.check(F.lib().bf_plan_stats(circuit.num_qubits, arr, n, C.byref(opts), C.byref(t), C.byref(g), C.byref(x),

@@ -331,8 +331,9 @@ static double cuda_core_units(const TilePass& tp) {
 }
 
 // complex128 digit blocks against the double-float tile kernel: one block
-// costs about this many double-float dense gates
-constexpr double kDigitBlockUnits = 2.5;
+// costs about this many double-float dense gates (measured on the 30-qubit
+// layered circuit: about 12 ms per block against 2.2 ms per dense gate)
+constexpr double kDigitBlockUnits = 5.0;
 
 // True when every op keeps the state's norm (unitary gates and unitaries to
 // 1e-12, permutations and the classical Grover and modexp passes; not
@@ -610,20 +611,42 @@ static void build_steps(int n, const bf_op* ops, int64_t nops, const bf_exec_opt
   flush();
 }
 
+static int pass_class_of(const Step& s) {
+  switch (s.kind) {
+    case Step::GATE: return BF_PASS_GATE;
+    case Step::TILE: return BF_PASS_TILE;
+    case Step::TBLOCK: return s.digits ? BF_PASS_BLOCK_DIGITS : BF_PASS_BLOCK_TF32;
+    default: return BF_PASS_OTHER;
+  }
+}
+
+// The next free event of the timing pool (created on first use).
+static cudaEvent_t pass_event(State& st, size_t k) {
+  while (st.pass_events.size() <= k) {
+    cudaEvent_t e;
+    BF_CUDA(cudaEventCreate(&e));
+    st.pass_events.push_back(e);
+  }
+  return st.pass_events[k];
+}
+
 static void run_steps(State& st, std::vector<Step>& steps, const Program& pg) {
   upload_program(st, pg);
   bool scaled = false;
   for (auto& s : steps) {
+    if (s.kind == Step::TBLOCK && s.digits && !scaled) {
+      // the digit scale, from the norm before the first digit pass
+      if (!st.d_scale) st.d_scale = static_cast<int*>(dev_alloc(st, 16));
+      launch_digit_scale(st, st.d_scale);
+      scaled = true;
+    }
+    const size_t ev = 2 * st.pass_class.size();
+    if (st.pass_timing) BF_CUDA(cudaEventRecord(pass_event(st, ev), st.stream));
     switch (s.kind) {
       case Step::GATE: launch_gate(st, s.gate); break;
       case Step::TILE: launch_tile_pass(st, st.d_prog + s.prog_off, s.nprog, s.tile); break;
       case Step::TBLOCK:
         if (s.digits) {
-          if (!scaled) {  // the digit scale, from the norm before the first digit pass
-            if (!st.d_scale) st.d_scale = static_cast<int*>(dev_alloc(st, 16));
-            launch_digit_scale(st, st.d_scale);
-            scaled = true;
-          }
           launch_block_pass_digits(st, reinterpret_cast<const Blk5*>(st.d_aux) + s.blk_off, s.nblk,
                                    st.d_aux + pg.images_offset(),
                                    reinterpret_cast<const uint16_t*>(st.d_aux + pg.offsets_offset()), s.tile,
@@ -647,6 +670,10 @@ static void run_steps(State& st, std::vector<Step>& steps, const Program& pg) {
       case Step::GROVER_LOOP: launch_grover_loop(st, s.marked.data(), (int)s.marked.size(), s.reps); break;
       case Step::MODEXP: launch_modexp(st, s.a, s.base, s.modulus); break;
     }
+    if (st.pass_timing) {
+      BF_CUDA(cudaEventRecord(pass_event(st, ev + 1), st.stream));
+      st.pass_class.push_back(pass_class_of(s));
+    }
   }
 }
 
@@ -661,7 +688,7 @@ void execute_ops(State& st, const bf_op* ops, int64_t nops, bf_exec_opts o) {
     fail(BF_EINVAL, "tile_qubits must be in [0, %d]", kMaxTileQubits);
   if (o.tile_qubits == 0) o.tile_qubits = env_int("BFGPU_TILE_QUBITS", default_tile_qubits(st));
   if (o.validate) validate_ops(st.n, ops, nops);
-  if (!o.tensor_blocks && env_int("BFGPU_TENSOR_BLOCKS", 0) && !st.shared_gpu) o.tensor_blocks = 1;
+  if (const char* tb = std::getenv("BFGPU_TENSOR_BLOCKS")) o.tensor_blocks = std::atoi(tb);
   std::vector<Step> steps;
   Program prog;
   build_steps(st.n, ops, nops, o, steps, prog, !st.shared_gpu, o.tensor_blocks != 0,
@@ -699,6 +726,8 @@ void release_state_members(State& st) {
   if (st.h_partial) cudaFreeHost(st.h_partial);
   if (st.h_flag) cudaFreeHost(st.h_flag);
   if (st.h_aux) cudaFreeHost(st.h_aux);
+  for (cudaEvent_t e : st.pass_events) cudaEventDestroy(e);
+  st.pass_events.clear();
   if (st.d_umat) cudaFree(st.d_umat);
   for (void* p : st.retired_host) cudaFreeHost(p);
   if (st.prog_event) cudaEventDestroy(st.prog_event);
@@ -744,6 +773,7 @@ int bf_exec_opts_init(bf_exec_opts* o) {
   o->specialized = BF_SPEC_ALL;
   o->tile_qubits = 0;
   o->sync = 0;
+  o->tensor_blocks = 1;
   return BF_OK;
 }
 
@@ -881,6 +911,33 @@ int bf_state_launch_count(const bf_state* hst, uint64_t* launches, int32_t reset
     if (!st || !launches) fail(BF_EINVAL, "null argument");
     *launches = st->launches;
     if (reset) const_cast<State*>(st)->launches = 0;
+  });
+}
+
+int bf_state_pass_timing(bf_state* hst, int32_t enable) {
+  State* st = S_(hst);
+  return guarded([&]() {
+    if (!st) fail(BF_EINVAL, "state is null");
+    st->pass_timing = enable != 0;
+  });
+}
+
+int bf_state_pass_times(bf_state* hst, int64_t* counts, double* ms) {
+  State* st = S_(hst);
+  return guarded([&]() {
+    if (!st || !counts || !ms) fail(BF_EINVAL, "null argument");
+    for (int c = 0; c < BF_PASS_CLASSES; ++c) {
+      counts[c] = 0;
+      ms[c] = 0;
+    }
+    BF_CUDA(cudaStreamSynchronize(st->stream));
+    for (size_t k = 0; k < st->pass_class.size(); ++k) {
+      float t = 0;
+      BF_CUDA(cudaEventElapsedTime(&t, st->pass_events[2 * k], st->pass_events[2 * k + 1]));
+      ++counts[st->pass_class[k]];
+      ms[st->pass_class[k]] += t;
+    }
+    st->pass_class.clear();
   });
 }
 
@@ -1069,7 +1126,8 @@ int bf_plan_stats(int32_t n, const bf_op* ops, int64_t nops, const bf_exec_opts*
     if (o.validate) validate_ops(n, ops, nops);
     std::vector<Step> steps;
     Program prog;
-    build_steps(n, ops, nops, o, steps, prog, true, o.tensor_blocks != 0);
+    build_steps(n, ops, nops, o, steps, prog, true, o.tensor_blocks != 0,
+                o.plan_dtype == BF_C64 ? BLOCK_TF32 : BLOCK_DIGITS);
     int64_t t = 0, g = 0, x = 0, bp = 0, nb = 0;
     double bytes = 0;
     for (auto& s : steps) {

@@ -193,6 +193,10 @@ struct State {
   size_t aux_cap = 0;
   // scale exponent of the complex128 digit passes (device int)
   int* d_scale = nullptr;
+  // pass timing: event pairs around each pass while enabled (pool reused)
+  bool pass_timing = false;
+  std::vector<cudaEvent_t> pass_events;
+  std::vector<int> pass_class;   // class of recorded pair k (events 2k, 2k+1)
 
   // pinned host buffers outgrown while copies from them may be in flight;
   // freed with the state (cudaFreeHost can synchronise the device)

@@ -160,13 +160,15 @@ typedef struct bf_exec_opts {
                                 norm it had before the circuit (double-float
                                 norms, FP64 factor); -1: never.  complex128
                                 states are never rescaled.                    */
-  int32_t tensor_blocks;     /* non-zero: tile passes group their gates into
-                                5-qubit blocks applied as tensor-core GEMMs
-                                (states of >= 12 qubits): 3xTF32 for
-                                complex64; for complex128 exact products of
-                                6 base-256 digits in bf16 (circuits of
-                                norm-preserving ops only)                     */
-  int32_t reserved;
+  int32_t tensor_blocks;     /* 1 (default): tile passes may group their gates
+                                into 5-qubit blocks applied as tensor-core
+                                GEMMs (states of >= 12 qubits; per pass, where
+                                cheaper): 3xTF32 for complex64; for complex128
+                                exact products of 6 base-256 digits in bf16
+                                (circuits of norm-preserving ops only).
+                                0: CUDA-core tile passes only               */
+  int32_t plan_dtype;        /* bf_plan_stats only: plan as for a BF_C128
+                                (default) or BF_C64 state                   */
 } bf_exec_opts;
 
 /* Fills *opts with the defaults above (strategy GPU_FUSED). */
@@ -205,6 +207,21 @@ int bf_execute(bf_state* st, const bf_op* ops, int64_t nops,
 /* Number of kernel launches bf_execute issued on this state since creation
  * (or since the last reset), for launch accounting. */
 int bf_state_launch_count(const bf_state* st, uint64_t* launches, int32_t reset);
+
+/* Pass timing: while enabled, bf_execute brackets every pass with CUDA events
+ * on the state's stream.  bf_state_pass_times waits for the stream and writes,
+ * per pass class, the number of timed passes and their summed device time in
+ * ms (arrays of BF_PASS_CLASSES), then clears the record.  The classes: */
+enum {
+  BF_PASS_GATE = 0,          /* per-gate kernels                          */
+  BF_PASS_TILE = 1,          /* CUDA-core shared-memory tile passes        */
+  BF_PASS_BLOCK_TF32 = 2,    /* complex64 3xTF32 tensor-core block passes  */
+  BF_PASS_BLOCK_DIGITS = 3,  /* complex128 digit tensor-core block passes  */
+  BF_PASS_OTHER = 4,         /* permutations, Grover, measurement, modexp  */
+  BF_PASS_CLASSES = 5
+};
+int bf_state_pass_timing(bf_state* st, int32_t enable);
+int bf_state_pass_times(bf_state* st, int64_t* counts, double* ms);
 
 /* ---- reductions ---------------------------------------------------------- */
 /* sum |amp|^2, accumulated in FP64 (state.mojo:482-501 accumulates in the

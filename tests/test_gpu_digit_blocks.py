@@ -1,0 +1,175 @@
+"""complex128 tile passes as 5-qubit blocks on the tensor cores, in exact
+base-256 digits (bf16 digit products summed exactly in FP32): parity with the
+FP64 oracle at max|Δamp| <= 1e-12 (scaled by the state's norm), with the
+double-float CUDA-core path, states of any norm, circuits that are not
+norm-preserving (planned without digit passes), pass timing, and the
+host-side plan (CPU)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from code_mojo_gb300 import butterfly as bfy
+from code_mojo_gb300 import workloads as W
+from oracle import pyoracle as O
+
+TOL = 1e-12
+
+
+def ctx(tensor: bool) -> bfy.ExecContext:
+    c = bfy.ExecContext()
+    c.execution_strategy = bfy.ExecutionStrategy.GPU_FUSED
+    c.gpu_tensor_blocks = tensor
+    return c
+
+
+def run(qc, re, im, tensor=True):
+    st = bfy.QuantumState.from_soa(re, im, "c128")
+    bfy.execute(st, qc, ctx(tensor))
+    out = st.to_complex()
+    st.close()
+    return out
+
+
+def oracle(qc, re, im):
+    r, i = O.run(qc, re, im)
+    return r + 1j * i
+
+
+def random_controlled_circuit(n, count, seed):
+    """CX / CCX / CP / CRY / U3 with controls and targets anywhere."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    qc = bfy.QuantumCircuit(n)
+    for _ in range(count):
+        kind = int(rng.integers(0, 5))
+        qs = [int(x) for x in rng.permutation(n)[:3]]
+        a = float(rng.uniform(0, 2 * np.pi))
+        if kind == 0:
+            qc.cx(qs[0], qs[1])
+        elif kind == 1:
+            qc.ccx(qs[0], qs[1], qs[2])
+        elif kind == 2:
+            qc.cp(qs[0], qs[1], a)
+        elif kind == 3:
+            qc.cry(qs[0], qs[1], a)
+        else:
+            qc.u3(qs[0], a, float(rng.uniform(0, 6)), float(rng.uniform(0, 6)))
+    return qc
+
+
+def test_plan_uses_digit_passes_for_complex128():
+    qc = W.random_layered_circuit(16, 8, seed=1)
+    on = bfy.plan_stats(qc, ctx(True), "c128")
+    off = bfy.plan_stats(qc, ctx(False), "c128")
+    assert on["block_passes"] > 0 and off["block_passes"] == 0
+    assert on["bytes_in_S"] <= off["bytes_in_S"]
+
+
+def test_plan_keeps_non_unitary_circuits_off_digit_passes():
+    """A gate that changes the norm: the digit scale could not bound the
+    state, so the whole circuit stays on double-float passes."""
+    qc = W.random_layered_circuit(16, 8, seed=1)
+    qc.custom(3, np.array([[1.0, 0.0], [0.0, 0.5]], dtype=np.complex128))
+    assert bfy.plan_stats(qc, ctx(True), "c128")["block_passes"] == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [12, 14, 16])
+def test_random_layered_from_basis(n):
+    qc = W.random_layered_circuit(n, 10, seed=n)
+    re, im = O.basis(n)
+    assert bfy.plan_stats(qc, ctx(True))["block_passes"] > 0
+    assert np.max(np.abs(run(qc, re, im) - oracle(qc, re, im))) <= TOL
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [13, 15])
+def test_qft_from_random_state(n):
+    qc = W.qft_circuit(n)
+    re, im = W.random_normal_state(n, 7)
+    assert np.max(np.abs(run(qc, re, im) - oracle(qc, re, im))) <= TOL
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_controls_and_targets_anywhere(seed):
+    n = 14
+    qc = random_controlled_circuit(n, 150, seed)
+    re, im = W.random_normal_state(n, seed)
+    assert np.max(np.abs(run(qc, re, im) - oracle(qc, re, im))) <= TOL
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scale", [1e-9, 1e-3, 37.0, 3e5])
+def test_states_of_any_norm(scale):
+    """The digit scale follows the norm: the error stays 1e-12 relative to it."""
+    n = 13
+    qc = W.random_layered_circuit(n, 8, seed=3)
+    re, im = W.random_normal_state(n, 4)
+    re, im = re * scale, im * scale
+    got = run(qc, re, im)
+    assert np.max(np.abs(got - oracle(qc, re, im))) <= TOL * scale
+
+
+@pytest.mark.gpu
+def test_matches_the_double_float_path():
+    n = 16
+    qc = W.random_layered_circuit(n, 12, seed=9)
+    re, im = W.random_normal_state(n, 9)
+    assert np.max(np.abs(run(qc, re, im, True) - run(qc, re, im, False))) <= TOL
+
+
+@pytest.mark.gpu
+def test_non_unitary_circuit_runs_on_double_float():
+    n = 13
+    qc = W.random_layered_circuit(n, 6, seed=2)
+    qc.custom(5, np.array([[1.0, 0.0], [0.0, 0.5]], dtype=np.complex128))
+    re, im = W.random_normal_state(n, 2)
+    assert np.max(np.abs(run(qc, re, im) - oracle(qc, re, im))) <= TOL
+
+
+@pytest.mark.gpu
+def test_repeated_runs_are_bit_identical():
+    """Digit sums are exact: the same input gives the same bits."""
+    n = 14
+    qc = W.random_layered_circuit(n, 6, seed=5)
+    re, im = W.random_normal_state(n, 5)
+    assert np.array_equal(run(qc, re, im), run(qc, re, im))
+
+
+@pytest.mark.gpu
+def test_pass_timing_counts_the_plan():
+    n = 16
+    qc = W.random_layered_circuit(n, 8, seed=6)
+    plan = bfy.plan_stats(qc, ctx(True))
+    st = bfy.QuantumState(n)
+    st.pass_timing(True)
+    bfy.execute(st, qc, ctx(True))
+    bfy.execute(st, qc, ctx(True))
+    t = st.pass_times()
+    st.pass_timing(False)
+    bfy.execute(st, qc, ctx(True))
+    after = st.pass_times()
+    st.close()
+    assert t["block_digits"][0] == 2 * plan["block_passes"]
+    assert t.get("tile", (0, 0))[0] == 2 * (plan["tile_passes"] - plan["block_passes"])
+    assert all(ms > 0 for _, ms in t.values())
+    assert after == {}
+
+
+@pytest.mark.gpu
+def test_30q_layered_round_trip_in_digits():
+    """Full size: the 40-layer circuit then its adjoint returns |0> on the
+    digit path (complex128, 16 GiB)."""
+    from code_mojo_gb300 import opsarray as OA
+    n = 30
+    ops = OA.random_layered(n, 40, 0)
+    assert bfy.plan_stats(ops, ctx(True))["block_passes"] > 0
+    st = bfy.QuantumState(n)
+    bfy.execute(st, ops, ctx(True))
+    bfy.execute(st, OA.adjoint(ops), ctx(True))
+    top_idx, top_p = st.topk(1)
+    norm = st.norm2()
+    st.close()
+    assert int(top_idx[0]) == 0 and top_p[0] >= 1 - 1e-10
+    assert abs(norm - 1) <= 1e-11

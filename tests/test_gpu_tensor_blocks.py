@@ -71,8 +71,8 @@ def random_controlled_circuit(n, count, seed):
 
 def test_plan_uses_block_passes_only_when_asked():
     qc = W.random_layered_circuit(16, 6, seed=1)
-    off = bfy.plan_stats(qc, ctx(False))
-    on = bfy.plan_stats(qc, ctx(True))
+    off = bfy.plan_stats(qc, ctx(False), "c64")
+    on = bfy.plan_stats(qc, ctx(True), "c64")
     assert off["block_passes"] == 0 and off["blocks"] == 0
     assert on["block_passes"] > 0 and on["blocks"] >= on["block_passes"]
     assert on["block_passes"] <= on["tile_passes"]
@@ -88,9 +88,9 @@ def test_passes_of_diagonal_gates_stay_on_cuda_cores():
     for _ in range(120):
         c, t = (int(x) for x in rng.permutation(12)[:2])
         qc.cp(c, t, float(rng.uniform(0, 2 * math.pi)))
-    s = bfy.plan_stats(qc, ctx(True))
+    s = bfy.plan_stats(qc, ctx(True), "c64")
     assert s["tile_passes"] >= 1 and s["block_passes"] < s["tile_passes"]
-    q = bfy.plan_stats(W.qft_circuit(20), ctx(True))
+    q = bfy.plan_stats(W.qft_circuit(20), ctx(True), "c64")
     assert q["block_passes"] < q["tile_passes"]
 
 
@@ -163,11 +163,11 @@ def test_small_states_use_the_cuda_core_path():
 
 
 @pytest.mark.gpu
-def test_complex128_ignores_the_option():
+def test_complex128_without_tensor_blocks():
     n = 13
     qc = W.random_layered_circuit(n, 8, seed=4)
     re, im = O.basis(n)
-    got, _ = run(qc, re, im, dtype="c128")
+    got, _ = run(qc, re, im, tensor=False, dtype="c128")
     r, i = O.run(qc, re, im)
     assert np.max(np.abs(got - (r + 1j * i))) <= 1e-12
 
@@ -218,7 +218,7 @@ def test_30q_layered_round_trip_on_tensor_cores():
     from code_mojo_gb300 import opsarray as OA
     n = 30
     ops = OA.random_layered(n, 40, 0)
-    assert bfy.plan_stats(ops, ctx(True))["block_passes"] > 0
+    assert bfy.plan_stats(ops, ctx(True), "c64")["block_passes"] > 0
     st = bfy.QuantumState(n, "c64")
     bfy.execute(st, ops, ctx(True))
     bfy.execute(st, OA.adjoint(ops), ctx(True))
