@@ -394,7 +394,10 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
                : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7])
+               :
+               : "memory");
 #pragma unroll
   for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
@@ -440,6 +443,35 @@ __device__ __forceinline__ void load_image_bytes(uint32_t dst, const void* src, 
 // rint for |x| < 2^22 on the FP32 pipe
 __device__ __forceinline__ float rint_small(float x) {
   return __fsub_rn(__fadd_rn(x, 12582912.0f), 12582912.0f);
+}
+// rint(t / 256) for |t| < 2^30: t / 256 is exact, and the FMA rounds its sum
+// with 1.5 * 2^23 once, to an integer
+__device__ __forceinline__ float rint_div256(float t) {
+  return __fsub_rn(__fmaf_rn(t, 0.00390625f, 12582912.0f), 12582912.0f);
+}
+
+// two 8-column TMEM loads in flight, one wait; the wait names the registers
+// so that no use of them is scheduled before it
+__device__ __forceinline__ void tmem_ld8x2(uint32_t ta, uint32_t tb, float* va, float* vb) {
+  uint32_t r[16];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(ta));
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                 "=r"(r[15])
+               : "r"(tb));
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                 "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                 "+r"(r[15])
+               :
+               : "memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    va[i] = __uint_as_float(r[i]);
+    vb[i] = __uint_as_float(r[8 + i]);
+  }
 }
 __device__ __forceinline__ int int_of_small(float x) {  // exact integer-valued |x| < 2^22
   return __float_as_int(__fadd_rn(x, 12582912.0f)) - 0x4B400000;
@@ -558,22 +590,31 @@ __global__ void __launch_bounds__(kDgThreads, 1) k_tblock_dg(const DgPassArgs a)
 
   for (; tile < a.ntiles && !failed; tile += gridDim.x) {
     const uint64_t obase = tile_base(tile);
-    // load: 8 amplitudes per thread, each as 6 digit pairs (re, im) into the planes
+    // load: 4 amplitudes per thread (all loads issued first), each as 6
+    // digit pairs (re, im) into the planes
+    double2 v[2 * kDgLoadIters];
 #pragma unroll
     for (int it = 0; it < kDgLoadIters; ++it) {
       const uint32_t i0 = (uint32_t)(it * kDgThreads + tid) * 2u;
       const double2* src = a.s + (obase | (i0 & 31u) | hoff[i0 >> 5]);
+      v[2 * it] = __ldcs(src);
+      v[2 * it + 1] = __ldcs(src + 1);
+    }
+    // the next tile's 128 rows of 32 amplitudes (512 contiguous bytes each:
+    // the tile holds qubits 0..4) into L2 while this tile computes
+    if (tid < 128 && tile + gridDim.x < a.ntiles) {
+      const double2* row = a.s + (tile_base(tile + gridDim.x) | hoff[tid]);
+      asm volatile("cp.async.bulk.prefetch.L2.global [%0], 512;" ::"l"(row) : "memory");
+    }
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const double2 v = __ldcs(src + h);
-        float dr[kDigits], di[kDigits];
-        range_ok &= digits_of(v.x, sh, dr);
-        range_ok &= digits_of(v.y, sh, di);
-        const uint32_t off = dest_at4(load_dest, 2 * it + h) << 2;
+    for (int e = 0; e < 2 * kDgLoadIters; ++e) {
+      float dr[kDigits], di[kDigits];
+      range_ok &= digits_of(v[e].x, sh, dr);
+      range_ok &= digits_of(v[e].y, sh, di);
+      const uint32_t off = dest_at4(load_dest, e) << 2;
 #pragma unroll
-        for (int p = 0; p < kDigits; ++p)
-          *reinterpret_cast<uint32_t*>(sm + (uint32_t)p * kDgPlane + off) = pack_bf16(dr[p], di[p]);
-      }
+      for (int p = 0; p < kDigits; ++p)
+        *reinterpret_cast<uint32_t*>(sm + (uint32_t)p * kDgPlane + off) = pack_bf16(dr[p], di[p]);
     }
     fence_proxy_async();
     __syncthreads();
@@ -631,25 +672,23 @@ __global__ void __launch_bounds__(kDgThreads, 1) k_tblock_dg(const DgPassArgs a)
       // Level s holds digit position s + 1 of the result.  From the lowest
       // level up: t = sum + carry, digit = t - 256 round(t / 256), carry the
       // rest; positions 6 and 7 only round; position 0 is the last carry.
+      // after the last block the result is V = hi 2^24 + lo with hi =
+      // carry 2^16 + d1 2^8 + d2 and lo = d3 2^16 + d4 2^8 + d5 (32-bit)
       float carry[kDgCols];
-      long long V[kDgCols];
+      int lo[kDgCols], hi[kDgCols];
 #pragma unroll
       for (int v = 0; v < kDgCols; ++v) {
         carry[v] = 0.f;
-        V[v] = 0;
+        lo[v] = 0;
+        hi[v] = 0;
       }
-      if (!mbar_wait(bar_lvl, ph_mma, a.spin_limit)) lost = true;
-      tc_fence_after();
-#pragma unroll
-      for (int s = kDgLevels - 1; s >= 0; --s) {
-        float d[kDgCols];
-        tmem_ld8(tlane + 64u * (uint32_t)s, d);
+      auto level = [&](const int s, float* d) {
         const int pos = s + 1;
 #pragma unroll
         for (int v = 0; v < kDgCols; ++v) {
           const float t = __fadd_rn(d[v], carry[v]);
-          const float q = rint_small(__fmul_rn(t, 0.00390625f));
-          d[v] = fmaf(q, -256.0f, t);
+          const float q = rint_div256(t);
+          d[v] = __fmaf_rn(q, -256.0f, t);
           carry[v] = q;
         }
         if (pos <= kDigits - 1) {
@@ -658,11 +697,28 @@ __global__ void __launch_bounds__(kDgThreads, 1) k_tblock_dg(const DgPassArgs a)
             for (int c = 0; c < kDgCplx; ++c)
               *reinterpret_cast<uint32_t*>(sm + (uint32_t)pos * kDgPlane + (dest_at4(dest, c) << 2)) =
                   pack_bf16(d[2 * c], d[2 * c + 1]);
+          } else if (pos >= 3) {
+#pragma unroll
+            for (int v = 0; v < kDgCols; ++v) lo[v] += int_of_small(d[v]) * (1 << (8 * (kDigits - 1 - pos)));
           } else {
 #pragma unroll
-            for (int v = 0; v < kDgCols; ++v) V[v] += (long long)int_of_small(d[v]) << (8 * (kDigits - 1 - pos));
+            for (int v = 0; v < kDgCols; ++v) hi[v] += int_of_small(d[v]) * (1 << (8 * (2 - pos)));
           }
         }
+      };
+      if (!mbar_wait(bar_lvl, ph_mma, a.spin_limit)) lost = true;
+      tc_fence_after();
+#pragma unroll
+      for (int s = kDgLevels - 1; s >= 1; s -= 2) {
+        float d0[kDgCols], d1[kDgCols];
+        tmem_ld8x2(tlane + 64u * (uint32_t)s, tlane + 64u * (uint32_t)(s - 1), d0, d1);
+        level(s, d0);
+        level(s - 1, d1);
+      }
+      if (kDgLevels & 1) {
+        float d0[kDgCols];
+        tmem_ld8(tlane, d0);
+        level(0, d0);
       }
       // position 0: the remaining carry
       if (more) {
@@ -674,8 +730,10 @@ __global__ void __launch_bounds__(kDgThreads, 1) k_tblock_dg(const DgPassArgs a)
         double2* stage = reinterpret_cast<double2*>(sm);
 #pragma unroll
         for (int c = 0; c < kDgCplx; ++c) {
-          const long long vr = V[2 * c] + ((long long)int_of_small(carry[2 * c]) << (8 * (kDigits - 1)));
-          const long long vi = V[2 * c + 1] + ((long long)int_of_small(carry[2 * c + 1]) << (8 * (kDigits - 1)));
+          const long long vr =
+              (long long)(hi[2 * c] + int_of_small(carry[2 * c]) * 65536) * 16777216ll + (long long)lo[2 * c];
+          const long long vi =
+              (long long)(hi[2 * c + 1] + int_of_small(carry[2 * c + 1]) * 65536) * 16777216ll + (long long)lo[2 * c + 1];
           stage[dest_at4(dest, c)] = make_double2(double_of(vr, e_scale - 48), double_of(vi, e_scale - 48));
         }
       }
