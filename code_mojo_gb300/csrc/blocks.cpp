@@ -109,10 +109,12 @@ uint64_t outside_set(const TileOp& t) { return t.cmask_out | (t.tloc < 0 ? (1ull
 
 namespace {
 
-// Index maps of one block: the 5 block qubits T (ascending: column bit r =
-// the r-th lowest) and the row order R (row bit r = local position R[r]).
+// Index maps of one block: the 5 block qubits T in column order J (column
+// bit k = local position J[k]) and the row order R (row bit r = local
+// position R[r]).
 struct BlockMap {
   uint32_t T = 0;
+  int J[5] = {0, 0, 0, 0, 0};
   int R[7] = {0, 0, 0, 0, 0, 0, 0};
   uint32_t dep_g(uint32_t g) const {
     uint32_t i = 0;
@@ -121,18 +123,14 @@ struct BlockMap {
   }
   uint32_t dep_j(uint32_t j) const {
     uint32_t i = 0;
-    int r = 0;
-    for (int pos = 0; pos < kBlockTileQubits; ++pos)
-      if ((T >> pos) & 1u) i |= ((j >> r++) & 1u) << pos;
+    for (int k = 0; k < 5; ++k) i |= ((j >> k) & 1u) << J[k];
     return i;
   }
   void ext(uint32_t i, uint32_t& g, uint32_t& j) const {
     g = 0;
     j = 0;
     for (int r = 0; r < 7; ++r) g |= ((i >> R[r]) & 1u) << r;
-    int r = 0;
-    for (int pos = 0; pos < kBlockTileQubits; ++pos)
-      if ((T >> pos) & 1u) j |= ((i >> pos) & 1u) << r++;
+    for (int k = 0; k < 5; ++k) j |= ((i >> J[k]) & 1u) << k;
   }
 };
 
@@ -143,12 +141,83 @@ struct BlockMap {
 BlockMap make_map(uint32_t T, uint32_t lane_positions) {
   BlockMap m;
   m.T = T;
+  int k = 0;
+  for (int pos = 0; pos < kBlockTileQubits; ++pos)
+    if ((T >> pos) & 1u) m.J[k++] = pos;
   int r = 0;
   for (int pos = 0; pos < kBlockTileQubits; ++pos)
     if (!((T >> pos) & 1u) && ((lane_positions >> pos) & 1u)) m.R[r++] = pos;
   for (int pos = 0; pos < kBlockTileQubits; ++pos)
     if (!((T >> pos) & 1u) && !((lane_positions >> pos) & 1u)) m.R[r++] = pos;
   return m;
+}
+
+// Maps of a digit pass.  An epilogue (or the load phase) writes 4-byte
+// operand words; the lanes of a warp vary 5 local positions P (the writer's
+// row bits 0..4; the load phase's positions 1..5) and the word of element
+// (g, j) lies in bank 4 ((j >> 2) ^ (g & 7)) + (j & 3).  The 32 lanes hit 32
+// banks when the positions of P, seen from the next block, supply bank bits
+// 0..4 once each: two of them as its column bits 0 and 1, the other three as
+// column bits 2..4 or row bits 0..2 (which the swizzle XORs onto bits 2..4).
+// So each block takes two positions of the writer's P as its lowest column
+// bits (padding its qubit set from P when it has fewer), the rest of P on
+// the matching column or row bits, and puts the next block's new qubits
+// among its own row bits 0..4, which are the lanes of its epilogue.
+std::vector<BlockMap> digit_maps(const std::vector<uint32_t>& qsets) {
+  std::vector<BlockMap> maps;
+  uint32_t P = 0x3Eu;  // load phase: lanes walk local positions 1..5
+  for (size_t b = 0; b < qsets.size(); ++b) {
+    BlockMap m;
+    uint32_t T = qsets[b];
+    for (int pos = 0; pos < kBlockTileQubits && __builtin_popcount(T) < 5; ++pos)
+      if (((P >> pos) & 1u) && !((T >> pos) & 1u) && __builtin_popcount(P & T) < 2) T |= 1u << pos;
+    for (int pos = 0; pos < kBlockTileQubits && __builtin_popcount(T) < 5; ++pos) T |= 1u << pos;
+    m.T = T;
+    int A[5], nA = 0, B[7], nB = 0;
+    for (int pos = 0; pos < kBlockTileQubits; ++pos)
+      if ((P >> pos) & 1u) {
+        if ((T >> pos) & 1u) A[nA++] = pos;
+        else B[nB++] = pos;
+      }
+    int J[5] = {-1, -1, -1, -1, -1}, R[7] = {-1, -1, -1, -1, -1, -1, -1};
+    int ia = 0, ib = 0;
+    for (int k = 0; k < 2 && ia < nA; ++k) J[k] = A[ia++];
+    for (int m2 = 0; m2 < 3; ++m2) {  // bank bit 2 + m2: column bit 2 + m2 or row bit m2
+      if (ia < nA) J[2 + m2] = A[ia++];
+      else if (ib < nB) R[m2] = B[ib++];
+    }
+    for (int r = 3; r < 7 && ib < nB; ++r) R[r] = B[ib++];
+    uint32_t used = 0;
+    for (int k = 0; k < 5; ++k)
+      if (J[k] >= 0) used |= 1u << J[k];
+    for (int k = 0, pos = 0; k < 5; ++k) {
+      if (J[k] >= 0) continue;
+      while (!((T >> pos) & 1u) || ((used >> pos) & 1u)) ++pos;
+      J[k] = pos;
+      used |= 1u << pos;
+    }
+    for (int r = 0; r < 7; ++r)
+      if (R[r] >= 0) used |= 1u << R[r];
+    // the next block's qubits that are not ours go to the free lane rows first
+    const uint32_t next = b + 1 < qsets.size() ? qsets[b + 1] & ~T : 0u;
+    for (int pass = 0; pass < 2; ++pass)
+      for (int r = 0; r < 7; ++r) {
+        if (R[r] >= 0 || (pass == 0 && r >= 5)) continue;
+        for (int pos = 0; pos < kBlockTileQubits; ++pos) {
+          if (((used | T) >> pos) & 1u) continue;
+          if (pass == 0 && !((next >> pos) & 1u)) continue;
+          R[r] = pos;
+          used |= 1u << pos;
+          break;
+        }
+      }
+    std::memcpy(m.J, J, sizeof J);
+    std::memcpy(m.R, R, sizeof R);
+    maps.push_back(m);
+    P = 0;
+    for (int r = 0; r < 5; ++r) P |= 1u << R[r];
+  }
+  return maps;
 }
 
 }  // namespace
@@ -194,19 +263,29 @@ bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsi
   if ((int)bl.size() > kMaxPassBlocks) return false;
   std::vector<BlockMap> maps;
   const size_t first = blocks.size();
-  // the load phase writes block 0's operands: a warp's lanes walk local bits 1..5
-  uint32_t lanes = 0x3Eu;
-  for (auto& b : bl) {
-    // pad to exactly 5 positions with unused tile qubits (identity on them)
-    uint32_t T = b.qset;
-    for (int pos = 0; pos < kBlockTileQubits && __builtin_popcount(T) < 5; ++pos) T |= 1u << pos;
-    maps.push_back(make_map(T, lanes));
-    // this block's epilogue: a warp's lanes walk its row bits 0..4
-    lanes = 0;
-    for (int r = 0; r < 5; ++r) lanes |= 1u << maps.back().R[r];
+  if (format == BLOCK_DIGITS) {
+    std::vector<uint32_t> qsets;
+    for (auto& b : bl) qsets.push_back(b.qset);
+    maps = digit_maps(qsets);
+  } else {
+    // the load phase writes block 0's operands: a warp's lanes walk local bits 1..5
+    uint32_t lanes = 0x3Eu;
+    for (auto& b : bl) {
+      // pad to exactly 5 positions with unused tile qubits (identity on them)
+      uint32_t T = b.qset;
+      for (int pos = 0; pos < kBlockTileQubits && __builtin_popcount(T) < 5; ++pos) T |= 1u << pos;
+      maps.push_back(make_map(T, lanes));
+      // this block's epilogue: a warp's lanes walk its row bits 0..4
+      lanes = 0;
+      for (int r = 0; r < 5; ++r) lanes |= 1u << maps.back().R[r];
+    }
+  }
+  for (size_t bi = 0; bi < bl.size(); ++bi) {
+    const BlockBuild& b = bl[bi];
+    const uint32_t T = maps[bi].T;
     int rank_of[kBlockTileQubits];
-    int r = 0;
-    for (int pos = 0; pos < kBlockTileQubits; ++pos) rank_of[pos] = ((T >> pos) & 1u) ? r++ : -1;
+    for (int pos = 0; pos < kBlockTileQubits; ++pos) rank_of[pos] = -1;
+    for (int k = 0; k < 5; ++k) rank_of[maps[bi].J[k]] = k;
     Blk5 d;
     std::memset(&d, 0, sizeof d);
     d.tmask = T;

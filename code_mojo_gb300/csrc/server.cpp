@@ -13,13 +13,14 @@
 // start and completion times.
 //
 // Scheduling: a request is large when 2^n * ops exceeds large_cost.  Small
-// requests wait in a FIFO and run on every slot at the highest stream
-// priority; large ones wait in a queue ordered by that cost (cheapest
-// first: under an offered load above capacity this completes the most
-// requests, and the biggest ones wait) and run only on the large slots, at
-// the lowest priority.  A large slot takes a small request first once the
-// oldest one has waited 20 ms, so that a backlog of large work cannot hold
-// small requests behind the few small-only slots.
+// requests wait in a FIFO and every slot that frees up takes the oldest one
+// before any large work; large ones wait in a queue ordered by that cost
+// (cheapest first: under an offered load above capacity this completes the
+// most requests, and the biggest ones wait) and run only on the large slots
+// while no small request waits.  Each slot owns a stream of the highest and
+// one of the lowest priority and runs small requests on the first, large
+// ones on the second, so the block scheduler hands SMs that free up to the
+// short requests first.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -62,7 +63,6 @@ struct Server {
   std::vector<bf_result> done;
   uint64_t next_id = 1, bytes_in_use = 0, peak_bytes = 0, budget = 0;
   uint64_t submitted = 0, completed = 0, failed = 0, running = 0;
-  double small_wait_s = 0.020;
   bool stop = false;
   std::vector<std::thread> workers;
 };
@@ -139,18 +139,21 @@ static void serve_one(Server& sv, State& st, ServedRequest& r, bf_result& res) {
 static void worker_main(Server* sv, int slot) {
   cudaSetDevice(sv->device);
   State st;
+  cudaStream_t s_hi = nullptr, s_lo = nullptr;
   bool ready = true;
   try {
     init_state_runtime(st);
     // the slot shares the GPU: no grid-wide persistent loops
     st.shared_gpu = true;
-    // small-request slots run at the highest stream priority, large-request
-    // slots at the lowest: the block scheduler then hands SMs that free up to
-    // the short requests first
+    // small requests on a stream of the highest priority, large ones on a
+    // stream of the lowest
     int lo = 0, hi = 0;
     BF_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
     BF_CUDA(cudaStreamDestroy(st.stream));
-    BF_CUDA(cudaStreamCreateWithPriority(&st.stream, cudaStreamNonBlocking, slot < sv->opts.large_slots ? lo : hi));
+    st.stream = nullptr;
+    BF_CUDA(cudaStreamCreateWithPriority(&s_hi, cudaStreamNonBlocking, hi));
+    BF_CUDA(cudaStreamCreateWithPriority(&s_lo, cudaStreamNonBlocking, lo));
+    st.stream = s_hi;
     // size the work buffers for the typical request up front
     upload_program_reserve(st, 16384);
     ensure_partials(st, 1 << 15);
@@ -169,23 +172,18 @@ static void worker_main(Server* sv, int slot) {
       auto fits_large = [&]() {
         return !sv->large_queue.empty() && sv->bytes_in_use + sv->large_queue.front()->bytes() <= sv->budget;
       };
-      // a small request that has waited longer than small_wait_s is served
-      // by any slot before large work
-      auto small_overdue = [&]() {
-        return fits_small() && now_s() - sv->queue.front()->t_submit > sv->small_wait_s;
-      };
-      // large slots take large requests first and otherwise help with small ones
       sv->cv_work.wait_for(lk, std::chrono::milliseconds(5),
                            [&]() { return sv->stop || fits_small() || (large_slot && fits_large()); });
       if (sv->stop) break;
-      if (!fits_small() && !(large_slot && fits_large())) continue;
-      if (large_slot && fits_large() && !small_overdue()) {
+      if (fits_small()) {
+        r = sv->queue.front();
+        sv->queue.pop_front();
+      } else if (large_slot && fits_large()) {
         std::pop_heap(sv->large_queue.begin(), sv->large_queue.end(), cheaper_last);
         r = sv->large_queue.back();
         sv->large_queue.pop_back();
       } else {
-        r = sv->queue.front();
-        sv->queue.pop_front();
+        continue;
       }
       sv->bytes_in_use += r->bytes();
       sv->peak_bytes = std::max(sv->peak_bytes, sv->bytes_in_use);
@@ -200,7 +198,12 @@ static void worker_main(Server* sv, int slot) {
     res.t_submit = r->t_submit;
     res.t_start = now_s();
     try {
-      if (!ready) fail(BF_ECUDA, "slot %d could not create its stream", slot);
+      if (!ready) fail(BF_ECUDA, "slot %d could not create its streams", slot);
+      cudaStream_t want = r->large ? s_lo : s_hi;
+      if (st.stream != want) {  // the other stream's work (an earlier request) is done first
+        BF_CUDA(cudaStreamSynchronize(st.stream));
+        st.stream = want;
+      }
       serve_one(*sv, st, *r, res);
       res.status = BF_OK;
     } catch (const Error& e) {
@@ -224,6 +227,12 @@ static void worker_main(Server* sv, int slot) {
     sv->cv_done.notify_all();
   }
   st.amp = nullptr;
+  // the state's members go with its current stream; the other one is idle
+  cudaStream_t other = st.stream == s_hi ? s_lo : s_hi;
+  if (other) {
+    cudaStreamSynchronize(other);
+    cudaStreamDestroy(other);
+  }
   release_state_members(st);
 }
 

@@ -288,8 +288,9 @@ int bf_batch_destroy(bf_batch* b);
  * running ones; states are allocated and freed stream-ordered, and requests
  * in different slots overlap on the device.  Requests whose estimated cost
  * (2^n * ops) is large wait in their own queue, cheapest first, served by
- * `large_slots` slots at the lowest stream priority, so they never hold
- * every slot while small requests queue. */
+ * `large_slots` slots at the lowest stream priority while no small request
+ * waits; a slot that frees up takes the oldest small request first and runs
+ * it at the highest stream priority. */
 typedef struct bf_server bf_server;
 typedef struct bf_server_opts {
   int32_t slots;              /* concurrent requests; 0 = 12, at most 64       */
