@@ -365,7 +365,9 @@ constexpr uint32_t kDgPlane = 16384;                       // 128 rows x 64 bf16
 constexpr uint32_t kDgSmemB = kDigits * kDgPlane;          // 6 A planes, then B
 constexpr uint32_t kDgSmemHoff = kDgSmemB + 2 * kDigitImageBytes;  // two image buffers
 constexpr uint32_t kDgSmemBar = kDgSmemHoff + 128 * 8;  // 2 image barriers, 7 level barriers, tmem slot
-constexpr uint32_t kDgSmemUsed = kDgSmemBar + 88;
+constexpr uint32_t kDgSmemBlk = kDgSmemBar + 128;             // the pass's block descriptors
+static_assert(sizeof(Blk5) == 32 && kDgSmemBlk % 16 == 0, "block descriptors are copied as 16-byte words");
+constexpr uint32_t kDgSmemUsed = kDgSmemBlk + kMaxPassBlocks * sizeof(Blk5);
 constexpr uint32_t kDgSmemAlloc = kDgSmemUsed + 1024;
 constexpr uint32_t kDgTmemCols = 512;                      // 7 levels x 64 columns
 constexpr int kDgLevels = 7;
@@ -484,12 +486,19 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
   return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632);
 }
 
-// round(x * 2^sh) as an integer of at most 48 bits and its 6 digits; false
-// when |x * 2^sh| >= 2^47 (the scale does not cover x)
+// byte j (0..3) of w minus 128, as an exact float: the byte goes into the
+// low mantissa bits of 1.5 * 2^23
+__device__ __forceinline__ float byte_digit(uint32_t w, int j) {
+  return __int_as_float((int)__byte_perm(w, 0x4B400000u, 0x7640u + (uint32_t)j)) - 12583040.0f;
+}
+
+// V = round(x * 2^sh), |V| < 2^47, as 6 balanced base-256 digits d (d[5]
+// the lowest): with W = V + 0x808080808080 every byte of W is its digit plus
+// 128 (the added 128s absorb the borrows), and the top digit is W / 2^40 -
+// 128.  False when |x * 2^sh| >= 2^47 (the scale does not cover x).
 __device__ __forceinline__ bool digits_of(double x, int sh, float* d) {
   const long long b = __double_as_longlong(x);
-  const int ex = (int)((b >> 52) & 0x7ff);
-  const long long m = (b & 0x000FFFFFFFFFFFFFll) | 0x0010000000000000ll;
+  const int ex = (int)((uint32_t)(b >> 52) & 0x7ffu);
   const int k = ex - 1075 + sh;  // |x| 2^sh = m 2^k
   long long V = 0;
   bool ok = true;
@@ -497,17 +506,19 @@ __device__ __forceinline__ bool digits_of(double x, int sh, float* d) {
     if (k > -6) {
       ok = false;
     } else {
+      const long long m = (b & 0x000FFFFFFFFFFFFFll) | 0x0010000000000000ll;
       V = (m + (1ll << (-k - 1))) >> (-k);
     }
   }
   if (b < 0) V = -V;
-#pragma unroll
-  for (int j = kDigits - 1; j >= 1; --j) {
-    const long long t = ((V & 255) ^ 128) - 128;
-    d[j] = float_of_small((int)t);
-    V = (V - t) >> 8;
-  }
-  d[0] = float_of_small((int)V);
+  const unsigned long long W = (unsigned long long)(V + 0x808080808080ll);
+  const uint32_t wl = (uint32_t)W, wh = (uint32_t)(W >> 32);
+  d[5] = byte_digit(wl, 0);
+  d[4] = byte_digit(wl, 1);
+  d[3] = byte_digit(wl, 2);
+  d[2] = byte_digit(wl, 3);
+  d[1] = byte_digit(wh, 0);
+  d[0] = __int_as_float((int)(0x4B400000u | (wh >> 8))) - 12583040.0f;
   return ok;
 }
 
@@ -529,6 +540,7 @@ __global__ void __launch_bounds__(kDgThreads, 1) k_tblock_dg(const DgPassArgs a)
   uint64_t* hoff = reinterpret_cast<uint64_t*>(sm + kDgSmemHoff);
   uint64_t* bars = reinterpret_cast<uint64_t*>(sm + kDgSmemBar);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + kDgSmemBar + 72);
+  Blk5* blk = reinterpret_cast<Blk5*>(sm + kDgSmemBlk);
   // bar_b + 8 k: image buffer k; bar_lvl + 8 s: the MMAs of level s (issued
   // from level 6 down, so a level's completion implies every higher level's)
   const uint32_t bar_b = smem_u32(&bars[0]), bar_lvl = smem_u32(&bars[2]);
@@ -552,6 +564,8 @@ __global__ void __launch_bounds__(kDgThreads, 1) k_tblock_dg(const DgPassArgs a)
       if ((h >> j) & 1) off |= 1ull << a.q[5 + j];
     hoff[h] = off;
   }
+  if (tid < a.nblocks * (int)(sizeof(Blk5) / 16))
+    reinterpret_cast<uint4*>(blk)[tid] = __ldg(reinterpret_cast<const uint4*>(a.blocks) + tid);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -580,16 +594,19 @@ __global__ void __launch_bounds__(kDgThreads, 1) k_tblock_dg(const DgPassArgs a)
   };
 
   uint64_t tile = blockIdx.x;
+  uint64_t next_base = 0;  // thread 0: tile_base of the CTA's next tile
   if (tid == 0 && tile < a.ntiles) {
-    const Blk5& b0 = a.blocks[0];
+    const Blk5& b0 = blk[0];
     load_image_bytes(sB, a.images + (size_t)(b0.img + variant_of(b0, tile_base(tile))) * kDigitImageBytes, bar_b,
                      kDigitImageBytes);
     b_in_flight |= 1;
   }
-  const uint2 load_dest = my_dests4(a.offsets, a.blocks[0].load_offs);
+  const uint2 load_dest = my_dests4(a.offsets, blk[0].load_offs);
 
   for (; tile < a.ntiles && !failed; tile += gridDim.x) {
     const uint64_t obase = tile_base(tile);
+    const bool has_next = tile + gridDim.x < a.ntiles;
+    if (tid == 0 && has_next) next_base = tile_base(tile + gridDim.x);
     // load: 4 amplitudes per thread (all loads issued first), each as 6
     // digit pairs (re, im) into the planes
     double2 v[2 * kDgLoadIters];
@@ -602,7 +619,7 @@ __global__ void __launch_bounds__(kDgThreads, 1) k_tblock_dg(const DgPassArgs a)
     }
     // the next tile's 128 rows of 32 amplitudes (512 contiguous bytes each:
     // the tile holds qubits 0..4) into L2 while this tile computes
-    if (tid < 128 && tile + gridDim.x < a.ntiles) {
+    if (tid < 128 && has_next) {
       const double2* row = a.s + (tile_base(tile + gridDim.x) | hoff[tid]);
       asm volatile("cp.async.bulk.prefetch.L2.global [%0], 512;" ::"l"(row) : "memory");
     }
@@ -621,7 +638,7 @@ __global__ void __launch_bounds__(kDgThreads, 1) k_tblock_dg(const DgPassArgs a)
 
     for (int bi = 0; bi < a.nblocks; ++bi) {
       const bool more = bi + 1 < a.nblocks;
-      const uint2 dest = my_dests4(a.offsets, a.blocks[bi].offs);
+      const uint2 dest = my_dests4(a.offsets, blk[bi].offs);
       bool lost = false;
       const uint32_t kb = kimg & 1u;
       const uint32_t sBk = sB + kb * kDigitImageBytes;
@@ -652,10 +669,10 @@ __global__ void __launch_bounds__(kDgThreads, 1) k_tblock_dg(const DgPassArgs a)
           const Blk5* nb = nullptr;
           uint64_t nbase = obase;
           if (more) {
-            nb = &a.blocks[bi + 1];
-          } else if (tile + gridDim.x < a.ntiles) {
-            nb = &a.blocks[0];
-            nbase = tile_base(tile + gridDim.x);
+            nb = &blk[bi + 1];
+          } else if (has_next) {
+            nb = &blk[0];
+            nbase = next_base;
           }
           if (nb) {
             load_image_bytes(sB + (kb ^ 1u) * kDigitImageBytes,
@@ -803,7 +820,8 @@ void launch_block_pass_digits(State& st, const Blk5* d_blocks, int nblocks, cons
                               const uint16_t* d_offsets, const TilePass& p, const int* d_exp) {
   if (st.dtype != BF_C128) fail(BF_EINVAL, "internal: digit blocks need a complex128 state");
   if (p.K != kBlockTileQubits || st.n < kBlockTileQubits) fail(BF_EINVAL, "internal: block pass needs a 12-qubit tile");
-  if (nblocks < 1) fail(BF_EINVAL, "internal: empty block pass");
+  if (nblocks < 1 || nblocks > kMaxPassBlocks) fail(BF_EINVAL, "internal: block pass of %d blocks", nblocks);
+  if (((uintptr_t)d_blocks & 15u) != 0) fail(BF_EINVAL, "internal: block descriptors must be 16-byte aligned");
   if (((uintptr_t)d_images & 15u) != 0 || ((uintptr_t)d_offsets & 15u) != 0)
     fail(BF_EINVAL, "internal: block images and tables must be 16-byte aligned");
   DgPassArgs a;
