@@ -593,20 +593,26 @@ __global__ void __launch_bounds__(kDgThreads, 1) k_tblock_dg(const DgPassArgs a)
     return ob;
   };
 
+  // Tile bases step by masked addition: with the tile positions filled with
+  // ones, adding the base of gridDim.x carries across them, so base(t + g) =
+  // ((base(t) | ~free) + base(g)) & free.
+  uint64_t tpos = 0;
+  for (int j = 0; j < kBlockTileQubits; ++j) tpos |= 1ull << a.q[j];
+  const uint64_t free_pos = ((a.ntiles << kBlockTileQubits) - 1) & ~tpos;
+  const uint64_t grid_base = tile_base(gridDim.x);
+  auto step_base = [&](uint64_t b) { return ((b | ~free_pos) + grid_base) & free_pos; };
   uint64_t tile = blockIdx.x;
-  uint64_t next_base = 0;  // thread 0: tile_base of the CTA's next tile
+  uint64_t obase = tile_base(tile);
   if (tid == 0 && tile < a.ntiles) {
     const Blk5& b0 = blk[0];
-    load_image_bytes(sB, a.images + (size_t)(b0.img + variant_of(b0, tile_base(tile))) * kDigitImageBytes, bar_b,
+    load_image_bytes(sB, a.images + (size_t)(b0.img + variant_of(b0, obase)) * kDigitImageBytes, bar_b,
                      kDigitImageBytes);
     b_in_flight |= 1;
   }
   const uint2 load_dest = my_dests4(a.offsets, blk[0].load_offs);
 
-  for (; tile < a.ntiles && !failed; tile += gridDim.x) {
-    const uint64_t obase = tile_base(tile);
+  for (; tile < a.ntiles && !failed; tile += gridDim.x, obase = step_base(obase)) {
     const bool has_next = tile + gridDim.x < a.ntiles;
-    if (tid == 0 && has_next) next_base = tile_base(tile + gridDim.x);
     // load: 4 amplitudes per thread (all loads issued first), each as 6
     // digit pairs (re, im) into the planes
     double2 v[2 * kDgLoadIters];
@@ -620,7 +626,7 @@ __global__ void __launch_bounds__(kDgThreads, 1) k_tblock_dg(const DgPassArgs a)
     // the next tile's 128 rows of 32 amplitudes (512 contiguous bytes each:
     // the tile holds qubits 0..4) into L2 while this tile computes
     if (tid < 128 && has_next) {
-      const double2* row = a.s + (tile_base(tile + gridDim.x) | hoff[tid]);
+      const double2* row = a.s + (step_base(obase) | hoff[tid]);
       asm volatile("cp.async.bulk.prefetch.L2.global [%0], 512;" ::"l"(row) : "memory");
     }
 #pragma unroll
@@ -672,7 +678,7 @@ __global__ void __launch_bounds__(kDgThreads, 1) k_tblock_dg(const DgPassArgs a)
             nb = &blk[bi + 1];
           } else if (has_next) {
             nb = &blk[0];
-            nbase = next_base;
+            nbase = step_base(obase);
           }
           if (nb) {
             load_image_bytes(sB + (kb ^ 1u) * kDigitImageBytes,
