@@ -273,9 +273,11 @@ uint64_t server_submit(Server& sv, int32_t n, int32_t dtype, const bf_op* ops, i
   }
   r->cost = (double)(1ull << n) * (double)std::max<int64_t>(1, nops);
   r->large = r->cost > (double)sv.opts.large_cost;
+  uint64_t id;
   {
     std::lock_guard<std::mutex> lk(sv.mu);
-    r->id = sv.next_id++;
+    // a slot may take, run and free the request as soon as the lock is released
+    id = r->id = sv.next_id++;
     r->t_submit = now_s();
     if (r->large) {
       sv.large_queue.push_back(r);
@@ -286,7 +288,7 @@ uint64_t server_submit(Server& sv, int32_t n, int32_t dtype, const bf_op* ops, i
     sv.submitted++;
   }
   sv.cv_work.notify_all();
-  return r->id;
+  return id;
 }
 
 int server_poll(Server& sv, bf_result* out, int max) {

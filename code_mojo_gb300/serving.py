@@ -142,6 +142,11 @@ def poisson_run(server: Server, requests, rate: float, duration_s: float, drain_
     drained = server.wait_idle(drain_s)
     results += server.poll(1 << 16)
     wall = time.perf_counter() - t0
+    # every result must belong to a request of this run
+    unknown = [r.id for r in results if r.id not in cost]
+    if unknown:
+        raise RuntimeError(f"{len(unknown)} results with ids this run never submitted, e.g. {unknown[:4]}; "
+                           f"{len(ids)} submitted, ids {min(ids)}..{max(ids)}")
     ok = [r for r in results if r.status == 0]
     lat = np.array([r.latency_s for r in ok]) * 1e3
     svc = np.array([r.latency_s - r.queue_s for r in ok]) * 1e3

@@ -42,7 +42,10 @@ def run_mixed(reqs, dtype, slots=8):
 
 @pytest.mark.parametrize("dtype", ["c64", "c128"])
 def test_result_is_the_same_alone_and_in_the_mix(dtype):
-    reqs = small_mix()
+    # four requests of several milliseconds first, so that the small ones
+    # submitted behind them find those slots busy and run on others
+    heavy = [("random_layered", OA.random_layered(18, 24, s)) for s in range(4)]
+    reqs = heavy + small_mix()
     alone = run_alone(reqs, dtype)
     mixed, st = run_mixed(reqs, dtype)
     tol = 1e-12 if dtype == "c128" else 1e-6
