@@ -41,8 +41,8 @@ METRIC = "30q HBM GB/s vs peak; served circuits/s, p50/p99 ms at fidelity≥1-1e
 # the same kernels at 26 qubits; traffic grows in proportion to the amplitudes
 # a launch processes.  Double-float tile pass: 2.153 GB / 2^26.
 TILE_TRAFFIC_BYTES_PER_AMP = 32.08
-# complex128 digit block pass (k_tblock_dg): 2.092 GB / 2^26
-DIGIT_TRAFFIC_BYTES_PER_AMP = 31.17
+# complex128 digit block pass (k_tblock_dg): 2.102 GB / 2^26
+DIGIT_TRAFFIC_BYTES_PER_AMP = 31.33
 # Tensor work of one complex128 digit block on one 128-row tile (4096
 # amplitudes): 26 digit-pair products of 128 x 64 x 64, 2 flops each.
 DIGIT_FLOPS_PER_AMP_BLOCK = 26 * 2 * 128 * 64 * 64 / 4096
