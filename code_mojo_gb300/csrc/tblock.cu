@@ -53,7 +53,8 @@ constexpr uint32_t kSmemA1 = kAOpBytes;       // As
 constexpr uint32_t kSmemB = 2 * kAOpBytes;    // Rb (2 x 8 KiB), Rs (2 x 8 KiB)
 constexpr uint32_t kSmemHoff = kSmemB + kBlockImageBytes;
 constexpr uint32_t kSmemBar = kSmemHoff + 128 * 8;
-constexpr uint32_t kSmemUsed = kSmemBar + 32;
+constexpr uint32_t kSmemBlk = kSmemBar + 32;   // the pass's block descriptors
+constexpr uint32_t kSmemUsed = kSmemBlk + kMaxPassBlocks * sizeof(Blk5);
 constexpr uint32_t kSmemAlloc = kSmemUsed + 1024;  // slack for 1024-byte alignment
 constexpr uint32_t kTmemCols = 64;
 
@@ -186,6 +187,7 @@ __global__ void __launch_bounds__(kBlkThreads, 2) k_tblock(const BlkPassArgs a) 
   uint64_t* bars = reinterpret_cast<uint64_t*>(sm + kSmemBar);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + kSmemBar + 16);
   int* ok_slot = reinterpret_cast<int*>(sm + kSmemBar + 20);
+  Blk5* blk = reinterpret_cast<Blk5*>(sm + kSmemBlk);
   const uint32_t bar_b = smem_u32(&bars[0]), bar_mma = smem_u32(&bars[1]);
   const int tid = threadIdx.x, warp = tid >> 5;
 
@@ -206,6 +208,8 @@ __global__ void __launch_bounds__(kBlkThreads, 2) k_tblock(const BlkPassArgs a) 
       if ((h >> j) & 1) off |= 1ull << a.q[5 + j];
     hoff[h] = off;
   }
+  if (tid < a.nblocks * (int)(sizeof(Blk5) / 16))
+    reinterpret_cast<uint4*>(blk)[tid] = __ldg(reinterpret_cast<const uint4*>(a.blocks) + tid);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -230,17 +234,23 @@ __global__ void __launch_bounds__(kBlkThreads, 2) k_tblock(const BlkPassArgs a) 
     return ob;
   };
 
+  // tile bases step by masked addition (base(t + g) = ((base(t) | ~free) + base(g)) & free)
+  uint64_t tpos = 0;
+  for (int j = 0; j < kBlockTileQubits; ++j) tpos |= 1ull << a.q[j];
+  const uint64_t free_pos = ((a.ntiles << kBlockTileQubits) - 1) & ~tpos;
+  const uint64_t grid_base = tile_base(gridDim.x);
+  auto step_base = [&](uint64_t b) { return ((b | ~free_pos) + grid_base) & free_pos; };
   uint64_t tile = blockIdx.x;
+  uint64_t obase = tile_base(tile);
   if (tid == 0 && tile < a.ntiles) {
-    const Blk5& b0 = a.blocks[0];
-    load_image(sB, a.images + (size_t)(b0.img + variant_of(b0, tile_base(tile))) * kBlockImageBytes, bar_b);
+    const Blk5& b0 = blk[0];
+    load_image(sB, a.images + (size_t)(b0.img + variant_of(b0, obase)) * kBlockImageBytes, bar_b);
     b_in_flight = true;
   }
 
   static_assert(kLoadIters * 2 == kBlockThreadElems, "one destination table entry per loaded amplitude");
-  const uint4 load_dest = my_dests(a.offsets, a.blocks[0].load_offs);
-  for (; tile < a.ntiles && !failed; tile += gridDim.x) {
-    const uint64_t obase = tile_base(tile);
+  const uint4 load_dest = my_dests(a.offsets, blk[0].load_offs);
+  for (; tile < a.ntiles && !failed; tile += gridDim.x, obase = step_base(obase)) {
     // load: 16 bytes at a time, split into the block-0 operands
     float4 v[kLoadIters];
 #pragma unroll
@@ -258,7 +268,7 @@ __global__ void __launch_bounds__(kBlkThreads, 2) k_tblock(const BlkPassArgs a) 
 
     for (int bi = 0; bi < a.nblocks; ++bi) {
       const bool more = bi + 1 < a.nblocks;
-      const uint4 dest = my_dests(a.offsets, a.blocks[bi].offs);
+      const uint4 dest = my_dests(a.offsets, blk[bi].offs);
       if (tid == 0) {
         int ok = mbar_wait(bar_b, ph_b, a.spin_limit) ? 1 : 0;
         if (ok) {
@@ -279,26 +289,23 @@ __global__ void __launch_bounds__(kBlkThreads, 2) k_tblock(const BlkPassArgs a) 
             }
           }
           mma_commit(bar_mma);
+          // the next image's address while the MMAs run
+          const unsigned char* next_img = nullptr;
+          if (more) {
+            next_img = a.images + (size_t)(blk[bi + 1].img + variant_of(blk[bi + 1], obase)) * kBlockImageBytes;
+          } else if (tile + gridDim.x < a.ntiles) {
+            next_img = a.images + (size_t)(blk[0].img + variant_of(blk[0], step_base(obase))) * kBlockImageBytes;
+          }
           ok = mbar_wait(bar_mma, ph_mma, a.spin_limit) ? 1 : 0;
           if (!ok) mma_lost_phase = (int)ph_mma;
-        }
-        if (!ok) atomicExch(a.flag, 1);
-        *ok_slot = ok;
-        // the B buffer is free once the MMAs are done: fetch the next image
-        if (ok) {
-          const Blk5* nb = nullptr;
-          uint64_t nbase = obase;
-          if (more) {
-            nb = &a.blocks[bi + 1];
-          } else if (tile + gridDim.x < a.ntiles) {
-            nb = &a.blocks[0];
-            nbase = tile_base(tile + gridDim.x);
-          }
-          if (nb) {
-            load_image(sB, a.images + (size_t)(nb->img + variant_of(*nb, nbase)) * kBlockImageBytes, bar_b);
+          // the B buffer is free once the MMAs are done: fetch the next image
+          if (ok && next_img) {
+            load_image(sB, next_img, bar_b);
             b_in_flight = true;
           }
         }
+        if (!ok) atomicExch(a.flag, 1);
+        *ok_slot = ok;
       }
       ph_b ^= 1u;
       ph_mma ^= 1u;
@@ -861,7 +868,8 @@ void launch_block_pass(State& st, const Blk5* d_blocks, int nblocks, const unsig
                        const uint16_t* d_offsets, const TilePass& p) {
   if (st.dtype != BF_C64) fail(BF_EINVAL, "internal: tensor-core blocks need a complex64 state");
   if (p.K != kBlockTileQubits || st.n < kBlockTileQubits) fail(BF_EINVAL, "internal: block pass needs a 12-qubit tile");
-  if (nblocks < 1) fail(BF_EINVAL, "internal: empty block pass");
+  if (nblocks < 1 || nblocks > kMaxPassBlocks) fail(BF_EINVAL, "internal: block pass of %d blocks", nblocks);
+  if (((uintptr_t)d_blocks & 15u) != 0) fail(BF_EINVAL, "internal: block descriptors must be 16-byte aligned");
   if (((uintptr_t)d_images & 15u) != 0) fail(BF_EINVAL, "internal: block images must be 16-byte aligned");
   BlkPassArgs a;
   std::memset(&a, 0, sizeof a);
