@@ -134,43 +134,30 @@ struct BlockMap {
   }
 };
 
-// Row order of a block: the non-block positions written by the lanes of one
-// warp come first, so that a warp's 32 operand stores fall on different
-// 16-byte chunks of the 128-byte swizzle (the swizzle XORs the chunk with
-// the row's low three bits).
-BlockMap make_map(uint32_t T, uint32_t lane_positions) {
-  BlockMap m;
-  m.T = T;
-  int k = 0;
-  for (int pos = 0; pos < kBlockTileQubits; ++pos)
-    if ((T >> pos) & 1u) m.J[k++] = pos;
-  int r = 0;
-  for (int pos = 0; pos < kBlockTileQubits; ++pos)
-    if (!((T >> pos) & 1u) && ((lane_positions >> pos) & 1u)) m.R[r++] = pos;
-  for (int pos = 0; pos < kBlockTileQubits; ++pos)
-    if (!((T >> pos) & 1u) && !((lane_positions >> pos) & 1u)) m.R[r++] = pos;
-  return m;
-}
 
-// Maps of a digit pass.  An epilogue (or the load phase) writes 4-byte
-// operand words; the lanes of a warp vary 5 local positions P (the writer's
-// row bits 0..4; the load phase's positions 1..5) and the word of element
-// (g, j) lies in bank 4 ((j >> 2) ^ (g & 7)) + (j & 3).  The 32 lanes hit 32
-// banks when the positions of P, seen from the next block, supply bank bits
-// 0..4 once each: two of them as its column bits 0 and 1, the other three as
-// column bits 2..4 or row bits 0..2 (which the swizzle XORs onto bits 2..4).
-// So each block takes two positions of the writer's P as its lowest column
-// bits (padding its qubit set from P when it has fewer), the rest of P on
-// the matching column or row bits, and puts the next block's new qubits
-// among its own row bits 0..4, which are the lanes of its epilogue.
-std::vector<BlockMap> digit_maps(const std::vector<uint32_t>& qsets) {
+// Block maps whose operand writes avoid shared-memory bank conflicts.  An
+// epilogue (or the load phase) writes one word per lane; the lanes that share
+// a store wavefront vary `nlanes` local positions P (the writer's row bits
+// 0..nlanes-1; the load phase's positions 1..nlanes) and the word of element
+// (row g, column j) lies in a bank whose index has bits j0..j(nlow-1) and
+// j(nlow+m) ^ g(m) for m = 0..2 (the 128-byte swizzle XORs the row's low three
+// bits onto the 16-byte chunk): 4-byte digit words, nlow = 2 and 32 lanes;
+// 8-byte TF32 pairs, nlow = 1 and a half-warp of 16 lanes per wavefront.  The
+// wavefront is conflict-free when the positions of P, seen from the next
+// block, supply each of those bank bits once: nlow of them as its lowest
+// column bits, the others as column bits nlow.. or row bits 0..2.  So each
+// block takes nlow positions of the writer's P as its lowest column bits
+// (padding its qubit set from P when it has fewer), the rest of P on the
+// matching column or row bits, and puts the next block's new qubits among its
+// own lane rows.
+std::vector<BlockMap> conflict_free_maps(const std::vector<uint32_t>& qsets, int nlow, int nlanes) {
   std::vector<BlockMap> maps;
-  uint32_t P = 0x3Eu;  // load phase: lanes walk local positions 1..5
+  uint32_t P = ((1u << nlanes) - 1u) << 1;  // load phase: lanes walk local positions 1..nlanes
   for (size_t b = 0; b < qsets.size(); ++b) {
     BlockMap m;
     uint32_t T = qsets[b];
     for (int pos = 0; pos < kBlockTileQubits && __builtin_popcount(T) < 5; ++pos)
-      if (((P >> pos) & 1u) && !((T >> pos) & 1u) && __builtin_popcount(P & T) < 2) T |= 1u << pos;
+      if (((P >> pos) & 1u) && !((T >> pos) & 1u) && __builtin_popcount(P & T) < nlow) T |= 1u << pos;
     for (int pos = 0; pos < kBlockTileQubits && __builtin_popcount(T) < 5; ++pos) T |= 1u << pos;
     m.T = T;
     int A[5], nA = 0, B[7], nB = 0;
@@ -181,9 +168,9 @@ std::vector<BlockMap> digit_maps(const std::vector<uint32_t>& qsets) {
       }
     int J[5] = {-1, -1, -1, -1, -1}, R[7] = {-1, -1, -1, -1, -1, -1, -1};
     int ia = 0, ib = 0;
-    for (int k = 0; k < 2 && ia < nA; ++k) J[k] = A[ia++];
-    for (int m2 = 0; m2 < 3; ++m2) {  // bank bit 2 + m2: column bit 2 + m2 or row bit m2
-      if (ia < nA) J[2 + m2] = A[ia++];
+    for (int k = 0; k < nlow && ia < nA; ++k) J[k] = A[ia++];
+    for (int m2 = 0; m2 < 3; ++m2) {  // bank bit nlow + m2: column bit nlow + m2 or row bit m2
+      if (ia < nA) J[nlow + m2] = A[ia++];
       else if (ib < nB) R[m2] = B[ib++];
     }
     for (int r = 3; r < 7 && ib < nB; ++r) R[r] = B[ib++];
@@ -202,7 +189,7 @@ std::vector<BlockMap> digit_maps(const std::vector<uint32_t>& qsets) {
     const uint32_t next = b + 1 < qsets.size() ? qsets[b + 1] & ~T : 0u;
     for (int pass = 0; pass < 2; ++pass)
       for (int r = 0; r < 7; ++r) {
-        if (R[r] >= 0 || (pass == 0 && r >= 5)) continue;
+        if (R[r] >= 0 || (pass == 0 && r >= nlanes)) continue;
         for (int pos = 0; pos < kBlockTileQubits; ++pos) {
           if (((used | T) >> pos) & 1u) continue;
           if (pass == 0 && !((next >> pos) & 1u)) continue;
@@ -215,7 +202,7 @@ std::vector<BlockMap> digit_maps(const std::vector<uint32_t>& qsets) {
     std::memcpy(m.R, R, sizeof R);
     maps.push_back(m);
     P = 0;
-    for (int r = 0; r < 5; ++r) P |= 1u << R[r];
+    for (int r = 0; r < nlanes; ++r) P |= 1u << R[r];
   }
   return maps;
 }
@@ -263,22 +250,11 @@ bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsi
   if ((int)bl.size() > kMaxPassBlocks) return false;
   std::vector<BlockMap> maps;
   const size_t first = blocks.size();
-  if (format == BLOCK_DIGITS) {
+  {
     std::vector<uint32_t> qsets;
     for (auto& b : bl) qsets.push_back(b.qset);
-    maps = digit_maps(qsets);
-  } else {
-    // the load phase writes block 0's operands: a warp's lanes walk local bits 1..5
-    uint32_t lanes = 0x3Eu;
-    for (auto& b : bl) {
-      // pad to exactly 5 positions with unused tile qubits (identity on them)
-      uint32_t T = b.qset;
-      for (int pos = 0; pos < kBlockTileQubits && __builtin_popcount(T) < 5; ++pos) T |= 1u << pos;
-      maps.push_back(make_map(T, lanes));
-      // this block's epilogue: a warp's lanes walk its row bits 0..4
-      lanes = 0;
-      for (int r = 0; r < 5; ++r) lanes |= 1u << maps.back().R[r];
-    }
+    // digit words: 4 bytes, 32 lanes per wavefront; TF32 pairs: 8 bytes, 16
+    maps = format == BLOCK_DIGITS ? conflict_free_maps(qsets, 2, 5) : conflict_free_maps(qsets, 1, 4);
   }
   for (size_t bi = 0; bi < bl.size(); ++bi) {
     const BlockBuild& b = bl[bi];
