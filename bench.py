@@ -360,8 +360,8 @@ def run_precision_bench(n_big: int, n_cmp: int, layers: int) -> dict:
         st.set_basis(0)
         lay = timed(st, qc, ctx(t))
         q = timed(st, qft, ctx(t))
-        out[name] = {"layered_ms": lay, "qft_ms": q, "plan_layered": bfy.plan_stats(qc, ctx(t)),
-                     "plan_qft": bfy.plan_stats(qft, ctx(t))}
+        out[name] = {"layered_ms": lay, "qft_ms": q, "plan_layered": bfy.plan_stats(qc, ctx(t), "c64"),
+                     "plan_qft": bfy.plan_stats(qft, ctx(t), "c64")}
     st.close()
     out["tensor_over_cuda_core_speed"] = ((out["cuda_cores"]["layered_ms"] + out["cuda_cores"]["qft_ms"]) /
                                           (out["tensor_cores"]["layered_ms"] + out["tensor_cores"]["qft_ms"]))

@@ -362,6 +362,27 @@ def test_random_layered_30q_round_trip():
     st.close()
 
 
+def test_random_layered_30q_matches_the_oracle():
+    """Full size against the oracle itself: two layers of the 30-qubit circuit
+    (60 U3 + 30 CX), the oracle's SIMD_PARALLEL port on the host cores (itself
+    checked against SCALAR at smaller sizes), compared amplitude by amplitude
+    in 64 MiB blocks."""
+    n = 30
+    qc = W.random_layered_circuit(n, 2, seed=0)
+    re, im = O.basis(n)
+    O.run_inplace(qc, re, im, strategy=O.OR_SIMD_PARALLEL, threads=O.num_cores(), chunks=O.num_cores())
+    st = bfy.QuantumState(n)
+    bfy.execute(st, qc)
+    blk = 1 << 22
+    gr, gi = np.empty(blk), np.empty(blk)
+    worst = 0.0
+    for off in range(0, 1 << n, blk):
+        F.check(F.lib().bf_state_download_range(st.handle, off, blk, gr.ctypes.data, gi.ctypes.data))
+        worst = max(worst, float(np.max(np.abs((gr - re[off:off + blk]) + 1j * (gi - im[off:off + blk])))))
+    st.close()
+    assert worst <= TOL128
+
+
 # ---- measurement and readout (apply_measure, state.mojo:447-553) --------------
 @pytest.mark.parametrize("dtype", ["c128", "c64"])
 @pytest.mark.parametrize("qubits,values", [([0, 1, 2], None), ([13, 2, 7], None), ([5], None),
