@@ -259,6 +259,43 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_qft_bench(n: int, reps: int) -> dict:
+    """The QFT workload: H + n(n-1)/2 CP + a full bit reversal on an N(0,1)
+    state (seed 0, unit norm), complex128, fused; CUDA events on the state's
+    stream around `reps` applications after 3 warm-up ones.  The 16 MiB state
+    of 20 qubits stays in L2, so the bandwidth figures are L2 figures."""
+    import torch
+    from code_mojo_gb300 import butterfly as bfy
+    from code_mojo_gb300 import workloads as W
+    qc = W.qft_circuit(n)
+    re, im = W.random_normal_state(n, 0)
+    st = bfy.QuantumState.from_soa(re, im)
+    ctx = bfy.ExecContext()
+    ctx.execution_strategy = bfy.ExecutionStrategy.GPU_FUSED
+    ctx.gpu_sync = False
+    stream = torch.cuda.ExternalStream(st.stream_ptr())
+    for _ in range(3):
+        bfy.execute(st, qc, ctx)
+    st.sync()
+    st.launch_count(reset=True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        bfy.execute(st, qc, ctx)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    launches = st.launch_count() / reps
+    st.close()
+    plan = bfy.plan_stats(qc, ctx)
+    pg = per_gate_bytes_in_S(qc)
+    S = 16.0 * (1 << n)
+    return {"qubits": n, "gates": len(qc.transformations), "ms_per_circuit": ms, "launches_per_circuit": launches,
+            "plan": plan, "per_gate_bytes_in_S": pg, "effective_GB_per_s": pg * S / (ms * 1e-3) / 1e9,
+            "fused_GB_per_s": plan["bytes_in_S"] * S / (ms * 1e-3) / 1e9,
+            "l2": f"state ({int(S) >> 20} MiB) stays in L2: bandwidths are L2 figures"}
+
+
 def run_batch_bench(count: int, reps: int, sample: int) -> dict:
     """The batched workload: `count` circuits, qubit counts uniform in [8, 20],
     half random layered (depth 20), half value encodings; one persistent
@@ -501,6 +538,7 @@ def run_ours(args) -> None:
                "d2h_bytes_per_step": 2 * 8 * N, "ms_per_step": dt * 1e3}
         del hre, him
 
+    qft = run_qft_bench(20, 50) if args.qft and rank == 0 else None
     batch = run_batch_bench(args.batch_count, 3, 256) if args.batch_count > 0 else None
     serving = (run_serving_bench(args.serve_rate, args.serve_seconds, args.serve_seconds, 12)
                if args.serve_seconds > 0 else None)
@@ -543,6 +581,7 @@ def run_ours(args) -> None:
         "clocks": clk.summary(),
         "e2e": e2e,
         "cpu_baseline": cpu,
+        "qft20": qft,
         "batch": batch,
         "serving": serving,
         "precision": precision,
@@ -565,6 +604,7 @@ def main():
     ap.add_argument("--cpu-gates", type=int, default=45)
     ap.add_argument("--ref-gates", type=int, default=15)
     ap.add_argument("--batch-count", type=int, default=4096)
+    ap.add_argument("--qft", type=int, default=1, help="time the 20-qubit QFT workload (0: skip)")
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--precision-qubits", type=int, default=33,

@@ -449,10 +449,6 @@ __device__ __forceinline__ void load_image_bytes(uint32_t dst, const void* src, 
                : "memory");
 }
 
-// rint for |x| < 2^22 on the FP32 pipe
-__device__ __forceinline__ float rint_small(float x) {
-  return __fsub_rn(__fadd_rn(x, 12582912.0f), 12582912.0f);
-}
 // rint(t / 256) for |t| < 2^30: t / 256 is exact, and the FMA rounds its sum
 // with 1.5 * 2^23 once, to an integer
 __device__ __forceinline__ float rint_div256(float t) {
@@ -484,9 +480,6 @@ __device__ __forceinline__ void tmem_ld8x2(uint32_t ta, uint32_t tb, float* va, 
 }
 __device__ __forceinline__ int int_of_small(float x) {  // exact integer-valued |x| < 2^22
   return __float_as_int(__fadd_rn(x, 12582912.0f)) - 0x4B400000;
-}
-__device__ __forceinline__ float float_of_small(int v) {  // |v| < 2^22
-  return __fsub_rn(__int_as_float(0x4B400000 + v), 12582912.0f);
 }
 // two exact small-integer floats -> (bf16 lo | bf16 hi << 16)
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
