@@ -124,10 +124,14 @@ struct Program {
   size_t aux_bytes() const { return blocks.empty() ? 0 : offsets_offset() + offsets.size() * sizeof(uint16_t); }
 };
 
-static void upload_program(State& st, const Program& pg) {
+// id: the plan's cache id (0: not cached); a program already on the device
+// for the same id is not uploaded again
+static void upload_program(State& st, const Program& pg, uint64_t id) {
   const std::vector<TileOp>& prog = pg.ops;
   const size_t aux = pg.aux_bytes();
   if (prog.empty() && aux == 0) return;
+  if (id != 0 && st.uploaded_plan == id) return;
+  st.uploaded_plan = id;
   if (st.prog_event_live) BF_CUDA(cudaEventSynchronize(st.prog_event));
   if (!prog.empty()) {
     upload_program_reserve(st, prog.size());
@@ -139,7 +143,6 @@ static void upload_program(State& st, const Program& pg) {
       size_t cap = std::max(aux, 2 * st.aux_cap);
       host_retire(st, st.h_aux);
       dev_free(st, st.d_aux);
-    dev_free(st, st.d_scale);
       st.h_aux = nullptr;
       st.d_aux = nullptr;
       st.aux_cap = 0;
@@ -385,8 +388,12 @@ static void build_steps(int n, const bf_op* ops, int64_t nops, const bf_exec_opt
       Step s;
       if (ps.is_tile && tensor && ps.tile.K == kBlockTileQubits && ps.tile.L == kTileLowQubits) {
         size_t b0 = pg.blocks.size(), i0 = pg.images.size(), o0 = pg.offsets.size();
-        if (plan_blocks(ps.tile, pg.blocks, pg.images, pg.offsets, format) &&
-            (double)(pg.blocks.size() - b0) * block_units < cuda_core_units(ps.tile)) {
+        // the most blocks for which the block pass is still the cheaper form
+        const double cu = cuda_core_units(ps.tile);
+        int max_blocks = 0;
+        while (max_blocks < kMaxPassBlocks && (double)(max_blocks + 1) * block_units < cu) ++max_blocks;
+        if (max_blocks > 0 && plan_blocks(ps.tile, pg.blocks, pg.images, pg.offsets, format, max_blocks) &&
+            (double)(pg.blocks.size() - b0) * block_units < cu) {
           s.kind = Step::TBLOCK;
           s.digits = format == BLOCK_DIGITS;
           s.tile = ps.tile;
@@ -630,10 +637,10 @@ static cudaEvent_t pass_event(State& st, size_t k) {
   return st.pass_events[k];
 }
 
-static void run_steps(State& st, std::vector<Step>& steps, const Program& pg) {
-  upload_program(st, pg);
+static void run_steps(State& st, const std::vector<Step>& steps, const Program& pg, uint64_t plan_id) {
+  upload_program(st, pg, plan_id);
   bool scaled = false;
-  for (auto& s : steps) {
+  for (const auto& s : steps) {
     if (s.kind == Step::TBLOCK && s.digits && !scaled) {
       // the digit scale, from the norm before the first digit pass
       if (!st.d_scale) st.d_scale = static_cast<int*>(dev_alloc(st, 16));
@@ -679,6 +686,41 @@ static void run_steps(State& st, std::vector<Step>& steps, const Program& pg) {
 
 static void free_state(State* st);
 
+// A state's last few plans, keyed by the exact op list (each op with its data
+// and qubit lists) and the options that shape a plan: running a circuit again
+// skips planning and, while its program is still on the device, the upload.
+struct PlanCache {
+  struct Entry {
+    std::vector<unsigned char> key;
+    std::vector<Step> steps;
+    Program prog;
+    uint64_t id = 0;
+  };
+  static constexpr size_t kEntries = 4;
+  std::vector<Entry> entries;  // most recent first
+  uint64_t next_id = 1;
+};
+
+static void plan_key(std::vector<unsigned char>& k, const State& st, const bf_op* ops, int64_t nops,
+                     const bf_exec_opts& o, BlockFormat format) {
+  auto put = [&](const void* p, size_t n) {
+    const unsigned char* c = static_cast<const unsigned char*>(p);
+    k.insert(k.end(), c, c + n);
+  };
+  const int32_t head[8] = {st.n, st.dtype, (int32_t)format, st.shared_gpu ? 1 : 0, o.strategy, o.tile_qubits,
+                           (int32_t)o.specialized, o.tensor_blocks};
+  k.reserve(sizeof head + (size_t)nops * sizeof(bf_op));
+  put(head, sizeof head);
+  for (int64_t i = 0; i < nops; ++i) {
+    bf_op c = ops[i];
+    c.data = nullptr;
+    c.qubits = nullptr;
+    put(&c, sizeof c);
+    if (ops[i].data) put(ops[i].data, op_data_len(ops[i]) * sizeof(double));
+    if (ops[i].qubits) put(ops[i].qubits, op_qubits_len(ops[i]) * sizeof(int32_t));
+  }
+}
+
 void execute_ops(State& st, const bf_op* ops, int64_t nops, bf_exec_opts o) {
   if (o.strategy >= 0 && o.strategy <= 7)
     fail(BF_EUNSUPPORTED, "Execution strategy %d is a CPU strategy; use BF_STRATEGY_GPU(_FUSED)", o.strategy);
@@ -689,16 +731,34 @@ void execute_ops(State& st, const bf_op* ops, int64_t nops, bf_exec_opts o) {
   if (o.tile_qubits == 0) o.tile_qubits = env_int("BFGPU_TILE_QUBITS", default_tile_qubits(st));
   if (o.validate) validate_ops(st.n, ops, nops);
   if (const char* tb = std::getenv("BFGPU_TENSOR_BLOCKS")) o.tensor_blocks = std::atoi(tb);
-  std::vector<Step> steps;
-  Program prog;
-  build_steps(st.n, ops, nops, o, steps, prog, !st.shared_gpu, o.tensor_blocks != 0,
-              st.dtype == BF_C128 ? BLOCK_DIGITS : BLOCK_TF32);
+  const BlockFormat format = st.dtype == BF_C128 ? BLOCK_DIGITS : BLOCK_TF32;
+  std::vector<unsigned char> key;
+  plan_key(key, st, ops, nops, o, format);
+  if (!st.plans) st.plans = new PlanCache();
+  auto& entries = st.plans->entries;
+  size_t hit = entries.size();
+  for (size_t e = 0; e < entries.size(); ++e)
+    if (entries[e].key == key) {
+      hit = e;
+      break;
+    }
+  if (hit == entries.size()) {
+    PlanCache::Entry ne;
+    build_steps(st.n, ops, nops, o, ne.steps, ne.prog, !st.shared_gpu, o.tensor_blocks != 0, format);
+    ne.key = std::move(key);
+    ne.id = st.plans->next_id++;
+    entries.insert(entries.begin(), std::move(ne));
+    if (entries.size() > PlanCache::kEntries) entries.pop_back();
+  } else if (hit != 0) {
+    std::rotate(entries.begin(), entries.begin() + (std::ptrdiff_t)hit, entries.begin() + (std::ptrdiff_t)hit + 1);
+  }
+  const PlanCache::Entry& plan = entries.front();
   // FP32 matrices are unitary only to ~6e-8, and that error changes the norm
   // coherently at every gate; the complex64 form restores the input norm.
   // renormalize == 2 (internal): the input is known to have unit norm.
   bool renorm = st.dtype == BF_C64 && nops > 0 && o.renormalize >= 0;
   if (renorm && o.renormalize != 2) launch_norm_before(st);
-  run_steps(st, steps, prog);
+  run_steps(st, plan.steps, plan.prog, plan.id);
   if (renorm) launch_renormalize(st, o.renormalize == 2);
   flag_readback(st);
 }
@@ -717,8 +777,11 @@ void release_state_members(State& st) {
     dev_free(st, st.d_renorm);
     dev_free(st, st.d_flag);
     dev_free(st, st.d_aux);
+    dev_free(st, st.d_scale);
     cudaStreamSynchronize(st.stream);
   }
+  delete st.plans;
+  st.plans = nullptr;
   if (st.amp) cudaFree(st.amp);
   if (st.scratch) cudaFree(st.scratch);
   if (st.h_prog) cudaFreeHost(st.h_prog);

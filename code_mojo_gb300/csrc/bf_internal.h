@@ -121,10 +121,10 @@ constexpr uint32_t kDigitImageBytes = kDigits * 8192;
 // next block's operand offset in the format's units, or after the last
 // block the staging slot); false when an op cannot be placed (more than 5
 // tile qubits or more than 3 outside qubits on its own), the pass needs more
-// than kMaxPassBlocks blocks, or (BLOCK_DIGITS) a block's matrix is not
-// unitary to 1e-12.
+// than min(kMaxPassBlocks, max_blocks) blocks (checked before any matrix is
+// built), or (BLOCK_DIGITS) a block's matrix is not unitary to 1e-12.
 bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsigned char>& images,
-                 std::vector<uint16_t>& offsets, BlockFormat format = BLOCK_TF32);
+                 std::vector<uint16_t>& offsets, BlockFormat format = BLOCK_TF32, int max_blocks = kMaxPassBlocks);
 #ifdef __CUDACC__
 #define BF_HOST_DEVICE __host__ __device__
 #else
@@ -149,6 +149,8 @@ BF_HOST_DEVICE inline uint32_t block_stage_slot(uint32_t i) { return i ^ (((i >>
 void block_image(const double* u, unsigned char* img);
 
 // ---------------------------------------------------------------------------
+struct PlanCache;  // a state's recent plans (api.cpp)
+
 // The device state.
 struct State {
   int32_t n = 0;
@@ -193,6 +195,9 @@ struct State {
   size_t aux_cap = 0;
   // scale exponent of the complex128 digit passes (device int)
   int* d_scale = nullptr;
+  // recent plans and the one whose program is on the device
+  PlanCache* plans = nullptr;
+  uint64_t uploaded_plan = 0;
   // pass timing: event pairs around each pass while enabled (pool reused)
   bool pass_timing = false;
   std::vector<cudaEvent_t> pass_events;

@@ -210,7 +210,7 @@ std::vector<BlockMap> conflict_free_maps(const std::vector<uint32_t>& qsets, int
 }  // namespace
 
 bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsigned char>& images,
-                 std::vector<uint16_t>& offsets, BlockFormat format) {
+                 std::vector<uint16_t>& offsets, BlockFormat format, int max_blocks) {
   const uint32_t image_bytes = format == BLOCK_DIGITS ? kDigitImageBytes : kBlockImageBytes;
   // destination of complex element (g, j) of a block's operands, in the
   // units of the kernel's table (TF32: bytes / 8; digits: bytes / 4 in a plane)
@@ -247,7 +247,8 @@ bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsi
     bl[place].ops.push_back(&t);
   }
 
-  if ((int)bl.size() > kMaxPassBlocks) return false;
+  // more blocks than the pass is worth: decided before any matrix is built
+  if ((int)bl.size() > std::min(kMaxPassBlocks, max_blocks)) return false;
   std::vector<BlockMap> maps;
   const size_t first = blocks.size();
   {

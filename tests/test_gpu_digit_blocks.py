@@ -173,3 +173,43 @@ def test_30q_layered_round_trip_in_digits():
     st.close()
     assert int(top_idx[0]) == 0 and top_p[0] >= 1 - 1e-10
     assert abs(norm - 1) <= 1e-11
+
+
+@pytest.mark.gpu
+def test_plans_of_growing_size_on_one_state():
+    """A state runs a small digit plan, a larger one (its block buffers grow)
+    and the small one again: every result matches the oracle."""
+    n = 14
+    small = W.random_layered_circuit(n, 2, seed=11)
+    large = W.random_layered_circuit(n, 24, seed=12)
+    re, im = W.random_normal_state(n, 13)
+    st = bfy.QuantumState(n)
+    for qc in (small, large, small):
+        st.upload(re, im)
+        bfy.execute(st, qc, ctx(True))
+        assert np.max(np.abs(st.to_complex() - oracle(qc, re, im))) <= TOL
+    st.close()
+
+
+@pytest.mark.gpu
+def test_plan_cache_tells_circuits_apart():
+    """A state keeps its recent plans keyed by the exact op list: circuits that
+    differ only in their matrices, or in the data of a unitary, get their own
+    plans, and running one again reuses its plan with the right result."""
+    n = 13
+    a = W.random_layered_circuit(n, 4, seed=21)
+    b = W.random_layered_circuit(n, 4, seed=22)  # same shape, other angles
+    u1 = np.linalg.qr(np.random.default_rng(1).normal(size=(4, 4)) + 1j * np.random.default_rng(2).normal(size=(4, 4)))[0]
+    u2 = np.linalg.qr(np.random.default_rng(3).normal(size=(4, 4)) + 1j * np.random.default_rng(4).normal(size=(4, 4)))[0]
+    c1, c2 = bfy.QuantumCircuit(n), bfy.QuantumCircuit(n)
+    c1.transformations = list(a.transformations)
+    c2.transformations = list(a.transformations)
+    c1.unitary(u1, 3, 2)
+    c2.unitary(u2, 3, 2)
+    re, im = W.random_normal_state(n, 23)
+    st = bfy.QuantumState(n)
+    for qc in (a, b, c1, c2, a, c2, b, c1):
+        st.upload(re, im)
+        bfy.execute(st, qc, ctx(True))
+        assert np.max(np.abs(st.to_complex() - oracle(qc, re, im))) <= TOL
+    st.close()
