@@ -241,7 +241,8 @@ Server* server_create(const bf_server_opts& opts) {
   sv->opts = opts;
   if (sv->opts.slots <= 0) sv->opts.slots = 12;
   if (sv->opts.slots > 64) fail(BF_EINVAL, "at most 64 slots");
-  if (sv->opts.large_slots <= 0) sv->opts.large_slots = std::max(1, sv->opts.slots - 2);
+  // a third of the slots (at least 2) serve small requests only
+  if (sv->opts.large_slots <= 0) sv->opts.large_slots = std::max(1, sv->opts.slots - std::max(2, sv->opts.slots / 3));
   if (sv->opts.large_slots > sv->opts.slots) fail(BF_EINVAL, "large_slots exceeds slots");
   if (sv->opts.large_cost == 0) sv->opts.large_cost = 1ull << 28;
   if (sv->opts.topk <= 0) sv->opts.topk = 16;

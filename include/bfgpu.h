@@ -296,7 +296,8 @@ typedef struct bf_server_opts {
   int32_t slots;              /* concurrent requests; 0 = 12, at most 64       */
   int32_t tile_qubits;        /* fusion width; 0 = default                     */
   int32_t topk;               /* outcomes returned per request, 1..16; 0 = 16 */
-  int32_t large_slots;        /* slots that run large requests; 0 = slots-2   */
+  int32_t large_slots;        /* slots that run large requests; 0: all but a
+                                 third of the slots (at least 2)           */
   uint64_t hbm_budget_bytes;  /* statevector bytes admitted at once;
                                  0 = 80 % of the free HBM at creation         */
   uint64_t large_cost;        /* a request is large when 2^n * ops exceeds
