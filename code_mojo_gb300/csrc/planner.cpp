@@ -226,6 +226,26 @@ static TileOp to_tile_op(const GateInstr& g, const int* loc_of) {
   return t;
 }
 
+// The work (per-gate bytes, in units of S) a tile pass over the qubit set
+// inQ takes from the remaining gates: a gate joins when its non-diagonal
+// target is in the set and it commutes with every gate deferred before it.
+static double pass_work(const std::vector<const GateInstr*>& remaining, uint64_t inQ) {
+  uint64_t blockedX = 0, blockedAll = 0;
+  double w = 0;
+  for (const GateInstr* g : remaining) {
+    const uint64_t tb = 1ull << g->target;
+    const uint64_t Xg = gk_is_diagonal(g->kind) ? 0 : tb;
+    const uint64_t Ag = g->cmask | tb;
+    if (!(Xg & blockedAll) && !(Ag & blockedX) && !(Xg & ~inQ)) {
+      w += gate_bytes_fraction(*g);
+    } else {
+      blockedX |= Xg;
+      blockedAll |= Ag;
+    }
+  }
+  return w;
+}
+
 std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int K, bool allow_single) {
   std::vector<PlanStep> steps;
   if (gates.empty()) return steps;
@@ -233,35 +253,74 @@ std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int
   // Low qubits always in the tile; when the tile is narrower than the state
   // at least one slot stays free, so every pass can take the next gate.
   const int L = (K >= n) ? std::min(K, kTileLowQubits) : std::min(K - 1, kTileLowQubits);
+  const uint64_t low = (L >= 64) ? ~0ull : ((1ull << L) - 1);
   std::vector<const GateInstr*> remaining;
   for (auto& g : gates) remaining.push_back(&g);
   while (!remaining.empty()) {
-    uint64_t inQ = (L >= 64) ? ~0ull : ((1ull << L) - 1);
+    // the tile's qubits: first the targets in order of appearance among the
+    // gates that could still join (first come), then single swaps of a chosen
+    // qubit for another target while that lets the pass take more work
+    uint64_t inQ = low;
     int nQ = L;
-    std::vector<const GateInstr*> taken, deferred;
-    uint64_t blockedX = 0, blockedAll = 0;
-    for (const GateInstr* g : remaining) {
-      bool diag = gk_is_diagonal(g->kind);
-      uint64_t tb = 1ull << g->target;
-      uint64_t Xg = diag ? 0 : tb;
-      uint64_t Ag = g->cmask | tb;
-      bool commutes = !(Xg & blockedAll) && !(Ag & blockedX);
-      bool fits = false;
-      if (commutes) {
-        if ((Xg & ~inQ) == 0) {
-          fits = true;
-        } else if (nQ + 1 <= K) {
-          inQ |= Xg;
-          nQ += 1;
-          fits = true;
+    {
+      uint64_t blockedX = 0, blockedAll = 0;
+      for (const GateInstr* g : remaining) {
+        const uint64_t tb = 1ull << g->target;
+        const uint64_t Xg = gk_is_diagonal(g->kind) ? 0 : tb;
+        const uint64_t Ag = g->cmask | tb;
+        bool fits = false;
+        if (!(Xg & blockedAll) && !(Ag & blockedX)) {
+          if ((Xg & ~inQ) == 0) {
+            fits = true;
+          } else if (nQ + 1 <= K) {
+            inQ |= Xg;
+            nQ += 1;
+            fits = true;
+          }
+        }
+        if (!fits) {
+          blockedX |= Xg;
+          blockedAll |= Ag;
         }
       }
-      if (fits) {
-        taken.push_back(g);
-      } else {
-        deferred.push_back(g);
-        blockedX |= Xg;
-        blockedAll |= Ag;
+    }
+    if (nQ == K && K < n) {
+      uint64_t targets = 0;
+      for (const GateInstr* g : remaining)
+        if (!gk_is_diagonal(g->kind)) targets |= 1ull << g->target;
+      double best = pass_work(remaining, inQ);
+      for (int round = 0; round < 8; ++round) {
+        uint64_t best_set = inQ;
+        for (int a = 0; a < n; ++a) {
+          if (!((inQ >> a) & 1) || ((low >> a) & 1)) continue;
+          for (int b = 0; b < n; ++b) {
+            if (((inQ >> b) & 1) || !((targets >> b) & 1)) continue;
+            const uint64_t cand = (inQ & ~(1ull << a)) | (1ull << b);
+            const double w = pass_work(remaining, cand);
+            if (w > best + 1e-9) {
+              best = w;
+              best_set = cand;
+            }
+          }
+        }
+        if (best_set == inQ) break;
+        inQ = best_set;
+      }
+    }
+    std::vector<const GateInstr*> taken, deferred;
+    {
+      uint64_t blockedX = 0, blockedAll = 0;
+      for (const GateInstr* g : remaining) {
+        const uint64_t tb = 1ull << g->target;
+        const uint64_t Xg = gk_is_diagonal(g->kind) ? 0 : tb;
+        const uint64_t Ag = g->cmask | tb;
+        if (!(Xg & blockedAll) && !(Ag & blockedX) && !(Xg & ~inQ)) {
+          taken.push_back(g);
+        } else {
+          deferred.push_back(g);
+          blockedX |= Xg;
+          blockedAll |= Ag;
+        }
       }
     }
     if (taken.empty()) fail(BF_EINVAL, "internal: tile planner made no progress (K=%d, n=%d)", K, n);
