@@ -44,7 +44,7 @@ enum {
   BF_EINVAL = -1,        /* invalid argument / circuit fails validation   */
   BF_ENOMEM = -2,        /* device or pinned allocation failed            */
   BF_ECUDA = -3,         /* CUDA runtime error (message has the details)  */
-  BF_EUNSUPPORTED = -4,  /* valid request this build does not handle      */
+  BF_EUNSUPPORTED = -4,  /* valid request the library does not handle   */
   BF_ETIMEDOUT = -5,     /* bounded wait expired (serving loop)           */
   BF_EBUSY = -6          /* admission refused: not enough free HBM/slots  */
 };
