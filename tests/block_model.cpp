@@ -1,0 +1,199 @@
+// block_model.cpp — a host functional model of the tensor-core block passes,
+// for the CPU tests (tests/test_block_model.py).
+//
+// It plans a circuit exactly as the engine does (the library's own
+// lower_gate, plan_gates and plan_blocks), then executes every block pass the
+// way the kernels move data: the load-phase destination table fills the
+// operand slots, each block multiplies the operand rows by its matrix decoded
+// from the matrix image (variant chosen by the tile's outside bits), the
+// block's destination table scatters the results into the next block's
+// operand slots or, after the last block, into the staging slots, and the
+// staged tile is stored.  Arithmetic is complex FP64 on the decoded matrices,
+// so the result checks the planner's grouping, orders, images and tables
+// against the oracle without a GPU.  Passes that are not planned as blocks
+// and single-gate steps are applied gate by gate.
+//
+//   block_model <digits|tf32> <ops file (binary op list)> <state in> <state out>
+//
+// The state files hold 2^n interleaved complex128 values.
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <iterator>
+#include <vector>
+
+#include "../code_mojo_gb300/csrc/bf_internal.h"
+
+using namespace bf;
+using cd = std::complex<double>;
+
+static uint64_t insert_zero(uint64_t x, int pos) {
+  const uint64_t m = (1ull << pos) - 1;
+  return ((x & ~m) << 1) | (x & m);
+}
+
+// one 2x2 gate (controls all 1) on the global state
+static void apply_gate(std::vector<cd>& s, int n, int target, uint64_t cmask, const double* m) {
+  const cd m00(m[0], m[1]), m01(m[2], m[3]), m10(m[4], m[5]), m11(m[6], m[7]);
+  const uint64_t half = 1ull << (n - 1);
+  for (uint64_t p = 0; p < half; ++p) {
+    const uint64_t i0 = insert_zero(p, target), i1 = i0 | (1ull << target);
+    if ((i0 & cmask) != cmask) continue;
+    const cd a = s[i0], b = s[i1];
+    s[i0] = m00 * a + m01 * b;
+    s[i1] = m10 * a + m11 * b;
+  }
+}
+
+static void apply_tile_op(std::vector<cd>& s, int n, const TilePass& tp, const TileOp& t) {
+  uint64_t cm = t.cmask_out;
+  for (int j = 0; j < tp.K; ++j)
+    if ((t.cmask_loc >> j) & 1u) cm |= 1ull << tp.q[j];
+  if (t.tloc >= 0) {
+    apply_gate(s, n, tp.q[t.tloc], cm, t.m);
+    return;
+  }
+  // diagonal gate whose target lies outside the tile
+  const cd e0(t.m[0], t.m[1]), e1(t.m[6], t.m[7]);
+  for (uint64_t i = 0; i < s.size(); ++i)
+    if ((i & cm) == cm) s[i] *= ((i >> t.tglob) & 1) ? e1 : e0;
+}
+
+// the 32x32 matrix u[j][l] of one image
+static void decode_image(const unsigned char* img, bool digits, cd* u) {
+  for (int n = 0; n < 64; ++n)
+    for (int k = 0; k < 64; k += 2) {  // c = 0: R^T[n][2l] = (Re u[j][l], Im u[j][l]) for d = 0, 1
+      double v;
+      if (digits) {
+        const size_t off = (size_t)n * 128 + (size_t)((((2 * k) >> 4) ^ (n & 7)) << 4) + (size_t)((2 * k) & 15);
+        long long V = 0;
+        for (int p = 0; p < kDigits; ++p) {
+          uint16_t h;
+          std::memcpy(&h, img + (size_t)p * 8192 + off, 2);
+          const uint32_t bits = (uint32_t)h << 16;
+          float f;
+          std::memcpy(&f, &bits, 4);
+          V = V * 256 + (long long)f;
+        }
+        v = std::ldexp((double)V, -48);
+      } else {
+        const size_t off = (size_t)(k >> 5) * 8192 + (size_t)n * 128 + (size_t)((((k & 31) >> 2) ^ (n & 7)) << 4) +
+                           (size_t)((k & 3) << 2);
+        float big, small;
+        std::memcpy(&big, img + off, 4);
+        std::memcpy(&small, img + 16384 + off, 4);
+        v = (double)big + (double)small;
+      }
+      const int j = n >> 1, l = k >> 1;
+      if ((n & 1) == 0) u[j * 32 + l].real(v);
+      else u[j * 32 + l].imag(v);
+    }
+}
+
+static void run_block_pass(std::vector<cd>& s, int n, const TilePass& tp, const std::vector<Blk5>& blocks,
+                           const std::vector<unsigned char>& images, const std::vector<uint16_t>& offsets,
+                           bool digits) {
+  const int T = digits ? kDigitThreads : kBlockThreads, E = kBlockTableEntries / T;
+  const uint32_t image_bytes = digits ? kDigitImageBytes : kBlockImageBytes;
+  // operand slot <-> (row g, complex column j)
+  std::vector<int> g_of(4096), j_of(4096);
+  for (uint32_t g = 0; g < 128; ++g)
+    for (uint32_t j = 0; j < 32; ++j) {
+      const uint32_t slot = digits ? digit_operand_offset(g, j) >> 2 : block_operand_offset(g, j) >> 3;
+      g_of[slot] = (int)g;
+      j_of[slot] = (int)j;
+    }
+  uint64_t hoff[128];
+  for (int h = 0; h < 128; ++h) {
+    hoff[h] = 0;
+    for (int j = 0; j < 7; ++j)
+      if ((h >> j) & 1) hoff[h] |= 1ull << tp.q[5 + j];
+  }
+  const uint64_t ntiles = 1ull << (n - kBlockTileQubits);
+  std::vector<cd> opnd(4096), next(4096), u(1024);
+  for (uint64_t tile = 0; tile < ntiles; ++tile) {
+    uint64_t obase = tile;
+    for (int j = 0; j < kBlockTileQubits; ++j) obase = insert_zero(obase, tp.q[j]);
+    auto gi = [&](uint32_t i) { return obase | (i & 31u) | hoff[i >> 5]; };
+    const uint16_t* load = offsets.data() + (size_t)blocks[0].load_offs * kBlockTableEntries;
+    for (int t = 0; t < T; ++t)
+      for (int e = 0; e < E; ++e) {
+        const uint32_t i = (uint32_t)(((e >> 1) * T + t) * 2 + (e & 1));
+        opnd[load[t * E + e]] = s[gi(i)];
+      }
+    for (size_t b = 0; b < blocks.size(); ++b) {
+      const Blk5& bk = blocks[b];
+      uint32_t v = 0;
+      for (int k = 0; k < bk.nout; ++k) v |= (uint32_t)((obase >> bk.outpos[k]) & 1ull) << k;
+      decode_image(images.data() + (size_t)(bk.img + v) * image_bytes, digits, u.data());
+      // rows of the operand: a[g][l]
+      std::vector<cd> a(128 * 32), d(128 * 32);
+      for (int slot = 0; slot < 4096; ++slot) a[g_of[slot] * 32 + j_of[slot]] = opnd[slot];
+      for (int g = 0; g < 128; ++g)
+        for (int j = 0; j < 32; ++j) {
+          cd acc = 0;
+          for (int l = 0; l < 32; ++l) acc += u[j * 32 + l] * a[g * 32 + l];
+          d[g * 32 + j] = acc;
+        }
+      const uint16_t* dest = offsets.data() + (size_t)bk.offs * kBlockTableEntries;
+      for (int t = 0; t < T; ++t)
+        for (int e = 0; e < E; ++e) {
+          const int w = t >> 5, lane = t & 31;
+          const int g = 32 * (w & 3) + lane, j = E * (w >> 2) + e;
+          next[dest[t * E + e]] = d[g * 32 + j];
+        }
+      opnd.swap(next);
+    }
+    // opnd now holds the staging slots
+    for (uint32_t i = 0; i < 4096; ++i) s[gi(i)] = opnd[block_stage_slot(i)];
+  }
+}
+
+int main(int argc, char** argv) {
+  if (argc != 5) {
+    std::fprintf(stderr, "usage: block_model <digits|tf32> <ops> <state in> <state out>\n");
+    return 2;
+  }
+  const bool digits = std::strcmp(argv[1], "digits") == 0;
+  std::ifstream fo(argv[2], std::ios::binary);
+  std::vector<char> blob((std::istreambuf_iterator<char>(fo)), {});
+  bf_oplist* list = nullptr;
+  if (bf_ops_deserialize(blob.data(), blob.size(), &list) != BF_OK) return 3;
+  const bf_op* ops;
+  int64_t nops;
+  int32_t n;
+  bf_oplist_view(list, &ops, &nops, &n);
+  std::vector<cd> s((size_t)1 << n);
+  std::ifstream fi(argv[3], std::ios::binary);
+  fi.read(reinterpret_cast<char*>(s.data()), (std::streamsize)(s.size() * sizeof(cd)));
+  std::vector<GateInstr> gates;
+  for (int64_t i = 0; i < nops; ++i) {
+    if (ops[i].kind != BF_OP_GATE) return 4;  // the model covers gate circuits
+    gates.push_back(lower_gate(ops[i], BF_SPEC_ALL));
+  }
+  int block_passes = 0, tile_passes = 0, gate_steps = 0;
+  for (const PlanStep& ps : plan_gates(n, gates, kBlockTileQubits)) {
+    if (!ps.is_tile) {
+      apply_gate(s, n, ps.gate.target, ps.gate.cmask, ps.gate.m);
+      ++gate_steps;
+      continue;
+    }
+    std::vector<Blk5> blocks;
+    std::vector<unsigned char> images;
+    std::vector<uint16_t> offsets;
+    if (ps.tile.K == kBlockTileQubits && ps.tile.L == kTileLowQubits &&
+        plan_blocks(ps.tile, blocks, images, offsets, digits ? BLOCK_DIGITS : BLOCK_TF32)) {
+      run_block_pass(s, n, ps.tile, blocks, images, offsets, digits);
+      ++block_passes;
+    } else {
+      for (const TileOp& t : ps.tile.ops) apply_tile_op(s, n, ps.tile, t);
+      ++tile_passes;
+    }
+  }
+  std::ofstream fw(argv[4], std::ios::binary);
+  fw.write(reinterpret_cast<const char*>(s.data()), (std::streamsize)(s.size() * sizeof(cd)));
+  std::printf("%d %d %d\n", block_passes, tile_passes, gate_steps);
+  return 0;
+}

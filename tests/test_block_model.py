@@ -1,0 +1,93 @@
+"""The tensor-core block passes, planned by the library and executed by a host
+functional model of the kernels' data movement (tests/block_model.cpp: the
+destination tables, the matrix images with their variants, the staging
+slots), compared with the oracle.  CPU only: it checks the planner's grouping,
+column and row orders, images and tables for both operand formats."""
+from __future__ import annotations
+
+import shutil
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from code_mojo_gb300 import butterfly as bfy
+from code_mojo_gb300 import workloads as W
+from oracle import pyoracle as O
+
+ROOT = Path(__file__).resolve().parent.parent
+CUDA_INC = Path("/usr/local/cuda/include")
+
+
+@pytest.fixture(scope="module")
+def model(tmp_path_factory):
+    if shutil.which("g++") is None or not CUDA_INC.exists():
+        pytest.skip("needs g++ and the CUDA headers")
+    from code_mojo_gb300 import build
+    lib = build.build_engine()
+    exe = tmp_path_factory.mktemp("block_model") / "block_model"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I", str(CUDA_INC), "-I", str(ROOT / "include"),
+                    str(ROOT / "tests" / "block_model.cpp"), "-o", str(exe), "-L", str(lib.parent), "-lbfgpu",
+                    f"-Wl,-rpath,{lib.parent}"], check=True, capture_output=True)
+    return exe
+
+
+def run_model(exe, fmt, qc, re, im, tmp_path):
+    ops, sin, sout = tmp_path / "ops.bin", tmp_path / "in.bin", tmp_path / "out.bin"
+    ops.write_bytes(bfy.serialize(qc))
+    (re + 1j * im).astype(np.complex128).tofile(sin)
+    r = subprocess.run([str(exe), fmt, str(ops), str(sin), str(sout)], check=True, capture_output=True, text=True)
+    block_passes, tile_passes, gate_steps = (int(x) for x in r.stdout.split())
+    return np.fromfile(sout, dtype=np.complex128), block_passes
+
+
+def random_controlled_circuit(n, count, seed):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    qc = bfy.QuantumCircuit(n)
+    for _ in range(count):
+        kind = int(rng.integers(0, 5))
+        qs = [int(x) for x in rng.permutation(n)[:3]]
+        a = float(rng.uniform(0, 2 * np.pi))
+        if kind == 0:
+            qc.cx(qs[0], qs[1])
+        elif kind == 1:
+            qc.ccx(qs[0], qs[1], qs[2])
+        elif kind == 2:
+            qc.cp(qs[0], qs[1], a)
+        elif kind == 3:
+            qc.cry(qs[0], qs[1], a)
+        else:
+            qc.u3(qs[0], a, float(rng.uniform(0, 6)), float(rng.uniform(0, 6)))
+    return qc
+
+
+def gates_only(qc):
+    """The circuit without its permutations (the model covers gate circuits)."""
+    out = bfy.QuantumCircuit(qc.num_qubits)
+    out.transformations = [t for t in qc.transformations if isinstance(t, bfy.GateTransformation)]
+    return out
+
+
+CIRCUITS = {
+    "layered13": lambda: W.random_layered_circuit(13, 10, seed=1),
+    "layered14": lambda: W.random_layered_circuit(14, 16, seed=2),
+    "controlled14": lambda: random_controlled_circuit(14, 160, 3),
+    "layered16x40": lambda: W.random_layered_circuit(16, 40, seed=4),
+    "qft13": lambda: gates_only(W.qft_circuit(13)),
+}
+
+
+@pytest.mark.parametrize("fmt", ["digits", "tf32"])
+@pytest.mark.parametrize("name", list(CIRCUITS))
+def test_block_passes_match_the_oracle(model, fmt, name, tmp_path):
+    qc = CIRCUITS[name]()
+    n = qc.num_qubits
+    re, im = W.random_normal_state(n, 7)
+    got, block_passes = run_model(model, fmt, qc, re, im, tmp_path)
+    r, i = O.run(qc, re, im)
+    err = float(np.max(np.abs(got - (r + 1j * i))))
+    if name != "qft13":
+        assert block_passes > 0
+    # digit images hold the matrices to 48 bits; TF32 hi + lo parts to about 2^-22
+    assert err <= (1e-12 if fmt == "digits" else 1e-5), err
