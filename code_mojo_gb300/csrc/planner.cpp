@@ -246,7 +246,72 @@ static double pass_work(const std::vector<const GateInstr*>& remaining, uint64_t
   return w;
 }
 
-std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int K, bool allow_single) {
+// The tensor-core blocks a pass over inQ would need: its gates grouped into
+// blocks of at most 5 tile qubits and 3 outside qubits, each gate into the
+// earliest block at or after the last one that shares a tile qubit with it
+// (the grouping of plan_blocks); large when a gate cannot be placed.
+static int pass_blocks(const std::vector<const GateInstr*>& remaining, uint64_t inQ) {
+  uint64_t blockedX = 0, blockedAll = 0;
+  uint64_t bq[64], bo[64];
+  int nb = 0;
+  for (const GateInstr* g : remaining) {
+    const uint64_t tb = 1ull << g->target;
+    const uint64_t Xg = gk_is_diagonal(g->kind) ? 0 : tb;
+    const uint64_t Ag = g->cmask | tb;
+    if ((Xg & blockedAll) || (Ag & blockedX) || (Xg & ~inQ)) {
+      blockedX |= Xg;
+      blockedAll |= Ag;
+      continue;
+    }
+    const uint64_t Q = Ag & inQ, O = Ag & ~inQ;
+    if (__builtin_popcountll(Q) > 5 || __builtin_popcountll(O) > 3) return 1000;
+    int last = -1;
+    for (int b = 0; b < nb; ++b)
+      if (bq[b] & Q) last = b;
+    int place = -1;
+    for (int b = std::max(last, 0); b < nb; ++b)
+      if (__builtin_popcountll(bq[b] | Q) <= 5 && __builtin_popcountll(bo[b] | O) <= 3) {
+        place = b;
+        break;
+      }
+    if (place < 0) {
+      if (nb == 64) return 1000;
+      bq[nb] = 0;
+      bo[nb] = 0;
+      place = nb++;
+    }
+    bq[place] |= Q;
+    bo[place] |= O;
+  }
+  return nb;
+}
+
+// The CUDA-core tile kernel's cost of the gates a pass over inQ takes, in
+// dense-gate units (dense 1, exchange 0.5, phase 0.4, other diagonal 0.6, a
+// diagonal gate on an outside target 0.4).
+static double pass_core_units(const std::vector<const GateInstr*>& remaining, uint64_t inQ) {
+  uint64_t blockedX = 0, blockedAll = 0;
+  double u = 0;
+  for (const GateInstr* g : remaining) {
+    const uint64_t tb = 1ull << g->target;
+    const uint64_t Xg = gk_is_diagonal(g->kind) ? 0 : tb;
+    const uint64_t Ag = g->cmask | tb;
+    if ((Xg & blockedAll) || (Ag & blockedX) || (Xg & ~inQ)) {
+      blockedX |= Xg;
+      blockedAll |= Ag;
+      continue;
+    }
+    if (!(tb & inQ)) u += 0.4;
+    else if (g->kind == GK_SWAP) u += 0.5;
+    else if (g->kind == GK_PHASE) u += 0.4;
+    else if (g->kind == GK_DIAG) u += 0.6;
+    else u += 1.0;
+  }
+  return u;
+}
+
+std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int K, bool allow_single,
+                                 double block_units) {
   std::vector<PlanStep> steps;
   if (gates.empty()) return steps;
   K = std::max(1, std::min(K, std::min(n, kMaxTileQubits)));
@@ -259,7 +324,9 @@ std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int
   while (!remaining.empty()) {
     // the tile's qubits: first the targets in order of appearance among the
     // gates that could still join (first come), then single swaps of a chosen
-    // qubit for another target while that lets the pass take more work
+    // qubit for another target while that improves the pass: more work, or
+    // for passes that run as tensor-core blocks more work per unit of time
+    // (a pass costs about as much as 2.5 blocks besides its blocks)
     uint64_t inQ = low;
     int nQ = L;
     {
@@ -288,24 +355,49 @@ std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int
       uint64_t targets = 0;
       for (const GateInstr* g : remaining)
         if (!gk_is_diagonal(g->kind)) targets |= 1ull << g->target;
-      double best = pass_work(remaining, inQ);
-      for (int round = 0; round < 8; ++round) {
-        uint64_t best_set = inQ;
-        for (int a = 0; a < n; ++a) {
-          if (!((inQ >> a) & 1) || ((low >> a) & 1)) continue;
-          for (int b = 0; b < n; ++b) {
-            if (((inQ >> b) & 1) || !((targets >> b) & 1)) continue;
-            const uint64_t cand = (inQ & ~(1ull << a)) | (1ull << b);
-            const double w = pass_work(remaining, cand);
-            if (w > best + 1e-9) {
-              best = w;
-              best_set = cand;
+      auto search = [&](uint64_t start, auto score) {
+        uint64_t set = start;
+        double best = score(set);
+        for (int round = 0; round < 8; ++round) {
+          uint64_t best_set = set;
+          for (int a = 0; a < n; ++a) {
+            if (!((set >> a) & 1) || ((low >> a) & 1)) continue;
+            for (int b = 0; b < n; ++b) {
+              if (((set >> b) & 1) || !((targets >> b) & 1)) continue;
+              const uint64_t cand = (set & ~(1ull << a)) | (1ull << b);
+              const double w = score(cand);
+              if (w > best + 1e-9) {
+                best = w;
+                best_set = cand;
+              }
             }
           }
+          if (best_set == set) break;
+          set = best_set;
         }
-        if (best_set == inQ) break;
-        inQ = best_set;
+        return set;
+      };
+      auto work = [&](uint64_t set) { return pass_work(remaining, set); };
+      const uint64_t start = inQ;
+      bool chosen = false;
+      const uint64_t by_work = search(start, work);
+      if (block_units > 0) {
+        // Passes that may run as tensor-core blocks: the tile that takes the
+        // most work per unit of time as blocks (a pass costs about 2.5 blocks
+        // besides its blocks), kept when its blocks beat the CUDA-core kernel
+        // on the same gates and it does more work per unit of time than the
+        // most-work tile does on the CUDA cores (same pass cost; a block
+        // costs block_units dense gates).
+        auto block_rate = [&](uint64_t c) { return work(c) / (2.5 + pass_blocks(remaining, c)); };
+        const uint64_t set = search(start, block_rate);
+        const double core = pass_core_units(remaining, set);
+        const double core_rate = work(by_work) / (2.5 + pass_core_units(remaining, by_work) / block_units);
+        if ((double)pass_blocks(remaining, set) * block_units < core && block_rate(set) >= core_rate) {
+          inQ = set;
+          chosen = true;
+        }
       }
+      if (!chosen) inQ = by_work;
     }
     std::vector<const GateInstr*> taken, deferred;
     {

@@ -174,7 +174,7 @@ int main(int argc, char** argv) {
     gates.push_back(lower_gate(ops[i], BF_SPEC_ALL));
   }
   int block_passes = 0, tile_passes = 0, gate_steps = 0;
-  for (const PlanStep& ps : plan_gates(n, gates, kBlockTileQubits)) {
+  for (const PlanStep& ps : plan_gates(n, gates, kBlockTileQubits, true, digits ? 5.0 : 3.3)) {
     if (!ps.is_tile) {
       apply_gate(s, n, ps.gate.target, ps.gate.cmask, ps.gate.m);
       ++gate_steps;
