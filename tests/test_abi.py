@@ -51,6 +51,7 @@ def test_exec_opts_defaults():
     o = F.bf_exec_opts()
     F.check(F.lib().bf_exec_opts_init(C.byref(o)))
     assert (o.strategy, o.validate, o.specialized, o.tile_qubits, o.sync) == (9, 1, 127, 0, 0)
+    assert o.tensor_blocks == 1 and o.plan_dtype == 0
 
 
 def test_state_create_rejects_bad_arguments_without_device():
@@ -143,6 +144,27 @@ def test_wider_tiles_move_fewer_bytes():
     qc = W.random_layered_circuit(30, 10, 0)
     b = [stats(qc, K=K)["bytes_in_S"] for K in (7, 9, 11, 13)]
     assert b == sorted(b, reverse=True)
+
+
+@pytest.mark.parametrize("dtype,max_passes,max_blocks", [("c128", 52, 130), ("c64", 52, 132)])
+def test_layered_30q_plan_quality(dtype, max_passes, max_blocks):
+    """The planner's tile search on the benchmark circuit: first-come tiles
+    needed 74 passes and 185 blocks; most-work tiles 48 passes and 162 blocks;
+    block-rate tiles about 51 passes and 125 blocks."""
+    ctx = bfy.ExecContext()
+    ctx.execution_strategy = bfy.ExecutionStrategy.GPU_FUSED
+    s = bfy.plan_stats(W.random_layered_circuit(30, 40, 0), ctx, dtype)
+    assert s["tile_passes"] <= max_passes and 0 < s["blocks"] <= max_blocks
+    assert s["block_passes"] >= s["tile_passes"] - 2
+
+
+def test_cuda_core_plan_takes_the_most_work_per_pass():
+    ctx = bfy.ExecContext()
+    ctx.execution_strategy = bfy.ExecutionStrategy.GPU_FUSED
+    ctx.gpu_tensor_blocks = False
+    ctx.gpu_tile_qubits = 12
+    s = bfy.plan_stats(W.random_layered_circuit(30, 40, 0), ctx)
+    assert s["tile_passes"] <= 50 and s["block_passes"] == 0
 
 
 def test_diagonal_gates_never_constrain_tiles():
