@@ -334,8 +334,10 @@ static double cuda_core_units(const TilePass& tp) {
 }
 
 // complex128 digit blocks against the double-float tile kernel: one block
-// costs about this many double-float dense gates (measured on the 30-qubit
-// layered circuit: about 12 ms per block against 2.2 ms per dense gate)
+// costs about this many double-float dense gates (on the 30-qubit layered
+// circuit a digit pass costs about 9 ms plus 8.3 ms per block, a dense gate
+// in a double-float tile pass about 2.4 ms; the charge leaves room for the
+// pass's fixed cost)
 constexpr double kDigitBlockUnits = 5.0;
 
 // True when every op keeps the state's norm (unitary gates and unitaries to
