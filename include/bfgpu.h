@@ -201,6 +201,8 @@ int bf_state_sync(bf_state* st);
 int bf_state_stream(bf_state* st, void** stream);
 
 /* ---- execution (execute, butterfly/core/executors.mojo:723-730) ---------- */
+/* Plans are cached per state (the last four, keyed by the exact op list with
+ * its data and the options that shape a plan). */
 int bf_execute(bf_state* st, const bf_op* ops, int64_t nops,
                const bf_exec_opts* opts);
 
