@@ -110,6 +110,13 @@ double parse_angle(const std::string& expr, const std::string& line) {
   return parse_number(s, line);
 }
 
+// an integer in [lo, hi] (checked before any conversion to int)
+int parse_int(const std::string& t, const std::string& line, int lo, int hi) {
+  const double v = parse_number(t, line);
+  if (!(v >= lo && v <= hi) || v != std::floor(v)) fail(BF_EINVAL, "Integer out of range in QASM: %s", line.c_str());
+  return (int)v;
+}
+
 // "q[3]" (optionally followed by ';' or ',') -> 3
 int parse_qubit(const std::string& token) {
   std::string t = trim(token);
@@ -117,7 +124,7 @@ int parse_qubit(const std::string& token) {
   if (!t.empty() && t.back() == ',') t = trim(t.substr(0, t.size() - 1));
   size_t lb = t.find('['), rb = t.find(']');
   if (lb == std::string::npos || rb == std::string::npos || rb <= lb) fail(BF_EINVAL, "Invalid qubit token: %s", t.c_str());
-  return (int)parse_number(t.substr(lb + 1, rb - lb - 1), t);
+  return parse_int(t.substr(lb + 1, rb - lb - 1), t, 0, 63);
 }
 
 bf_op gate_op(int gate, int target, double arg) {
@@ -148,8 +155,9 @@ OpList* qasm3_parse(const char* text) {
         continue;
       if (s.compare(0, 5, "qubit") == 0) {
         size_t lb = s.find('['), rb = s.find(']');
-        if (lb == std::string::npos || rb == std::string::npos) fail(BF_EINVAL, "Invalid qubit declaration: %s", s.c_str());
-        L->num_qubits = (int)parse_number(s.substr(lb + 1, rb - lb - 1), s);
+        if (lb == std::string::npos || rb == std::string::npos || rb <= lb)
+          fail(BF_EINVAL, "Invalid qubit declaration: %s", s.c_str());
+        L->num_qubits = parse_int(s.substr(lb + 1, rb - lb - 1), s, 1, 64);
         L->ops.clear();
         L->data.clear();
         L->qubits.clear();
@@ -252,6 +260,8 @@ OpList* ops_deserialize(const void* blob, size_t len) {
     take(&ver, 4);
     if (ver != kWireVersion) fail(BF_EINVAL, "op list version %u (expected %u)", ver, kWireVersion);
     take(&L->num_qubits, 4);
+    if (L->num_qubits < 1 || L->num_qubits > 64)
+      fail(BF_EINVAL, "op list qubit count %d is out of range", (int)L->num_qubits);
     take(&res, 4);
     take(&nops, 8);
     if (nops < 0 || (uint64_t)nops > (len - at) / (kFixed + 24)) fail(BF_EINVAL, "op list count %lld is invalid", (long long)nops);

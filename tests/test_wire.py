@@ -178,3 +178,58 @@ def test_serialized_request_serves_like_the_direct_one():
     assert res[a].status == 0 and res[b].status == 0
     assert np.array_equal(res[a].top_index, res[b].top_index)
     assert np.array_equal(res[a].top_prob, res[b].top_prob)
+
+
+def test_random_corruptions_never_crash_the_reader():
+    """Byte flips, truncations and spliced counts in a valid op list: the
+    reader returns an op list or an error, never reads out of bounds (a
+    crash would end this process)."""
+    blob = bytearray(bfy.serialize(circuit_with_everything()))
+    rng = np.random.Generator(np.random.PCG64(17))
+    refused = accepted = 0
+    for trial in range(3000):
+        b = bytearray(blob)
+        kind = trial % 3
+        if kind == 0:
+            for _ in range(int(rng.integers(1, 8))):
+                b[int(rng.integers(0, len(b)))] = int(rng.integers(0, 256))
+        elif kind == 1:
+            b = b[: int(rng.integers(0, len(b)))]
+        else:
+            at = int(rng.integers(8, len(b) - 8))
+            b[at:at + 8] = int(rng.integers(0, 2 ** 63)).to_bytes(8, "little")
+        try:
+            back = bfy.deserialize(bytes(b))
+            accepted += 1
+            assert 1 <= back.num_qubits <= 64
+            back.close()
+        except F.BFError:
+            refused += 1
+    assert refused > 0
+
+
+def test_random_qasm_text_never_crashes_the_parser():
+    """Mutated QASM text: parsed or refused with a message, never a crash."""
+    base = ("OPENQASM 3.0;\ninclude \"stdgates.inc\";\nqubit[5] q;\nh q[0];\nx q[3];\n"
+            "p(pi/4) q[1];\ncp(-pi/8) q[2], q[4];\nh q[4];\n")
+    rng = np.random.Generator(np.random.PCG64(23))
+    alphabet = "qhxpc[](),;/*-+.0123456789pi \n"
+    parsed = 0
+    for trial in range(3000):
+        t = list(base)
+        for _ in range(int(rng.integers(1, 6))):
+            at = int(rng.integers(0, len(t)))
+            op = int(rng.integers(0, 3))
+            if op == 0:
+                t[at] = alphabet[int(rng.integers(0, len(alphabet)))]
+            elif op == 1:
+                del t[at]
+            else:
+                t.insert(at, alphabet[int(rng.integers(0, len(alphabet)))])
+        try:
+            qc = bfy.parse_qasm3_string("".join(t))
+            parsed += 1
+            assert qc.num_qubits >= 1
+        except (F.BFError, ValueError):
+            pass
+    assert parsed > 0
