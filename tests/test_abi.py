@@ -184,3 +184,34 @@ def test_batch_workload_shape():
     # gate transformations only (a batch takes nothing else)
     for c in circs:
         assert all(isinstance(t, bfy.GateTransformation) for t in c.transformations)
+
+
+def test_random_op_records_are_validated_without_crashing():
+    """Random op records (pointers null, counts and fields random): the
+    validator and the host planner return a status, never crash."""
+    rng = np.random.Generator(np.random.PCG64(31))
+    statuses = set()
+    for trial in range(2000):
+        nops = int(rng.integers(1, 6))
+        arr = (F.bf_op * nops)()
+        for o in arr:
+            o.kind = int(rng.integers(-2, 16))
+            o.gate = int(rng.integers(-2, 12))
+            o.target = int(rng.integers(-3, 70))
+            o.target2 = int(rng.integers(-3, 10))
+            o.controls = int(rng.integers(0, 2 ** 63))
+            o.ncontrols = int(rng.integers(-1, 5))
+            o.flags = int(rng.integers(0, 4))
+            o.arg = float(rng.normal())
+            o.nqubits = int(rng.integers(-2, 5))
+            for k in range(8):
+                o.mat[k] = float(rng.normal())
+        n = int(rng.integers(-1, 42))
+        statuses.add(F.lib().bf_validate(n, arr, nops))
+        ctx = F.bf_exec_opts()
+        F.lib().bf_exec_opts_init(C.byref(ctx))
+        t, g, x, bp, nb = (C.c_int64() for _ in range(5))
+        b = C.c_double()
+        statuses.add(F.lib().bf_plan_stats(n, arr, nops, C.byref(ctx), C.byref(t), C.byref(g), C.byref(x),
+                                           C.byref(b), C.byref(bp), C.byref(nb)))
+    assert F.BF_EINVAL in statuses
