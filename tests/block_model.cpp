@@ -13,7 +13,14 @@
 // against the oracle without a GPU.  Passes that are not planned as blocks
 // and single-gate steps are applied gate by gate.
 //
-//   block_model <digits|tf32> <ops file (binary op list)> <state in> <state out>
+// Mode digits-exact follows the complex128 digit kernel's arithmetic step
+// by step instead: the scale from the norm before the first digit pass,
+// each value rounded to six balanced base-256 digits, exact integer level
+// sums of the 26 digit pairs, the carries with round-half-even, and the
+// FP64 result after the last block, so that the model gives the bits the
+// kernel gives.
+//
+//   block_model <digits|digits-exact|tf32> <ops file (binary op list)> <state in> <state out>
 //
 // The state files hold 2^n interleaved complex128 values.
 #include <cmath>
@@ -92,6 +99,132 @@ static void decode_image(const unsigned char* img, bool digits, cd* u) {
     }
 }
 
+// ---- the digit kernel's arithmetic ------------------------------------------
+
+// round(x * 2^sh) (half away from zero on the magnitude) as six balanced
+// base-256 digits, d[5] the lowest
+static void value_digits_of(double x, int sh, int* d) {
+  long long V = (long long)std::llround(std::ldexp(std::fabs(x), sh));
+  if (x < 0) V = -V;
+  for (int j = kDigits - 1; j >= 1; --j) {
+    const long long t = ((V & 255) ^ 128) - 128;
+    d[j] = (int)t;
+    V = (V - t) >> 8;
+  }
+  d[0] = (int)V;
+}
+
+// the six digits e_0..e_5 of every entry of an image's 64x64 real matrix, [n][k]
+static void image_digits(const unsigned char* img, int (*b)[64][64]) {
+  for (int n = 0; n < 64; ++n)
+    for (int k = 0; k < 64; ++k) {
+      const size_t off = (size_t)n * 128 + (size_t)((((2 * k) >> 4) ^ (n & 7)) << 4) + (size_t)((2 * k) & 15);
+      for (int p = 0; p < kDigits; ++p) {
+        uint16_t h;
+        std::memcpy(&h, img + (size_t)p * 8192 + off, 2);
+        const uint32_t bits = (uint32_t)h << 16;
+        float f;
+        std::memcpy(&f, &bits, 4);
+        b[p][n][k] = (int)f;
+      }
+    }
+}
+
+static void run_digit_pass_exact(std::vector<cd>& s, int n, const TilePass& tp, const std::vector<Blk5>& blocks,
+                                 const std::vector<unsigned char>& images, const std::vector<uint16_t>& offsets,
+                                 int e_scale) {
+  const int T = kDigitThreads, E = kBlockTableEntries / T;
+  const int sh = 48 - e_scale;
+  std::vector<int> g_of(4096), j_of(4096);
+  for (uint32_t g = 0; g < 128; ++g)
+    for (uint32_t j = 0; j < 32; ++j) {
+      const uint32_t slot = digit_operand_offset(g, j) >> 2;
+      g_of[slot] = (int)g;
+      j_of[slot] = (int)j;
+    }
+  uint64_t hoff[128];
+  for (int h = 0; h < 128; ++h) {
+    hoff[h] = 0;
+    for (int j = 0; j < 7; ++j)
+      if ((h >> j) & 1) hoff[h] |= 1ull << tp.q[5 + j];
+  }
+  struct Slot { int re[kDigits], im[kDigits]; };
+  std::vector<Slot> opnd(4096), next(4096);
+  std::vector<double> stage_re(4096), stage_im(4096);
+  static int b[kDigits][64][64];
+  std::vector<int> a((size_t)kDigits * 128 * 64);
+  const uint64_t ntiles = 1ull << (n - kBlockTileQubits);
+  for (uint64_t tile = 0; tile < ntiles; ++tile) {
+    uint64_t obase = tile;
+    for (int j = 0; j < kBlockTileQubits; ++j) obase = insert_zero(obase, tp.q[j]);
+    auto gi = [&](uint32_t i) { return obase | (i & 31u) | hoff[i >> 5]; };
+    const uint16_t* load = offsets.data() + (size_t)blocks[0].load_offs * kBlockTableEntries;
+    for (int t = 0; t < T; ++t)
+      for (int e = 0; e < E; ++e) {
+        const uint32_t i = (uint32_t)(((e >> 1) * T + t) * 2 + (e & 1));
+        Slot& sl = opnd[load[t * E + e]];
+        value_digits_of(s[gi(i)].real(), sh, sl.re);
+        value_digits_of(s[gi(i)].imag(), sh, sl.im);
+      }
+    for (size_t bi = 0; bi < blocks.size(); ++bi) {
+      const Blk5& bk = blocks[bi];
+      const bool last = bi + 1 == blocks.size();
+      uint32_t v = 0;
+      for (int k = 0; k < bk.nout; ++k) v |= (uint32_t)((obase >> bk.outpos[k]) & 1ull) << k;
+      image_digits(images.data() + (size_t)(bk.img + v) * kDigitImageBytes, b);
+      for (int slot = 0; slot < 4096; ++slot)
+        for (int i = 0; i < kDigits; ++i) {
+          a[((size_t)i * 128 + g_of[slot]) * 64 + 2 * j_of[slot]] = opnd[slot].re[i];
+          a[((size_t)i * 128 + g_of[slot]) * 64 + 2 * j_of[slot] + 1] = opnd[slot].im[i];
+        }
+      const uint16_t* dest = offsets.data() + (size_t)bk.offs * kBlockTableEntries;
+      for (int t = 0; t < T; ++t)
+        for (int e = 0; e < E; ++e) {
+          const int w = t >> 5, lane = t & 31;
+          const int g = 32 * (w & 3) + lane, jo = E * (w >> 2) + e;
+          int dig[2][kDigits];
+          long long V[2];
+          for (int d = 0; d < 2; ++d) {
+            const int nn = 2 * jo + d;
+            long long D[7];
+            for (int lv = 0; lv < 7; ++lv) {
+              D[lv] = 0;
+              for (int i = 0; i <= lv && i < kDigits; ++i) {
+                const int j = lv - i;
+                if (j >= kDigits) continue;
+                const int* ar = &a[((size_t)i * 128 + g) * 64];
+                for (int k = 0; k < 64; ++k) D[lv] += (long long)ar[k] * b[j][nn][k];
+              }
+            }
+            // carries from the lowest level up, rounding half to even
+            double carry = 0;
+            for (int lv = 6; lv >= 0; --lv) {
+              const double t2 = (double)D[lv] + carry;
+              const double q = std::nearbyint(t2 / 256.0);
+              if (lv + 1 <= kDigits - 1) dig[d][lv + 1] = (int)(t2 - 256.0 * q);
+              carry = q;
+            }
+            dig[d][0] = (int)carry;
+            V[d] = 0;
+            for (int p2 = 0; p2 < kDigits; ++p2) V[d] = V[d] * 256 + dig[d][p2];
+          }
+          const uint16_t to = dest[t * E + e];
+          if (last) {
+            stage_re[to] = std::ldexp((double)V[0], e_scale - 48);
+            stage_im[to] = std::ldexp((double)V[1], e_scale - 48);
+          } else {
+            for (int p2 = 0; p2 < kDigits; ++p2) {
+              next[to].re[p2] = dig[0][p2];
+              next[to].im[p2] = dig[1][p2];
+            }
+          }
+        }
+      if (!last) opnd.swap(next);
+    }
+    for (uint32_t i = 0; i < 4096; ++i) s[gi(i)] = cd(stage_re[block_stage_slot(i)], stage_im[block_stage_slot(i)]);
+  }
+}
+
 static void run_block_pass(std::vector<cd>& s, int n, const TilePass& tp, const std::vector<Blk5>& blocks,
                            const std::vector<unsigned char>& images, const std::vector<uint16_t>& offsets,
                            bool digits) {
@@ -156,7 +289,9 @@ int main(int argc, char** argv) {
     std::fprintf(stderr, "usage: block_model <digits|tf32> <ops> <state in> <state out>\n");
     return 2;
   }
-  const bool digits = std::strcmp(argv[1], "digits") == 0;
+  const bool exact = std::strcmp(argv[1], "digits-exact") == 0;
+  const bool digits = exact || std::strcmp(argv[1], "digits") == 0;
+  int e_scale = 0;  // the digit scale, from the norm before the first digit pass
   std::ifstream fo(argv[2], std::ios::binary);
   std::vector<char> blob((std::istreambuf_iterator<char>(fo)), {});
   bf_oplist* list = nullptr;
@@ -185,7 +320,18 @@ int main(int argc, char** argv) {
     std::vector<uint16_t> offsets;
     if (ps.tile.K == kBlockTileQubits && ps.tile.L == kTileLowQubits &&
         plan_blocks(ps.tile, blocks, images, offsets, digits ? BLOCK_DIGITS : BLOCK_TF32)) {
-      run_block_pass(s, n, ps.tile, blocks, images, offsets, digits);
+      if (exact) {
+        if (e_scale == 0) {
+          double nrm2 = 0;
+          for (const cd& x : s) nrm2 += std::norm(x);
+          int k = 0;
+          std::frexp(std::sqrt(nrm2) * (1.0 + 1e-6), &k);
+          e_scale = nrm2 > 0 ? k + 1 : 1;
+        }
+        run_digit_pass_exact(s, n, ps.tile, blocks, images, offsets, e_scale);
+      } else {
+        run_block_pass(s, n, ps.tile, blocks, images, offsets, digits);
+      }
       ++block_passes;
     } else {
       for (const TileOp& t : ps.tile.ops) apply_tile_op(s, n, ps.tile, t);

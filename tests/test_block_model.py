@@ -2,7 +2,8 @@
 functional model of the kernels' data movement (tests/block_model.cpp: the
 destination tables, the matrix images with their variants, the staging
 slots), compared with the oracle.  CPU only: it checks the planner's grouping,
-column and row orders, images and tables for both operand formats."""
+column and row orders, images and tables for both operand formats, and the
+complex128 digit kernel's arithmetic step by step."""
 from __future__ import annotations
 
 import shutil
@@ -76,6 +77,30 @@ CIRCUITS = {
     "layered16x40": lambda: W.random_layered_circuit(16, 40, seed=4),
     "qft13": lambda: gates_only(W.qft_circuit(13)),
 }
+
+
+@pytest.mark.parametrize("name", ["layered13", "layered14", "controlled14", "qft13"])
+def test_digit_arithmetic_matches_the_oracle(model, name, tmp_path):
+    """The digit kernel's own arithmetic (48-bit fixed point relative to the
+    scale, exact level sums, carries rounding half to even) stays within
+    1e-12 of the oracle and within 5e-13 of the same plan in FP64 (one
+    rounding of at most 2^-49 of the scale per block)."""
+    qc = CIRCUITS[name]()
+    re, im = W.random_normal_state(qc.num_qubits, 7)
+    exact, _ = run_model(model, "digits-exact", qc, re, im, tmp_path)
+    fp64, _ = run_model(model, "digits", qc, re, im, tmp_path)
+    r, i = O.run(qc, re, im)
+    assert float(np.max(np.abs(exact - (r + 1j * i)))) <= 1e-12
+    assert float(np.max(np.abs(exact - fp64))) <= 5e-13
+
+
+def test_digit_arithmetic_scales_with_the_norm(model, tmp_path):
+    """A state of norm 37: the scale follows it, the error stays 1e-12 relative."""
+    qc = CIRCUITS["layered13"]()
+    re, im = W.random_normal_state(13, 9)
+    got, _ = run_model(model, "digits-exact", qc, 37 * re, 37 * im, tmp_path)
+    r, i = O.run(qc, 37 * re, 37 * im)
+    assert float(np.max(np.abs(got - (r + 1j * i)))) <= 37e-12
 
 
 @pytest.mark.parametrize("fmt", ["digits", "tf32"])
