@@ -213,3 +213,38 @@ def test_plan_cache_tells_circuits_apart():
         bfy.execute(st, qc, ctx(True))
         assert np.max(np.abs(st.to_complex() - oracle(qc, re, im))) <= TOL
     st.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("layers,seed", [(8, 0), (12, 1), (16, 0)])
+def test_digit_passes_equal_the_arithmetic_model_bit_for_bit(layers, seed, tmp_path):
+    """The GPU's digit passes give exactly the bits of the host model of the
+    digit arithmetic (tests/block_model.cpp, digits-exact): the same scale,
+    48-bit digits, exact level sums and half-even carries.  The circuits are
+    planned as block passes only, so no double-float pass is involved."""
+    import shutil
+    import subprocess
+    from pathlib import Path
+
+    from code_mojo_gb300 import build
+
+    root = Path(__file__).resolve().parent.parent
+    if shutil.which("g++") is None or not Path("/usr/local/cuda/include").exists():
+        pytest.skip("needs g++ and the CUDA headers")
+    lib = build.build_engine()
+    exe = tmp_path / "block_model"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I", "/usr/local/cuda/include", "-I", str(root / "include"),
+                    str(root / "tests" / "block_model.cpp"), "-o", str(exe), "-L", str(lib.parent), "-lbfgpu",
+                    f"-Wl,-rpath,{lib.parent}"], check=True, capture_output=True)
+    n = 13
+    qc = W.random_layered_circuit(n, layers, seed=seed)
+    plan = bfy.plan_stats(qc, ctx(True))
+    assert plan["block_passes"] == plan["tile_passes"] > 0 and plan["gate_kernels"] == 0
+    re, im = W.random_normal_state(n, 7)
+    (tmp_path / "ops.bin").write_bytes(bfy.serialize(qc))
+    (re + 1j * im).astype(np.complex128).tofile(tmp_path / "in.bin")
+    subprocess.run([str(exe), "digits-exact", str(tmp_path / "ops.bin"), str(tmp_path / "in.bin"),
+                    str(tmp_path / "out.bin")], check=True, capture_output=True)
+    model = np.fromfile(tmp_path / "out.bin", dtype=np.complex128)
+    got = run(qc, re, im)
+    assert np.array_equal(got, model)
