@@ -229,7 +229,7 @@ static TileOp to_tile_op(const GateInstr& g, const int* loc_of) {
 // The work (per-gate bytes, in units of S) a tile pass over the qubit set
 // inQ takes from the remaining gates: a gate joins when its non-diagonal
 // target is in the set and it commutes with every gate deferred before it.
-static double pass_work(const std::vector<const GateInstr*>& remaining, uint64_t inQ) {
+static double pass_work(const std::vector<const GateInstr*>& remaining, uint64_t inQ, uint64_t all) {
   uint64_t blockedX = 0, blockedAll = 0;
   double w = 0;
   for (const GateInstr* g : remaining) {
@@ -241,6 +241,7 @@ static double pass_work(const std::vector<const GateInstr*>& remaining, uint64_t
     } else {
       blockedX |= Xg;
       blockedAll |= Ag;
+      if ((blockedX & all) == all) break;  // every later gate meets a deferred one
     }
   }
   return w;
@@ -250,7 +251,7 @@ static double pass_work(const std::vector<const GateInstr*>& remaining, uint64_t
 // blocks of at most 5 tile qubits and 3 outside qubits, each gate into the
 // earliest block at or after the last one that shares a tile qubit with it
 // (the grouping of plan_blocks); large when a gate cannot be placed.
-static int pass_blocks(const std::vector<const GateInstr*>& remaining, uint64_t inQ) {
+static int pass_blocks(const std::vector<const GateInstr*>& remaining, uint64_t inQ, uint64_t all) {
   uint64_t blockedX = 0, blockedAll = 0;
   uint64_t bq[64], bo[64];
   int nb = 0;
@@ -261,6 +262,7 @@ static int pass_blocks(const std::vector<const GateInstr*>& remaining, uint64_t 
     if ((Xg & blockedAll) || (Ag & blockedX) || (Xg & ~inQ)) {
       blockedX |= Xg;
       blockedAll |= Ag;
+      if ((blockedX & all) == all) break;
       continue;
     }
     const uint64_t Q = Ag & inQ, O = Ag & ~inQ;
@@ -289,7 +291,7 @@ static int pass_blocks(const std::vector<const GateInstr*>& remaining, uint64_t 
 // The CUDA-core tile kernel's cost of the gates a pass over inQ takes, in
 // dense-gate units (dense 1, exchange 0.5, phase 0.4, other diagonal 0.6, a
 // diagonal gate on an outside target 0.4).
-static double pass_core_units(const std::vector<const GateInstr*>& remaining, uint64_t inQ) {
+static double pass_core_units(const std::vector<const GateInstr*>& remaining, uint64_t inQ, uint64_t all) {
   uint64_t blockedX = 0, blockedAll = 0;
   double u = 0;
   for (const GateInstr* g : remaining) {
@@ -299,6 +301,7 @@ static double pass_core_units(const std::vector<const GateInstr*>& remaining, ui
     if ((Xg & blockedAll) || (Ag & blockedX) || (Xg & ~inQ)) {
       blockedX |= Xg;
       blockedAll |= Ag;
+      if ((blockedX & all) == all) break;
       continue;
     }
     if (!(tb & inQ)) u += 0.4;
@@ -329,6 +332,10 @@ std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int
     // (a pass costs about as much as 2.5 blocks besides its blocks)
     uint64_t inQ = low;
     int nQ = L;
+    // the qubits the remaining gates touch: once the deferred gates act
+    // non-diagonally on all of them, no later gate can join a pass
+    uint64_t all = 0;
+    for (const GateInstr* g : remaining) all |= g->cmask | (1ull << g->target);
     {
       uint64_t blockedX = 0, blockedAll = 0;
       for (const GateInstr* g : remaining) {
@@ -348,6 +355,7 @@ std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int
         if (!fits) {
           blockedX |= Xg;
           blockedAll |= Ag;
+          if ((blockedX & all) == all) break;
         }
       }
     }
@@ -377,7 +385,7 @@ std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int
         }
         return set;
       };
-      auto work = [&](uint64_t set) { return pass_work(remaining, set); };
+      auto work = [&](uint64_t set) { return pass_work(remaining, set, all); };
       const uint64_t start = inQ;
       bool chosen = false;
       const uint64_t by_work = search(start, work);
@@ -388,11 +396,11 @@ std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int
         // on the same gates and it does more work per unit of time than the
         // most-work tile does on the CUDA cores (same pass cost; a block
         // costs block_units dense gates).
-        auto block_rate = [&](uint64_t c) { return work(c) / (2.5 + pass_blocks(remaining, c)); };
+        auto block_rate = [&](uint64_t c) { return work(c) / (2.5 + pass_blocks(remaining, c, all)); };
         const uint64_t set = search(start, block_rate);
-        const double core = pass_core_units(remaining, set);
-        const double core_rate = work(by_work) / (2.5 + pass_core_units(remaining, by_work) / block_units);
-        if ((double)pass_blocks(remaining, set) * block_units < core && block_rate(set) >= core_rate) {
+        const double core = pass_core_units(remaining, set, all);
+        const double core_rate = work(by_work) / (2.5 + pass_core_units(remaining, by_work, all) / block_units);
+        if ((double)pass_blocks(remaining, set, all) * block_units < core && block_rate(set) >= core_rate) {
           inQ = set;
           chosen = true;
         }
@@ -402,7 +410,9 @@ std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int
     std::vector<const GateInstr*> taken, deferred;
     {
       uint64_t blockedX = 0, blockedAll = 0;
-      for (const GateInstr* g : remaining) {
+      size_t i = 0;
+      for (; i < remaining.size(); ++i) {
+        const GateInstr* g = remaining[i];
         const uint64_t tb = 1ull << g->target;
         const uint64_t Xg = gk_is_diagonal(g->kind) ? 0 : tb;
         const uint64_t Ag = g->cmask | tb;
@@ -412,8 +422,13 @@ std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int
           deferred.push_back(g);
           blockedX |= Xg;
           blockedAll |= Ag;
+          if ((blockedX & all) == all) {
+            ++i;
+            break;
+          }
         }
       }
+      deferred.insert(deferred.end(), remaining.begin() + (std::ptrdiff_t)i, remaining.end());
     }
     if (taken.empty()) fail(BF_EINVAL, "internal: tile planner made no progress (K=%d, n=%d)", K, n);
     double single_bytes = 0;
