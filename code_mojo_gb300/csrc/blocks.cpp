@@ -9,6 +9,7 @@
 // widened to any 5 qubits of the tile and to gates that are not adjacent in
 // the op list.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <complex>
 #include <cstring>
@@ -58,13 +59,16 @@ void block_image(const double* u, unsigned char* img) {
 // base-256 digits e_1..e_5 in [-128, 127] and the leading e_0 in [-256, 256],
 // from the nearest integer to v * 2^48.
 static void value_digits(double v, int* e) {
-  long long V = std::llround(std::ldexp(v, 48));
-  for (int j = kDigits - 1; j >= 1; --j) {
-    long long d = ((V & 255) ^ 128) - 128;
-    e[j] = (int)d;
-    V = (V - d) >> 8;
-  }
-  e[0] = (int)V;
+  // v * 2^48 is exact and below 2^49 in magnitude, so adding one half is
+  // exact too and truncation rounds halves away from zero (as llround)
+  const double r = v * 281474976710656.0;
+  const long long V = (long long)(r + (r >= 0 ? 0.5 : -0.5));
+  // with W = V + 128 (1 + 2^8 + ... + 2^32) + 512 * 2^40 (nonnegative for
+  // |V| <= 2^49), each of the five low bytes of W is its digit plus 128 (the
+  // added 128s absorb the borrows) and the leading digit is W / 2^40 - 512
+  const unsigned long long W = (unsigned long long)(V + 0x8080808080ll + (512ll << 40));
+  for (int j = kDigits - 1; j >= 1; --j) e[j] = (int)((W >> (8 * (kDigits - 1 - j))) & 255u) - 128;
+  e[0] = (int)(W >> 40) - 512;
 }
 
 static uint16_t bf16_of_int(int d) {  // exact for |d| <= 256
@@ -78,7 +82,12 @@ static uint16_t bf16_of_int(int d) {  // exact for |d| <= 256
 // entry as 6 bf16 digit planes (plane j holds e_j), K-major with the
 // 128-byte swizzle, 8 KiB per plane.
 void block_image_digits(const double* u, unsigned char* img) {
-  std::memset(img, 0, kDigitImageBytes);
+  static const std::array<uint16_t, 513> bf16_of = [] {
+    std::array<uint16_t, 513> t{};
+    for (int d = -256; d <= 256; ++d) t[(size_t)(d + 256)] = bf16_of_int(d);
+    return t;
+  }();
+  uint16_t* planes = reinterpret_cast<uint16_t*>(img);
   for (int n = 0; n < 64; ++n)
     for (int k = 0; k < 64; ++k) {
       const int j = n >> 1, d = n & 1, l = k >> 1, c = k & 1;
@@ -86,11 +95,9 @@ void block_image_digits(const double* u, unsigned char* img) {
       const double v = c == 0 ? (d == 0 ? re : im) : (d == 0 ? -im : re);
       int e[kDigits];
       value_digits(v, e);
-      const size_t off = (size_t)n * 128 + (size_t)((((2 * k) >> 4) ^ (n & 7)) << 4) + (size_t)((2 * k) & 15);
-      for (int p = 0; p < kDigits; ++p) {
-        uint16_t h = bf16_of_int(e[p]);
-        std::memcpy(img + (size_t)p * 8192 + off, &h, 2);
-      }
+      const size_t off = ((size_t)n * 128 + (size_t)((((2 * k) >> 4) ^ (n & 7)) << 4) + (size_t)((2 * k) & 15)) / 2;
+      if (e[0] < -256 || e[0] > 256) fail(BF_EINVAL, "internal: block matrix entry %g outside the digit range", v);
+      for (int p = 0; p < kDigits; ++p) planes[(size_t)p * 4096 + off] = bf16_of[(size_t)(e[p] + 256)];
     }
 }
 
@@ -314,15 +321,26 @@ bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsi
         flat[2 * i + 1] = U[i].imag();
       }
       if (format == BLOCK_DIGITS) {
-        // the digit form is exact only for entries of modulus <= 1: unitary blocks
-        double worst = 0;
-        for (int r = 0; r < 32; ++r)
-          for (int c = 0; c < 32; ++c) {
-            cd acc(0.0, 0.0);
-            for (int k = 0; k < 32; ++k) acc += std::conj(U[k * 32 + r]) * U[k * 32 + c];
-            worst = std::max(worst, std::abs(acc - (r == c ? cd(1.0, 0.0) : cd(0.0, 0.0))));
+        // the digit form is exact only for entries of modulus <= 1: unitary
+        // blocks (U^H U = I to 1e-12; columns as contiguous re / im vectors)
+        double cre[32][32], cim[32][32];
+        for (int k = 0; k < 32; ++k)
+          for (int r = 0; r < 32; ++r) {
+            cre[r][k] = U[k * 32 + r].real();
+            cim[r][k] = U[k * 32 + r].imag();
           }
-        if (worst > 1e-12) return false;
+        double worst2 = 0;
+        for (int r = 0; r < 32; ++r)
+          for (int c = r; c < 32; ++c) {
+            double ar = 0, ai = 0;
+            for (int k = 0; k < 32; ++k) {
+              ar += cre[r][k] * cre[c][k] + cim[r][k] * cim[c][k];
+              ai += cre[r][k] * cim[c][k] - cim[r][k] * cre[c][k];
+            }
+            if (r == c) ar -= 1.0;
+            worst2 = std::max(worst2, ar * ar + ai * ai);
+          }
+        if (worst2 > 1e-24) return false;
       }
       size_t at = images.size();
       images.resize(at + image_bytes);
@@ -332,7 +350,24 @@ bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsi
     blocks.push_back(d);
   }
 
-  // destination tables: u16 per (thread, amplitude) of the format's kernel
+  // destination tables: u16 per (thread, amplitude) of the format's kernel;
+  // the index maps of every block as lookup tables (tile element -> row
+  // and column, and back)
+  struct MapLut {
+    uint16_t g_of[4096], j_of[4096];
+    uint16_t from_g[128], from_j[32];
+  };
+  std::vector<MapLut> lut(maps.size());
+  for (size_t k = 0; k < maps.size(); ++k) {
+    for (uint32_t i = 0; i < 4096; ++i) {
+      uint32_t g, j;
+      maps[k].ext(i, g, j);
+      lut[k].g_of[i] = (uint16_t)g;
+      lut[k].j_of[i] = (uint16_t)j;
+    }
+    for (uint32_t g = 0; g < 128; ++g) lut[k].from_g[g] = (uint16_t)maps[k].dep_g(g);
+    for (uint32_t j = 0; j < 32; ++j) lut[k].from_j[j] = (uint16_t)maps[k].dep_j(j);
+  }
   const int T = format == BLOCK_DIGITS ? kDigitThreads : kBlockThreads;
   const int E = kBlockTableEntries / T;
   const size_t table = (size_t)kBlockTableEntries;
@@ -346,9 +381,8 @@ bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsi
     blocks[first].load_offs = (uint32_t)(at / table);
     for (int t = 0; t < T; ++t)
       for (int e = 0; e < E; ++e) {
-        uint32_t i = (uint32_t)(((e >> 1) * T + t) * 2 + (e & 1)), g, j;
-        maps[0].ext(i, g, j);
-        offsets[at + (size_t)t * E + e] = dest(g, j);
+        const uint32_t i = (uint32_t)(((e >> 1) * T + t) * 2 + (e & 1));
+        offsets[at + (size_t)t * E + e] = dest(lut[0].g_of[i], lut[0].j_of[i]);
       }
   }
   for (size_t k = 0; k < maps.size(); ++k) {
@@ -360,12 +394,10 @@ bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsi
       for (int e = 0; e < E; ++e) {
         const uint32_t w = (uint32_t)t >> 5, lane = (uint32_t)t & 31u;
         const uint32_t g = 32u * (w & 3u) + lane, j = (uint32_t)E * (w >> 2) + (uint32_t)e;
-        const uint32_t i = maps[k].dep_g(g) | maps[k].dep_j(j);
+        const uint32_t i = (uint32_t)lut[k].from_g[g] | lut[k].from_j[j];
         uint16_t v;
         if (k + 1 < maps.size()) {
-          uint32_t g2, j2;
-          maps[k + 1].ext(i, g2, j2);
-          v = dest(g2, j2);
+          v = dest(lut[k + 1].g_of[i], lut[k + 1].j_of[i]);
         } else {
           v = (uint16_t)block_stage_slot(i);
         }
