@@ -52,11 +52,21 @@ SEED = 0
 
 
 def per_gate_bytes_in_S(qc) -> float:
-    """Algorithmic bytes of the per-gate path, in units of the state size S."""
+    """Algorithmic bytes of the per-gate path, in units of the state size S,
+    counted from the gates alone (no engine call, so the reference arm never
+    loads the engine): a gate reads and writes every amplitude it must
+    touch, 2S for a dense or exchanging 1-qubit gate and S for P or Z (only
+    the target-1 half changes), each control halving it."""
     from code_mojo_gb300 import butterfly as bfy
-    ctx = bfy.ExecContext()
-    ctx.execution_strategy = bfy.ExecutionStrategy.GPU
-    return bfy.plan_stats(qc, ctx)["bytes_in_S"]
+    total = 0.0
+    for tr in qc.transformations:
+        pair = [tr.first, tr.second] if isinstance(tr, bfy.FusedPairTransformation) else [tr]
+        for g in pair:
+            if not isinstance(g, bfy.GateTransformation):
+                raise ValueError(f"per-gate byte count covers gate transformations only, not {type(g).__name__}")
+            f = 1.0 if g.gate_info.kind in (bfy.GateKind.P, bfy.GateKind.Z) else 2.0
+            total += f / (1 << len(g.controls))
+    return total
 
 
 def measured_tensor_peak(sustained: bool) -> tuple[float, str]:
@@ -231,6 +241,15 @@ def cpu_sample(qc, n: int, gates: int, threads: int, state=None) -> dict:
             "seconds": dt}
 
 
+def workload_config(world: int) -> dict:
+    """The `config` both arms print: the workload, not the engine's settings."""
+    return {"workload": f"random layered circuit, {N_QUBITS} qubits, {LAYERS} layers (U3 on every qubit + CX on a "
+                        f"random perfect matching), complex128, from |0>",
+            "qubits": N_QUBITS, "layers": LAYERS, "seed": SEED, "state_bytes": 16 << N_QUBITS,
+            "metric_basis": "per-gate bytes (dense 1-qubit gate 2S, CX S) per circuit / time",
+            "l2": "state (16 GiB) larger than L2; no flush", "parallelism": f"replicas x{world}"}
+
+
 def run_reference(args) -> None:
     rank, world, local = dist_setup(args.gpus)
     if rank != 0:
@@ -250,10 +269,9 @@ def run_reference(args) -> None:
         "impl": "reference", "metric": METRIC, "value": v, "unit": "GB/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.median([r["seconds"] for r in vals])) * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"random layered circuit, {N_QUBITS} qubits, {LAYERS} layers (U3 + CX matching), "
-                               f"complex128, from |0>; each step a bounded sample: first {args.ref_gates} gates",
-                   "qubits": N_QUBITS, "layers": LAYERS, "seed": SEED},
-        "cpu_baseline": {"value": v, "unit": "GB/s", "cores": threads, "kind": "port", "sample": vals[0]["sample"]},
+        "config": workload_config(args.gpus),
+        "cpu_baseline": {"value": v, "unit": "GB/s", "cores": threads, "kind": "port",
+                         "sample": "each step: " + vals[0]["sample"]},
         "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -305,14 +323,8 @@ def run_batch_bench(count: int, reps: int, sample: int) -> dict:
     import torch
     from code_mojo_gb300 import batch as B
     from code_mojo_gb300 import opsarray as OA
-    rng = np.random.Generator(np.random.PCG64(7))
-    circs = []
-    for i in range(count):
-        n = int(rng.integers(8, 21))
-        if i % 2 == 0:
-            circs.append(OA.random_layered(n, 20, int(rng.integers(0, 2 ** 31))))
-        else:
-            circs.append(OA.value_encoding(n, float(rng.uniform(0, 2 ** n))))
+    circs = OA.batch_mix(count, seed=7)
+    rng = np.random.Generator(np.random.PCG64(8))
     out = {"circuits": count, "qubits": "uniform 8..20", "mix": "half random layered depth 20, half value encoding"}
     batches = {}
     for dtype in ("c64", "c128"):
@@ -436,6 +448,50 @@ def run_precision_bench(n_big: int, n_cmp: int, layers: int) -> dict:
     return out
 
 
+def hbm_figure(plan: dict, n: int, ms_step: float, world: int) -> dict:
+    """The metric's HBM reading of the fused step: the bytes its passes must
+    move (each tile or block pass reads and writes the state once, 2S) over
+    the step time, against the measured copy bandwidth."""
+    S = 16.0 * (1 << n)
+    peak, src = measured_peaks()
+    fused_bytes = plan["bytes_in_S"] * S
+    gbs = fused_bytes * world / (ms_step * 1e-3) / 1e9
+    return {"fused_bytes_per_step": fused_bytes, "passes_per_step": plan["tile_passes"] + plan["gate_kernels"] +
+            plan["other_passes"], "achieved_GBps": gbs, "peak_GBps": peak, "frac_of_peak": gbs / peak / world,
+            "peak_source": f"{src} hbm_gbs", "target_frac": 0.70, "target_met": gbs / peak / world >= 0.70}
+
+
+def summary_of(line: dict) -> dict:
+    """The workloads' headline figures in a few keys."""
+    def g(d, *path):
+        for k in path:
+            if not isinstance(d, dict) or k not in d:
+                return None
+            d = d[k]
+        return d
+
+    out = {"circuit30_ms": line["ms_per_step"], "hbm_frac_fused": g(line, "hbm", "frac_of_peak"),
+           "digit_pass_ms": g(line, "roofline", "avg_launch_ms"), "e2e_ms": g(line, "e2e", "ms_per_step"),
+           "e2e_pageable_ms": g(line, "e2e", "pageable", "ms_per_step"),
+           "e2e_cold_ms": g(line, "e2e", "cold_first_call_ms"),
+           "qft20_ms": g(line, "qft20", "ms_per_circuit")}
+    if line.get("value_encoding"):
+        out["value_encoding_ms"] = {k: v.get("ms") for k, v in line["value_encoding"].get("runs", {}).items()}
+    for dt in ("c64", "c128"):
+        out[f"batch_{dt}_circuits_per_s"] = g(line, "batch", dt, "circuits_per_s")
+    out["batch_max_infidelity"] = g(line, "batch", "max_infidelity_c64_vs_c128")
+    for dt in ("c64", "c128"):
+        sv = g(line, "serving", dt) or {}
+        out[f"serve_{dt}"] = {k: sv.get(k) for k in ("circuits_per_s", "p50_ms", "p99_ms")} if sv else None
+        cap = g(line, "serving", "capacity", dt) or {}
+        out[f"capacity_{dt}"] = {k: cap.get(k) for k in ("circuits_per_s", "p50_ms", "p99_ms")} if cap else None
+    out["precision_infidelity_32q"] = g(line, "precision", "infidelity_vs_complex128", "tensor_cores")
+    out["precision_33q_ms"] = (None if not line.get("precision") else
+                               g(line, "precision", "tensor_cores", "layered_ms") +
+                               g(line, "precision", "tensor_cores", "qft_ms"))
+    return out
+
+
 def autotune_width(st, qc, candidates) -> tuple[int, dict]:
     """Fusion width: times one layer-block of the circuit at each width and
     keeps the fastest per unit of work."""
@@ -510,33 +566,67 @@ def run_ours(args) -> None:
                     "launches_per_circuit": len(qc.transformations),
                     "frac_of_hbm_peak": pg_bytes / (pms * 1e-3) / 1e9 / measured_peaks()[0]}
 
-    # e2e through the public API with host SoA buffers (pinned)
+    # e2e through the public API with host SoA buffers: the upload of the
+    # step's input, the circuit and the download of its result, timed on the
+    # host around each step; page-locked host arrays (the headline), pageable
+    # ones (a Mojo List[Float64] is pageable), and a cold first call on a new
+    # state (plan, program upload and copies) with pageable arrays
     e2e = None
-    if args.e2e_steps > 0:
+    e2e_steps = args.e2e_steps if args.e2e_steps >= 0 else args.steps
+    if e2e_steps > 0:
         N = 1 << n
-        hre = torch.zeros(N, dtype=torch.float64, pin_memory=True)
-        him = torch.zeros(N, dtype=torch.float64, pin_memory=True)
-        hre[0] = 1.0
         lib = __import__("code_mojo_gb300._ffi", fromlist=["lib"])
         L = lib.lib()
         ectx = ctx.copy()
         ectx.gpu_sync = True
 
-        def e2e_step():
-            lib.check(L.bf_state_upload_soa(st.handle, hre.data_ptr(), him.data_ptr()))
-            bfy.execute(st, qc, ectx)
-            lib.check(L.bf_state_download_soa(st.handle, hre.data_ptr(), him.data_ptr()))
+        def e2e_run(state, hre, him, steps):
+            def step():
+                lib.check(L.bf_state_upload_soa(state.handle, hre.ctypes.data, him.ctypes.data))
+                bfy.execute(state, qc, ectx)
+                lib.check(L.bf_state_download_soa(state.handle, hre.ctypes.data, him.ctypes.data))
+            times = []
+            for _ in range(steps):
+                barrier(world)
+                t0 = time.perf_counter()
+                step()
+                times.append(time.perf_counter() - t0)
+            return times
 
-        e2e_step()
-        barrier(world)
-        t0 = time.perf_counter()
-        for _ in range(args.e2e_steps):
-            e2e_step()
-        dt = (time.perf_counter() - t0) / args.e2e_steps
-        dt = barrier_max(dt, world)
+        def host_arrays(pinned):
+            if pinned:
+                t_re = torch.zeros(N, dtype=torch.float64, pin_memory=True)
+                t_im = torch.zeros(N, dtype=torch.float64, pin_memory=True)
+                hre, him = t_re.numpy(), t_im.numpy()
+                keep = (t_re, t_im)
+            else:
+                hre, him = host_state(n)
+                keep = None
+            hre[0] = 1.0
+            return hre, him, keep
+
+        hre, him, keep = host_arrays(True)
+        e2e_run(st, hre, him, 1)  # warm-up
+        times = e2e_run(st, hre, him, e2e_steps)
+        dt = barrier_max(float(np.mean(times)), world)
         e2e = {"value": pg_bytes * world / dt / 1e9, "unit": "GB/s", "h2d_bytes_per_step": 2 * 8 * N,
-               "d2h_bytes_per_step": 2 * 8 * N, "ms_per_step": dt * 1e3}
-        del hre, him
+               "d2h_bytes_per_step": 2 * 8 * N, "ms_per_step": dt * 1e3, "steps": e2e_steps,
+               "host_memory": "page-locked", "ms_min": min(times) * 1e3, "ms_max": max(times) * 1e3}
+        del hre, him, keep
+        if args.e2e_pageable_steps > 0:
+            hre, him, _ = host_arrays(False)
+            ptimes = e2e_run(st, hre, him, args.e2e_pageable_steps)
+            pdt = barrier_max(float(np.mean(ptimes)), world)
+            e2e["pageable"] = {"value": pg_bytes * world / pdt / 1e9, "unit": "GB/s", "ms_per_step": pdt * 1e3,
+                               "steps": args.e2e_pageable_steps, "ms_min": min(ptimes) * 1e3}
+            cold = bfy.QuantumState(n)
+            cold.sync()
+            ctimes = e2e_run(cold, hre, him, 1)
+            cold.close()
+            e2e["cold_first_call_ms"] = ctimes[0] * 1e3
+            e2e["cold_first_call"] = ("a new state's first upload + execute (planning and program upload "
+                                      "included) + download, pageable host arrays; state creation excluded")
+            del hre, him
 
     qft = run_qft_bench(20, 50) if args.qft and rank == 0 else None
     batch = run_batch_bench(args.batch_count, 3, 256) if args.batch_count > 0 else None
@@ -562,11 +652,9 @@ def run_ours(args) -> None:
         "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fixed48+df64" if digits else "df64", "data": "synthetic",
-        "config": {"workload": f"random layered circuit, {n} qubits, {LAYERS} layers (U3 on every qubit + CX on a "
-                               f"random perfect matching), complex128 (FP64 storage; {arith}), from |0>",
-                   "qubits": n, "layers": LAYERS, "seed": SEED, "state_bytes": int(S), "tile_qubits": K,
-                   "tensor_blocks": digits,
-                   "l2": "state (16 GiB) larger than L2; no flush", "parallelism": f"replicas x{world}"},
+        "config": workload_config(world),
+        "engine": {"arithmetic": f"FP64 storage; {arith}", "tile_qubits": K, "tensor_blocks": digits},
+        "hbm": hbm_figure(plan, n, ms_step, world),
         "gate_passes_per_s": len(qc.transformations) * world / (ms_step * 1e-3),
         "circuits_per_s": world / (ms_step * 1e-3),
         "per_gate_bytes_per_circuit": pg_bytes,
@@ -586,6 +674,7 @@ def run_ours(args) -> None:
         "serving": serving,
         "precision": precision,
     }
+    line["summary"] = summary_of(line)  # last, so that a tail of the output keeps it
     print(json.dumps(line), flush=True)
     st.close()
 
@@ -600,9 +689,10 @@ def main():
     ap.add_argument("--no-tensor-blocks", action="store_true",
                     help="CUDA-core tile passes only (double-float complex128)")
     ap.add_argument("--per-gate-steps", type=int, default=1)
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=-1, help="-1: as many as --steps")
+    ap.add_argument("--e2e-pageable-steps", type=int, default=2)
     ap.add_argument("--cpu-gates", type=int, default=45)
-    ap.add_argument("--ref-gates", type=int, default=15)
+    ap.add_argument("--ref-gates", type=int, default=45, help="gates per reference-arm step (45: one whole layer)")
     ap.add_argument("--batch-count", type=int, default=4096)
     ap.add_argument("--qft", type=int, default=1, help="time the 20-qubit QFT workload (0: skip)")
     ap.add_argument("--serve-seconds", type=float, default=10.0)

@@ -788,6 +788,12 @@ void release_state_members(State& st) {
   if (st.scratch) cudaFree(st.scratch);
   if (st.h_prog) cudaFreeHost(st.h_prog);
   if (st.d_stage) cudaFree(st.d_stage);
+  for (int k = 0; k < 2; ++k) {
+    if (st.stage_copied[k]) cudaEventDestroy(st.stage_copied[k]);
+    if (st.stage_done[k]) cudaEventDestroy(st.stage_done[k]);
+  }
+  if (st.stage_start) cudaEventDestroy(st.stage_start);
+  if (st.copy_stream) cudaStreamDestroy(st.copy_stream);
   if (st.h_partial) cudaFreeHost(st.h_partial);
   if (st.h_flag) cudaFreeHost(st.h_flag);
   if (st.h_aux) cudaFreeHost(st.h_aux);
@@ -806,11 +812,25 @@ static void free_state(State* st) {
   delete st;
 }
 
-static constexpr uint64_t kStageElems = 1ull << 23;  // 8 Mi amplitudes per chunk
+// Boundary copies move the host SoA arrays in chunks of kStageElems
+// amplitudes through two device staging buffers (re and im of one chunk
+// each): the copy of chunk k+1 on the copy stream runs while the conversion
+// kernel of chunk k runs on the state's stream.
+static constexpr uint64_t kStageElems = 1ull << 22;  // 4 Mi amplitudes (64 MiB of re + im) per chunk
 
 static void ensure_stage(State& st) {
-  size_t want = (size_t)std::min<uint64_t>(st.N, kStageElems) * 2 * sizeof(double);
+  const size_t want = (size_t)std::min<uint64_t>(st.N, kStageElems) * 2 * sizeof(double) * 2;
+  if (!st.copy_stream) {
+    BF_CUDA(cudaStreamCreateWithFlags(&st.copy_stream, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; ++k) {
+      BF_CUDA(cudaEventCreateWithFlags(&st.stage_copied[k], cudaEventDisableTiming));
+      BF_CUDA(cudaEventCreateWithFlags(&st.stage_done[k], cudaEventDisableTiming));
+    }
+    BF_CUDA(cudaEventCreateWithFlags(&st.stage_start, cudaEventDisableTiming));
+  }
   if (st.stage_bytes >= want) return;
+  BF_CUDA(cudaStreamSynchronize(st.stream));
+  BF_CUDA(cudaStreamSynchronize(st.copy_stream));
   if (st.d_stage) cudaFree(st.d_stage);
   st.d_stage = nullptr;
   st.stage_bytes = 0;
@@ -819,6 +839,74 @@ static void ensure_stage(State& st) {
     fail(BF_ENOMEM, "cannot allocate %zu bytes of boundary staging", want);
   }
   st.stage_bytes = want;
+}
+
+// re and im halves of staging buffer k
+static double* stage_re(State& st, int k) {
+  const uint64_t chunk = std::min<uint64_t>(st.N, kStageElems);
+  return static_cast<double*>(st.d_stage) + (size_t)k * 2 * chunk;
+}
+static double* stage_im(State& st, int k) { return stage_re(st, k) + std::min<uint64_t>(st.N, kStageElems); }
+
+// Host SoA -> device.  Returns once every byte of re and im has been copied
+// out of host memory (the conversion kernels may still run, stream-ordered
+// before any later work on the state), so the caller may reuse the arrays.
+static void upload_soa(State& st, const double* re, const double* im) {
+  ensure_stage(st);
+  const uint64_t chunk = std::min<uint64_t>(st.N, kStageElems);
+  // the staging buffers' earlier users are on the state's stream
+  BF_CUDA(cudaEventRecord(st.stage_start, st.stream));
+  BF_CUDA(cudaStreamWaitEvent(st.copy_stream, st.stage_start, 0));
+  int k = 0;
+  for (uint64_t off = 0; off < st.N; off += chunk, k ^= 1) {
+    const uint64_t cnt = std::min(chunk, st.N - off);
+    if (off >= 2 * chunk) BF_CUDA(cudaStreamWaitEvent(st.copy_stream, st.stage_done[k], 0));
+    BF_CUDA(cudaMemcpyAsync(stage_re(st, k), re + off, cnt * sizeof(double), cudaMemcpyHostToDevice,
+                            st.copy_stream));
+    BF_CUDA(cudaMemcpyAsync(stage_im(st, k), im + off, cnt * sizeof(double), cudaMemcpyHostToDevice,
+                            st.copy_stream));
+    BF_CUDA(cudaEventRecord(st.stage_copied[k], st.copy_stream));
+    BF_CUDA(cudaStreamWaitEvent(st.stream, st.stage_copied[k], 0));
+    launch_interleave(st, stage_re(st, k), stage_im(st, k), off, cnt);
+    BF_CUDA(cudaEventRecord(st.stage_done[k], st.stream));
+  }
+  BF_CUDA(cudaStreamSynchronize(st.copy_stream));
+}
+
+// Device amplitudes [offset, offset + count) -> host SoA; blocks until the
+// host arrays hold them.  The conversion of chunk c+1 is queued before the
+// copy of chunk c, because a copy into pageable host memory returns only
+// once it has finished.
+static void download_soa(State& st, uint64_t offset, uint64_t count, double* re, double* im) {
+  if (count == 0) {
+    sync_state(st);
+    return;
+  }
+  ensure_stage(st);
+  const uint64_t chunk = std::min<uint64_t>(st.N, kStageElems);
+  const uint64_t nchunks = (count + chunk - 1) / chunk;
+  BF_CUDA(cudaEventRecord(st.stage_start, st.copy_stream));
+  BF_CUDA(cudaStreamWaitEvent(st.stream, st.stage_start, 0));
+  auto convert = [&](uint64_t c) {
+    const int k = (int)(c & 1);
+    if (c >= 2) BF_CUDA(cudaStreamWaitEvent(st.stream, st.stage_copied[k], 0));
+    launch_deinterleave(st, stage_re(st, k), stage_im(st, k), offset + c * chunk, std::min(chunk, count - c * chunk));
+    BF_CUDA(cudaEventRecord(st.stage_done[k], st.stream));
+  };
+  convert(0);
+  for (uint64_t c = 0; c < nchunks; ++c) {
+    if (c + 1 < nchunks) convert(c + 1);
+    const int k = (int)(c & 1);
+    const uint64_t cnt = std::min(chunk, count - c * chunk);
+    BF_CUDA(cudaStreamWaitEvent(st.copy_stream, st.stage_done[k], 0));
+    BF_CUDA(cudaMemcpyAsync(re + c * chunk, stage_re(st, k), cnt * sizeof(double), cudaMemcpyDeviceToHost,
+                            st.copy_stream));
+    BF_CUDA(cudaMemcpyAsync(im + c * chunk, stage_im(st, k), cnt * sizeof(double), cudaMemcpyDeviceToHost,
+                            st.copy_stream));
+    BF_CUDA(cudaEventRecord(st.stage_copied[k], st.copy_stream));
+  }
+  BF_CUDA(cudaStreamSynchronize(st.copy_stream));
+  sync_state(st);
 }
 
 }  // namespace bf
@@ -888,7 +976,11 @@ int bf_state_create(int32_t n, int32_t dtype, bf_state** out) {
 
 int bf_state_destroy(bf_state* hst) {
   State* st = S_(hst);
-  return guarded([&]() { free_state(st); });
+  return guarded([&]() {
+    if (!st) return;
+    DeviceGuard dg(st->device);
+    free_state(st);
+  });
 }
 
 int bf_state_info(const bf_state* hst, int32_t* n, int32_t* dtype) {
@@ -904,6 +996,7 @@ int bf_state_set_basis(bf_state* hst, uint64_t idx) {
   State* st = S_(hst);
   return guarded([&]() {
     if (!st) fail(BF_EINVAL, "state is null");
+    DeviceGuard dg(st->device);
     if (idx >= st->N) fail(BF_EINVAL, "basis index %llu out of range", (unsigned long long)idx);
     launch_set_basis(*st, idx);
   });
@@ -913,16 +1006,8 @@ int bf_state_upload_soa(bf_state* hst, const double* re, const double* im) {
   State* st = S_(hst);
   return guarded([&]() {
     if (!st || !re || !im) fail(BF_EINVAL, "null argument");
-    ensure_stage(*st);
-    double* d_re = static_cast<double*>(st->d_stage);
-    uint64_t chunk = std::min<uint64_t>(st->N, kStageElems);
-    double* d_im = d_re + chunk;
-    for (uint64_t off = 0; off < st->N; off += chunk) {
-      uint64_t cnt = std::min(chunk, st->N - off);
-      BF_CUDA(cudaMemcpyAsync(d_re, re + off, cnt * sizeof(double), cudaMemcpyHostToDevice, st->stream));
-      BF_CUDA(cudaMemcpyAsync(d_im, im + off, cnt * sizeof(double), cudaMemcpyHostToDevice, st->stream));
-      launch_interleave(*st, d_re, d_im, off, cnt);
-    }
+    DeviceGuard dg(st->device);
+    upload_soa(*st, re, im);
   });
 }
 
@@ -930,18 +1015,9 @@ int bf_state_download_range(bf_state* hst, uint64_t offset, uint64_t count, doub
   State* st = S_(hst);
   return guarded([&]() {
     if (!st || (count && (!re || !im))) fail(BF_EINVAL, "null argument");
+    DeviceGuard dg(st->device);
     if (offset > st->N || count > st->N - offset) fail(BF_EINVAL, "range out of bounds");
-    ensure_stage(*st);
-    double* d_re = static_cast<double*>(st->d_stage);
-    uint64_t chunk = std::min<uint64_t>(st->N, kStageElems);
-    double* d_im = d_re + chunk;
-    for (uint64_t done = 0; done < count; done += chunk) {
-      uint64_t cnt = std::min(chunk, count - done);
-      launch_deinterleave(*st, d_re, d_im, offset + done, cnt);
-      BF_CUDA(cudaMemcpyAsync(re + done, d_re, cnt * sizeof(double), cudaMemcpyDeviceToHost, st->stream));
-      BF_CUDA(cudaMemcpyAsync(im + done, d_im, cnt * sizeof(double), cudaMemcpyDeviceToHost, st->stream));
-    }
-    sync_state(*st);
+    download_soa(*st, offset, count, re, im);
   });
 }
 
@@ -958,6 +1034,7 @@ int bf_state_sync(bf_state* hst) {
   State* st = S_(hst);
   return guarded([&]() {
     if (!st) fail(BF_EINVAL, "state is null");
+    DeviceGuard dg(st->device);
     sync_state(*st);
   });
 }
@@ -991,6 +1068,7 @@ int bf_state_pass_times(bf_state* hst, int64_t* counts, double* ms) {
   State* st = S_(hst);
   return guarded([&]() {
     if (!st || !counts || !ms) fail(BF_EINVAL, "null argument");
+    DeviceGuard dg(st->device);
     for (int c = 0; c < BF_PASS_CLASSES; ++c) {
       counts[c] = 0;
       ms[c] = 0;
@@ -1010,6 +1088,7 @@ int bf_execute(bf_state* hst, const bf_op* ops, int64_t nops, const bf_exec_opts
   State* st = S_(hst);
   return guarded([&]() {
     if (!st) fail(BF_EINVAL, "state is null");
+    DeviceGuard dg(st->device);
     bf_exec_opts o;
     if (opts) o = *opts;
     else bf_exec_opts_init(&o);
@@ -1022,6 +1101,7 @@ int bf_norm2(bf_state* hst, double* out) {
   State* st = S_(hst);
   return guarded([&]() {
     if (!st || !out) fail(BF_EINVAL, "null argument");
+    DeviceGuard dg(st->device);
     *out = reduce_norm2(*st);
   });
 }
@@ -1031,6 +1111,8 @@ int bf_inner(bf_state* ha, bf_state* hb, double* re, double* im) {
   State* b = S_(hb);
   return guarded([&]() {
     if (!a || !b || !re || !im) fail(BF_EINVAL, "null argument");
+    if (a->device != b->device) fail(BF_EINVAL, "the two states live on different devices (%d, %d)", a->device, b->device);
+    DeviceGuard dg(a->device);
     inner_product(*a, *b, re, im);
   });
 }
@@ -1039,6 +1121,7 @@ int bf_probabilities(bf_state* hst, const int32_t* qubits, const int8_t* values,
   State* st = S_(hst);
   return guarded([&]() {
     if (!st || !out) fail(BF_EINVAL, "null argument");
+    DeviceGuard dg(st->device);
     std::vector<double> p;
     marginal_probs(*st, qubits, values, nq, p);
     std::memcpy(out, p.data(), p.size() * sizeof(double));
@@ -1050,6 +1133,7 @@ int bf_measure(bf_state* hst, const int32_t* targets, const int8_t* values, int3
   State* st = S_(hst);
   return guarded([&]() {
     if (!st) fail(BF_EINVAL, "state is null");
+    DeviceGuard dg(st->device);
     measure(*st, targets, values, ntargets, seed, outcome, probability);
   });
 }
@@ -1058,6 +1142,7 @@ int bf_probs_topk(bf_state* hst, int32_t k, uint64_t* indices, double* probs) {
   State* st = S_(hst);
   return guarded([&]() {
     if (!st || !indices || !probs) fail(BF_EINVAL, "null argument");
+    DeviceGuard dg(st->device);
     probs_topk(*st, k, indices, probs);
   });
 }
@@ -1085,6 +1170,7 @@ int bf_batch_create(int32_t ncirc, const int32_t* num_qubits, const bf_op* const
 int bf_batch_run(bf_batch* h, int32_t sync) {
   return guarded([&]() {
     if (!h) fail(BF_EINVAL, "batch is null");
+    DeviceGuard dg(batch_device(*B_(h)));
     batch_run(*B_(h), sync != 0);
   });
 }
@@ -1092,6 +1178,7 @@ int bf_batch_run(bf_batch* h, int32_t sync) {
 int bf_batch_sync(bf_batch* h) {
   return guarded([&]() {
     if (!h) fail(BF_EINVAL, "batch is null");
+    DeviceGuard dg(batch_device(*B_(h)));
     batch_sync(*B_(h));
   });
 }
@@ -1099,6 +1186,7 @@ int bf_batch_sync(bf_batch* h) {
 int bf_batch_download(bf_batch* h, int32_t circuit, double* re, double* im) {
   return guarded([&]() {
     if (!h || !re || !im) fail(BF_EINVAL, "null argument");
+    DeviceGuard dg(batch_device(*B_(h)));
     batch_download(*B_(h), circuit, re, im);
   });
 }
@@ -1119,7 +1207,11 @@ int bf_batch_stream(bf_batch* h, void** stream) {
 }
 
 int bf_batch_destroy(bf_batch* h) {
-  return guarded([&]() { batch_destroy(B_(h)); });
+  return guarded([&]() {
+    if (!h) return;
+    DeviceGuard dg(batch_device(*B_(h)));
+    batch_destroy(B_(h));
+  });
 }
 
 int bf_norm2_noalloc(const void* d_amps, uint64_t num_amps, int32_t dtype, double* d_out, void* stream) {
@@ -1173,7 +1265,11 @@ int bf_server_stats(bf_server* h, bf_server_counters* out) {
 }
 
 int bf_server_destroy(bf_server* h) {
-  return guarded([&]() { server_destroy(V_(h)); });
+  return guarded([&]() {
+    if (!h) return;
+    DeviceGuard dg(server_device(*V_(h)));
+    server_destroy(V_(h));
+  });
 }
 
 // Host-only: validates and plans ops for a state of n qubits without a

@@ -207,9 +207,16 @@ static void enqueue(Batch& b) {
   }
 }
 
+// The kernel's shared-memory limit is set once per device to the largest a
+// batch can ask for (a 13-qubit tile), so batches of different tile sizes,
+// created on any thread, never lower it under one another.
 template <class P>
 static void size_grid(Batch& b) {
-  BF_CUDA(cudaFuncSetAttribute(k_batch<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b.smem));
+  static PerDeviceOnce configured;  // one per instantiation of P
+  configured.run(b.device, [] {
+    const size_t most = std::max<size_t>(tile_smem_bytes<P>(kMaxTileQubits, 0), kTileThreads * sizeof(double));
+    BF_CUDA(cudaFuncSetAttribute(k_batch<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most));
+  });
   int per_sm = 0;
   BF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<P>, kTileThreads, b.smem));
   if (per_sm < 1) fail(BF_EUNSUPPORTED, "batch kernel cannot be resident with %zu bytes of shared memory", b.smem);
@@ -424,5 +431,7 @@ void batch_stats(const Batch& b, int64_t* tasks, int64_t* passes, uint64_t* stat
 }
 
 void* batch_stream(const Batch& b) { return (void*)b.stream; }
+
+int batch_device(const Batch& b) { return b.device; }
 
 }  // namespace bf

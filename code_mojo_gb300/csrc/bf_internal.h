@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -21,6 +23,58 @@ struct Error {
 [[noreturn]] void fail(int code, const char* fmt, ...);
 void check_cuda(cudaError_t e, const char* what);
 #define BF_CUDA(call) ::bf::check_cuda((call), #call)
+
+// ---------------------------------------------------------------------------
+// Devices.  Kernel attributes (cudaFuncSetAttribute) belong to one device,
+// and the entry points may be called from several threads at once, so each
+// launcher configures its kernels once per device under a lock.
+constexpr int kMaxDevices = 64;
+class PerDeviceOnce {
+ public:
+  // Runs f() the first time it is called with the current device `dev`.
+  template <class F>
+  void run(int dev, F&& f) {
+    if (dev < 0 || dev >= kMaxDevices) fail(BF_EUNSUPPORTED, "device ordinal %d out of range", dev);
+    const uint64_t bit = 1ull << dev;
+    if (done_.load(std::memory_order_acquire) & bit) return;
+    std::lock_guard<std::mutex> lock(mu_);
+    if (done_.load(std::memory_order_relaxed) & bit) return;
+    f();
+    done_.fetch_or(bit, std::memory_order_release);
+  }
+
+ private:
+  std::atomic<uint64_t> done_{0};
+  std::mutex mu_;
+};
+
+// Makes `dev` the calling thread's current device for the guard's lifetime
+// and restores the caller's device afterwards.  Every entry point that takes
+// a state, batch or server runs its work under one, so a handle created on
+// one GPU keeps launching there whatever device the calling thread has set.
+class DeviceGuard {
+ public:
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev_) != cudaSuccess) {
+      cudaGetLastError();
+      prev_ = -1;
+    }
+    if (dev >= 0 && prev_ != dev) {
+      BF_CUDA(cudaSetDevice(dev));
+      switched_ = true;
+    }
+  }
+  ~DeviceGuard() {
+    if (switched_ && prev_ >= 0) cudaSetDevice(prev_);
+  }
+  DeviceGuard(const DeviceGuard&) = delete;
+  DeviceGuard& operator=(const DeviceGuard&) = delete;
+
+ private:
+  int prev_ = -1;
+  bool switched_ = false;
+};
+int current_device();
 
 // ---------------------------------------------------------------------------
 // Compute precision of a state.
@@ -169,9 +223,15 @@ struct State {
   size_t prog_cap = 0;
   cudaEvent_t prog_event = nullptr;
   bool prog_event_live = false;
-  // staging for SoA <-> interleaved conversion
+  // staging for SoA <-> interleaved conversion: two chunk buffers, so that
+  // the copy of one chunk (on copy_stream) overlaps the conversion kernel of
+  // the other (on stream); the events order the two streams per buffer
   void* d_stage = nullptr;
   size_t stage_bytes = 0;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t stage_copied[2] = {nullptr, nullptr};  // copy into / out of buffer k done
+  cudaEvent_t stage_done[2] = {nullptr, nullptr};    // conversion kernel on buffer k done
+  cudaEvent_t stage_start = nullptr;                 // the state's earlier work
   // dense unitary matrix (device copy of the current op's matrix)
   double* d_umat = nullptr;
   // norms before / after a complex64 circuit and the rescale factor
@@ -306,6 +366,7 @@ void batch_destroy(Batch* b);
 void batch_stats(const Batch& b, int64_t* tasks, int64_t* passes, uint64_t* state_bytes, int32_t* graph,
                  uint64_t* launches);
 void* batch_stream(const Batch& b);
+int batch_device(const Batch& b);
 
 // Wire formats (wire.cpp).
 struct OpList;
@@ -325,5 +386,6 @@ int server_poll(Server& sv, bf_result* out, int max);
 bool server_wait_idle(Server& sv, int64_t timeout_ms);
 void server_stats(Server& sv, bf_server_counters& s);
 void server_destroy(Server* sv);
+int server_device(const Server& sv);
 
 }  // namespace bf

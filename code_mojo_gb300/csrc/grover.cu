@@ -584,13 +584,12 @@ static bool try_grover_cluster(State& st, LoopArgs& a) {
   if (C > 16) return false;
   a.chunk = st.N / C;
   const size_t smem = (size_t)a.chunk * sizeof(typename P::Smem);
-  static bool configured = false;
-  if (!configured) {
+  static PerDeviceOnce configured;  // one per instantiation of P
+  configured.run(st.device, [] {
     BF_CUDA(cudaFuncSetAttribute(k_grover_cluster<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)kClusterChunkBytes));
     BF_CUDA(cudaFuncSetAttribute(k_grover_cluster<P>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    configured = true;
-  }
+  });
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(C);
   cfg.blockDim = dim3(kClusterThreads);

@@ -16,6 +16,12 @@
 // so nothing needs clearing first.  Calls whose kernels overlap on the GPU
 // (on different streams, or from different threads without ordering) race on
 // the array and may return wrong sums: serialise them.
+//
+// Range: the sum is accumulated in double-float, whose exponent range is
+// FP32's.  Components of magnitude below about 1.1e-19 add nothing (their
+// squares flush to zero: at most 2^31 x 1.2e-38 in all), and a component of
+// magnitude 1.8e19 or more overflows the sum.  Normalised states are far
+// inside that range.
 #include <mutex>
 
 #include "amp_math.cuh"
@@ -93,7 +99,10 @@ __global__ void __launch_bounds__(kNoAllocThreads) k_norm2_finish(const double* 
 
 // Device address of g_norm2_scratch, resolved once per device with that
 // device current.  The host-side name g_norm2_scratch is only a stand-in for
-// the symbol and must never be passed to a kernel.
+// the symbol and must never be passed to a kernel.  The table is never
+// cleared: after cudaDeviceReset (or any teardown of the device's primary
+// context) the cached address is stale, so a process that resets a device
+// must not call bf_norm2_noalloc on it again.
 static void* noalloc_scratch_for_current_device() {
   static std::mutex mu;
   static void* addr[64] = {nullptr};
@@ -117,6 +126,13 @@ void norm2_noalloc(const void* d_amps, uint64_t num_amps, int32_t dtype, double*
   if (!d_amps || !d_out) fail(BF_EINVAL, "bf_norm2_noalloc: null device pointer");
   if (dtype != BF_C128 && dtype != BF_C64) fail(BF_EINVAL, "bf_norm2_noalloc: unknown dtype %d", dtype);
   if (num_amps == 0) fail(BF_EINVAL, "bf_norm2_noalloc: no amplitudes");
+  // The kernels read whole double2 (16 B) or float2 (8 B) amplitudes and
+  // write one double; a misaligned pointer would fault on the device and
+  // poison the caller's context, so it is refused here, before any launch.
+  const uintptr_t amp_align = dtype == BF_C128 ? 16u : 8u;
+  if (reinterpret_cast<uintptr_t>(d_amps) % amp_align != 0)
+    fail(BF_EINVAL, "bf_norm2_noalloc: d_amps must be %u-byte aligned for this dtype", (unsigned)amp_align);
+  if (reinterpret_cast<uintptr_t>(d_out) % 8u != 0) fail(BF_EINVAL, "bf_norm2_noalloc: d_out must be 8-byte aligned");
   if (num_amps > kNoAllocMaxAmps)
     fail(BF_EINVAL,
          "bf_norm2_noalloc: %llu amplitudes exceed the maximum of %llu (2^31) set by its static scratch; "

@@ -26,6 +26,12 @@ void check_cuda(cudaError_t e, const char* what) {
   }
 }
 
+int current_device() {
+  int dev = 0;
+  BF_CUDA(cudaGetDevice(&dev));
+  return dev;
+}
+
 // ---- validation: validate_circuit (executors.mojo:78-185) ----------------
 static void check_qubit(int idx, int n, const char* label) {
   if (idx < 0 || idx >= n) fail(BF_EINVAL, "%s out of bounds: %d", label, idx);

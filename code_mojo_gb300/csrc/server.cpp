@@ -331,4 +331,6 @@ void server_destroy(Server* sv) {
   delete sv;
 }
 
+int server_device(const Server& sv) { return sv.device; }
+
 }  // namespace bf

@@ -448,12 +448,11 @@ static void launch_unitary_p(State& st, const double* h_u, int t, int m, int con
   double* d_u = st.d_umat;
   BF_CUDA(cudaMemcpyAsync(d_u, h_u, mbytes, cudaMemcpyHostToDevice, st.stream));
   size_t smem = ((size_t)dim * dim + kUniThreads) * sizeof(typename P::Smem);
-  static int configured[3] = {0, 0, 0};
-  if (!configured[st.prec]) {
+  static PerDeviceOnce configured;  // one per instantiation of P
+  configured.run(st.device, [] {
     BF_CUDA(cudaFuncSetAttribute(k_unitary<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)(((size_t)64 * 64 + kUniThreads) * sizeof(typename P::Smem))));
-    configured[st.prec] = 1;
-  }
+  });
   uint64_t ctas = std::min<uint64_t>((a.groups + a.G - 1) / a.G, (uint64_t)st.num_sms * 8);
   k_unitary<P><<<(unsigned)ctas, kUniThreads, smem, st.stream>>>(static_cast<typename P::Glob*>(st.amp), d_u, a);
   BF_CUDA(cudaGetLastError());

@@ -845,12 +845,11 @@ void launch_block_pass_digits(State& st, const Blk5* d_blocks, int nblocks, cons
   a.scale_exp = d_exp;
   a.flag = state_flag(st);
   a.spin_limit = 1u << 24;
-  static bool configured = false;
-  if (!configured) {
+  static PerDeviceOnce configured;
+  configured.run(st.device, [] {
     BF_CUDA(cudaFuncSetAttribute(k_tblock_dg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDgSmemAlloc));
     BF_CUDA(cudaFuncSetAttribute(k_tblock_dg, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-    configured = true;
-  }
+  });
   uint64_t grid = std::min<uint64_t>(a.ntiles, (uint64_t)st.num_sms);
   k_tblock_dg<<<(unsigned)grid, kDgThreads, kDgSmemAlloc, st.stream>>>(a);
   BF_CUDA(cudaGetLastError());
@@ -879,13 +878,12 @@ void launch_block_pass(State& st, const Blk5* d_blocks, int nblocks, const unsig
   a.ntiles = st.N >> kBlockTileQubits;
   a.flag = state_flag(st);
   a.spin_limit = 1u << 24;
-  static bool configured = false;
-  if (!configured) {
+  static PerDeviceOnce configured;
+  configured.run(st.device, [] {
     BF_CUDA(cudaFuncSetAttribute(k_tblock, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemAlloc));
     // the whole L1/shared split as shared memory: two CTAs per SM
     BF_CUDA(cudaFuncSetAttribute(k_tblock, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-    configured = true;
-  }
+  });
   // two CTAs per SM when the shared memory holds them (one CTA's MMAs then
   // overlap the other's loads and conversions); the occupancy calculator
   // can report one under the default carveout, so count from the SM's size

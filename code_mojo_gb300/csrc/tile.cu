@@ -40,13 +40,11 @@ static void launch_tile_p(State& st, const TileOp* d_ops, int nops, const TilePa
   for (int j = 0; j < geo.L; ++j)
     if (geo.q[j] != j) fail(BF_EINVAL, "internal: tile qubits must start with 0..%d", geo.L - 1);
   size_t smem = tile_smem_bytes<P>(p.K, geo.L);
-  static int configured[3] = {0, 0, 0};
-  int idx = st.prec;
-  if (!configured[idx]) {
+  static PerDeviceOnce configured;  // one per instantiation of P
+  configured.run(st.device, [] {
     BF_CUDA(cudaFuncSetAttribute(k_tile<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)tile_smem_bytes<P>(kMaxTileQubits, 0)));
-    configured[idx] = 1;
-  }
+  });
   uint64_t blocks = st.N >> p.K;
   if (blocks > 0x7fffffffull) fail(BF_EUNSUPPORTED, "tile grid too large");
   k_tile<P><<<(unsigned)blocks, kTileThreads, smem, st.stream>>>(static_cast<typename P::Glob*>(st.amp), d_ops,

@@ -143,3 +143,18 @@ def adjoint(ops: OpArray) -> OpArray:
     angled = np.isin(a["gate"], [F.BF_GATE_P, F.BF_GATE_RX, F.BF_GATE_RY, F.BF_GATE_RZ])
     a["arg"][angled] = -a["arg"][angled]
     return OpArray(ops.num_qubits, a, list(ops.keep))
+
+
+def batch_mix(count: int = 4096, seed: int = 7, nmin: int = 8, nmax: int = 20, depth: int = 20) -> list[OpArray]:
+    """The batched workload: `count` circuits with qubit counts uniform in
+    [nmin, nmax]; even positions are random layered circuits of `depth`
+    layers, odd ones value encodings with v uniform in [0, 2^n)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for i in range(count):
+        n = int(rng.integers(nmin, nmax + 1))
+        if i % 2 == 0:
+            out.append(random_layered(n, depth, int(rng.integers(0, 2 ** 31))))
+        else:
+            out.append(value_encoding(n, float(rng.uniform(0, 2 ** n))))
+    return out

@@ -190,7 +190,13 @@ int bf_state_info(const bf_state* st, int32_t* num_qubits, int32_t* dtype);
 /* |idx> basis state. */
 int bf_state_set_basis(bf_state* st, uint64_t idx);
 /* Host SoA arrays re[2^n], im[2^n] (the reference's layout, state.mojo:20-21)
- * to and from the device's interleaved layout.  Download blocks. */
+ * to and from the device's interleaved layout, pageable or page-locked host
+ * memory alike.  Upload returns once re and im have been read (the caller
+ * may reuse them at once; the conversion on the device is stream-ordered
+ * before later work on the state).  Download blocks until re and im hold
+ * the amplitudes.  Both move 4 Mi-amplitude chunks through two device
+ * buffers so that one chunk's host copy overlaps the next chunk's
+ * conversion. */
 int bf_state_upload_soa(bf_state* st, const double* re, const double* im);
 int bf_state_download_soa(bf_state* st, double* re, double* im);
 /* Copies amplitudes [offset, offset+count) to host SoA arrays (blocks). */
@@ -345,9 +351,15 @@ int bf_server_destroy(bf_server* s);
  * `stream` (a cudaStream_t; NULL = the default stream).  Nothing is
  * allocated: the partial sums use a 512 KiB array built into the library
  * (held by every GPU that loads it), which limits num_amps to 2^31; larger
- * inputs are rejected with BF_EINVAL.  The first call on a device resolves
- * that array's address; make it before capturing a stream.  All calls share
- * the array, so calls that overlap on the GPU race: serialise them. */
+ * inputs are rejected with BF_EINVAL, and so are d_amps not aligned to its
+ * amplitude size (16 B for BF_C128, 8 B for BF_C64) and d_out not aligned to
+ * 8 B, before anything is launched.  The first call on a device resolves
+ * that array's address; make it before capturing a stream.  The address is
+ * kept for the life of the process: after cudaDeviceReset on a device, do
+ * not call this again there.  All calls share the array, so calls that
+ * overlap on the GPU race: serialise them.  The sum is accumulated in
+ * double-float (FP32's exponent range): components below about 1.1e-19 in
+ * magnitude add nothing, and one of 1.8e19 or more overflows. */
 int bf_norm2_noalloc(const void* d_amps, uint64_t num_amps, int32_t dtype,
                      double* d_out, void* stream);
 

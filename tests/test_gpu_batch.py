@@ -54,3 +54,39 @@ def test_value_encoding_in_a_batch_lands_on_the_reversed_value():
         p = np.abs(b.download(c)) ** 2
         assert int(np.argmax(p)) == rev and p[rev] > 1 - 1e-5
     b.close()
+
+
+@pytest.mark.parametrize("dtype", ["c64", "c128"])
+def test_batch_at_full_spec_matches_the_oracle_per_circuit(dtype):
+    """The benchmarked batch itself: 4096 circuits of 8..20 qubits, half
+    random layered at depth 20, half value encodings with v uniform in
+    [0, 2^n), one persistent launch; a seeded sample of 64 circuits checked
+    one by one against the oracle's FP64 run (complex128: max|d amp| <=
+    1e-12; complex64: infidelity <= 1e-6)."""
+    from code_mojo_gb300 import opsarray as OA
+    circs = OA.batch_mix(4096, seed=7)
+    b = B.Batch(circs, dtype=dtype)
+    b.run()
+    rng = np.random.Generator(np.random.PCG64(101 if dtype == "c64" else 102))
+    sample = rng.choice(len(circs), size=64, replace=False)
+    # the sample covers the whole qubit range and both circuit kinds
+    assert max(circs[c].num_qubits for c in sample) >= 19 and len({c % 2 for c in sample}) == 2
+    worst = 0.0
+    for c in sample:
+        ops = circs[int(c)]
+        n = ops.num_qubits
+        re, im = O.basis(n)
+        if n >= 17:
+            O.run_inplace(ops, re, im, strategy=O.OR_SIMD_PARALLEL, threads=O.num_cores(), chunks=O.num_cores())
+        else:
+            re, im = O.run(ops, re, im)
+        exp = re + 1j * im
+        got = b.download(int(c))
+        if dtype == "c128":
+            d = float(np.max(np.abs(got - exp)))
+            assert d <= 1e-12, (int(c), n, d)
+        else:
+            d = 1 - abs(np.vdot(exp, got)) ** 2
+            assert d <= 1e-6, (int(c), n, d)
+        worst = max(worst, d)
+    b.close()

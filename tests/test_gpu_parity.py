@@ -383,6 +383,31 @@ def test_random_layered_30q_matches_the_oracle():
     assert worst <= TOL128
 
 
+def test_random_layered_30q_40_layers_matches_the_oracle(capsys):
+    """The benchmarked circuit itself, all 40 layers (1200 U3 + 600 CX, the
+    default plan of digit tensor-core passes), against the oracle's
+    SIMD_PARALLEL port on every host core, amplitude by amplitude.  The
+    worst difference is printed."""
+    n = 30
+    qc = W.random_layered_circuit(n, 40, seed=0)
+    st = bfy.QuantumState(n)
+    bfy.execute(st, qc)
+    plan = bfy.plan_stats(qc)
+    re, im = O.basis(n)
+    O.run_inplace(qc, re, im, strategy=O.OR_SIMD_PARALLEL, threads=O.num_cores(), chunks=O.num_cores())
+    blk = 1 << 22
+    gr, gi = np.empty(blk), np.empty(blk)
+    worst = 0.0
+    for off in range(0, 1 << n, blk):
+        F.check(F.lib().bf_state_download_range(st.handle, off, blk, gr.ctypes.data, gi.ctypes.data))
+        worst = max(worst, float(np.max(np.abs((gr - re[off:off + blk]) + 1j * (gi - im[off:off + blk])))))
+    st.close()
+    with capsys.disabled():
+        print(f"\n30-qubit 40-layer circuit ({plan['block_passes']} digit passes, {plan['blocks']} blocks): "
+              f"max|d amp| against the oracle = {worst:.3e}")
+    assert worst <= TOL128
+
+
 # ---- measurement and readout (apply_measure, state.mojo:447-553) --------------
 @pytest.mark.parametrize("dtype", ["c128", "c64"])
 @pytest.mark.parametrize("qubits,values", [([0, 1, 2], None), ([13, 2, 7], None), ([5], None),

@@ -120,3 +120,22 @@ def test_large_requests_run_cheapest_first():
     # start order is queue order
     order = sorted(ids, key=lambda rid: res[rid].queue_s)
     assert order == sorted(ids, key=lambda rid: cost[rid])
+
+
+def test_served_complex64_results_match_the_oracle():
+    """complex64 served results against the FP64 oracle: the top-16
+    probabilities within 1e-6 of the oracle's at the served indices, and the
+    served set is a top-16 set of the oracle's distribution (up to ties
+    within that tolerance).  The mix runs Grover searches, value encodings
+    and layered circuits of 6..20 qubits on 4 slots at once."""
+    reqs = SV.request_mix(16, seed=13, nmin=6, nmax=20)
+    mixed, _ = run_mixed(reqs, "c64", slots=4)
+    for i, (kind, ops) in enumerate(reqs):
+        re, im = O.basis(ops.num_qubits)
+        O.run_inplace(ops, re, im, strategy=O.OR_SIMD_PARALLEL, threads=O.num_cores(), chunks=O.num_cores())
+        p = re * re + im * im
+        r = mixed[i]
+        idx = r.top_index.astype(np.int64)
+        assert np.max(np.abs(p[idx] - r.top_prob)) <= 1e-6, (i, kind, ops.num_qubits)
+        kth = np.sort(p)[::-1][len(idx) - 1]
+        assert np.all(p[idx] >= kth - 1e-6), (i, kind)
