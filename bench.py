@@ -314,6 +314,96 @@ def run_qft_bench(n: int, reps: int) -> dict:
             "l2": f"state ({int(S) >> 20} MiB) stays in L2: bandwidths are L2 figures"}
 
 
+# The reference's published times for this workload (osx-arm64 CPU, median
+# of 5 trials x 3 iterations including circuit construction and state
+# allocation): benches/results/2026_02_06/execution_strategies_*.csv:17-21
+# (GRID_PARALLEL_FUSED, unfused circuit) and benches/results/2026_01_12/
+# value_encoding_strategies_qiskit_*.csv:13 (n = 25, GRID_PARALLEL_FUSED).
+PUBLISHED_VALUE_ENCODING_MS = {20: 10.72, 22: 83.53, 24: 376.05, 25: 822.66}
+
+
+def run_value_encoding_bench(sizes, fused_sizes, cpu: bool) -> dict:
+    """The reference's value-encoding "full" workload (encode_value_circuit
+    with v = 4.7: H on every qubit, P(2 pi v / 2^(j+1)) on qubit j, then the
+    MSB-first inverse QFT without swap; benches/bench_execution_strategies.mojo:
+    16-34), complex128, from |0...0>.  Per size: the device time of execute
+    on a resident state (CUDA events, median of 15 after 3 warm-ups); the
+    reference's own method around the public API (circuit construction,
+    state creation, execute, synchronisation: wall time, median of 5 trials
+    x 3 iterations after one warm-up); and the restated SIMD_PARALLEL
+    strategy on this host's cores (median of 3 after one warm-up, circuit
+    construction excluded).  `fused_sizes` run the circuit through
+    fuse_circuit_specialized_pairs first, as the reference's fused
+    benchmark does (benches/bench_value_encoding_strategies_qiskit.mojo:22-39)."""
+    import torch
+    from code_mojo_gb300 import butterfly as bfy
+    from code_mojo_gb300 import fusion as FU
+    from code_mojo_gb300 import workloads as W
+    v = 4.7
+    ctx = bfy.ExecContext()
+    ctx.execution_strategy = bfy.ExecutionStrategy.GPU_FUSED
+    ctx.gpu_sync = False
+    out = {"v": v, "dtype": "complex128", "runs": {}}
+    cases = [(n, False) for n in sizes] + [(n, True) for n in fused_sizes]
+    for n, fused in cases:
+        build = (lambda: FU.fuse_circuit_specialized_pairs(W.encode_value_circuit(n, v))) if fused else \
+            (lambda: W.encode_value_circuit(n, v))
+        qc = build()
+        st = bfy.QuantumState(n)
+        stream = torch.cuda.ExternalStream(st.stream_ptr())
+        dev = []
+        for i in range(18):
+            st.set_basis(0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            bfy.execute(st, qc, ctx)
+            e1.record(stream)
+            e1.synchronize()
+            if i >= 3:
+                dev.append(e0.elapsed_time(e1))
+        st.close()
+        sctx = ctx.copy()
+        sctx.gpu_sync = True
+
+        def ref_method():
+            t0 = time.perf_counter()
+            c = build()
+            s = bfy.QuantumState(n)
+            bfy.execute(s, c, sctx)
+            s.sync()
+            dt = time.perf_counter() - t0
+            s.close()
+            return dt * 1e3
+        ref_method()
+        trials = [float(np.median([ref_method() for _ in range(3)])) for _ in range(5)]
+        key = f"{n}{'_fused_pairs' if fused else ''}"
+        r = {"qubits": n, "fused_pairs": fused, "gates": sum(2 if isinstance(t, bfy.FusedPairTransformation) else 1
+                                                             for t in qc.transformations),
+             "transformations": len(qc.transformations), "ms": float(np.median(dev)),
+             "ms_reference_method": float(np.median(trials)),
+             "published_reference_ms": PUBLISHED_VALUE_ENCODING_MS.get(n),
+             "plan": bfy.plan_stats(qc, ctx)}
+        if r["published_reference_ms"]:
+            r["speedup_vs_published"] = r["published_reference_ms"] / r["ms_reference_method"]
+        if cpu:
+            from oracle import pyoracle as O
+            cores = O.num_cores()
+            times = []
+            for i in range(4):
+                re, im = O.basis(n)
+                t0 = time.perf_counter()
+                O.run_inplace(qc, re, im, strategy=O.OR_SIMD_PARALLEL, threads=cores, chunks=cores)
+                if i:
+                    times.append((time.perf_counter() - t0) * 1e3)
+            r["cpu_port_ms"] = float(np.median(times))
+            r["cpu_port_cores"] = cores
+        out["runs"][key] = r
+    out["published_source"] = ("reference CSVs, osx-arm64 CPU, GRID_PARALLEL_FUSED (benches/results/2026_02_06/"
+                               "execution_strategies_*.csv:17-21; n=25: benches/results/2026_01_12/"
+                               "value_encoding_strategies_qiskit_*.csv:13)")
+    return out
+
+
 def run_batch_bench(count: int, reps: int, sample: int) -> dict:
     """The batched workload: `count` circuits, qubit counts uniform in [8, 20],
     half random layered (depth 20), half value encodings; one persistent
@@ -629,6 +719,8 @@ def run_ours(args) -> None:
             del hre, him
 
     qft = run_qft_bench(20, 50) if args.qft and rank == 0 else None
+    value_enc = (run_value_encoding_bench([20, 22, 24], [25], cpu=args.cpu_gates > 0)
+                 if args.value_encoding and rank == 0 else None)
     batch = run_batch_bench(args.batch_count, 3, 256) if args.batch_count > 0 else None
     serving = (run_serving_bench(args.serve_rate, args.serve_seconds, args.serve_seconds, 12)
                if args.serve_seconds > 0 else None)
@@ -670,6 +762,7 @@ def run_ours(args) -> None:
         "e2e": e2e,
         "cpu_baseline": cpu,
         "qft20": qft,
+        "value_encoding": value_enc,
         "batch": batch,
         "serving": serving,
         "precision": precision,
@@ -695,6 +788,8 @@ def main():
     ap.add_argument("--ref-gates", type=int, default=45, help="gates per reference-arm step (45: one whole layer)")
     ap.add_argument("--batch-count", type=int, default=4096)
     ap.add_argument("--qft", type=int, default=1, help="time the 20-qubit QFT workload (0: skip)")
+    ap.add_argument("--value-encoding", type=int, default=1,
+                    help="time the reference's value-encoding workload at 20/22/24 qubits and fused at 25 (0: skip)")
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--precision-qubits", type=int, default=33,

@@ -481,12 +481,16 @@ static void build_steps(int n, const bf_op* ops, int64_t nops, const bf_exec_opt
                          (is_p(op) && is_p(t1) && op.target != t1.target) ||
                          (is_h(op) && is_p(t1) && op.target != t1.target) ||
                          (is_p(op) && is_h(t1) && op.target != t1.target);
-          if (special) {
+          if (fused) {
+            // a fused pair is its two gates in order: both join the run that
+            // the tile planner fuses, whatever the pair's kind (the
+            // reference's 4x4 product for H+CP and the like is the same map)
+            run.push_back(lower_gate(op, o.specialized));
+            run.push_back(lower_gate(t1, o.specialized));
+          } else if (special) {
             // one pass for both gates: a two-gate run through the tile planner
             std::vector<GateInstr> pair = {lower_gate(op, o.specialized), lower_gate(t1, o.specialized)};
-            if (fused) {
-              run.insert(run.end(), pair.begin(), pair.end());
-            } else {
+            {
               std::vector<GateInstr> saved;
               saved.swap(run);
               run = pair;
