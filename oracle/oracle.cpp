@@ -845,6 +845,232 @@ void fft_in_place(std::vector<double>& re, std::vector<double>& im, bool inverse
   }
 }
 
+// ---- fusion rewrites (transformations_fusion.mojo:24-908) ------------------
+// A second restatement of the reference's fusion passes, over op records,
+// so that the host mirror's rewrite (code_mojo_gb300/fusion.py) is checked
+// against an independent one.  An item is a gate (one record), a fused pair
+// (two records, the first flagged BF_OPF_FUSE_WITH_NEXT), a 1- or 2-qubit
+// unitary, a controlled 1-qubit unitary, or any other record passed through.
+enum ItemKind { IT_GATE, IT_PAIR, IT_UNITARY, IT_CUNITARY, IT_OTHER };
+struct Item {
+  ItemKind kind = IT_OTHER;
+  bf_op op[2] = {};           // IT_GATE / IT_OTHER: op[0]; IT_PAIR: both
+  std::vector<Cplx> u;        // IT_UNITARY (2x2 or 4x4) / IT_CUNITARY (2x2), row-major
+  int target = 0, m = 0, control = -1;
+};
+
+// ControlKind of a gate record: 0 none, 1 one control, 2 several
+int control_kind(const bf_op& o) { return o.ncontrols == 0 ? 0 : (o.ncontrols == 1 ? 1 : 2); }
+int control_of(const bf_op& o) { return control_kind(o) == 1 ? lowest_bit(o.controls) : 0; }
+bool is_special(const bf_op& o) { return is_h(o) || is_p(o) || is_cp(o); }
+
+Item gate_item(const bf_op& o) {
+  Item it;
+  it.kind = IT_GATE;
+  it.op[0] = o;
+  return it;
+}
+
+// can_fuse_special_pair (:181-219)
+bool can_fuse_special(const bf_op& t0, const bf_op& t1) {
+  if (control_kind(t0) == 2 || control_kind(t1) == 2) return false;
+  if (is_cp(t0) && is_cp(t1) && t0.controls == t1.controls && t0.target != t1.target) return true;
+  int lo = t0.target, hi = t0.target;
+  auto widen = [&](int q) { lo = std::min(lo, q); hi = std::max(hi, q); };
+  if (control_kind(t0) == 1) widen(control_of(t0));
+  if (control_kind(t1) == 1) widen(control_of(t1));
+  widen(t1.target);
+  if (hi - lo != 1) return false;
+  return (is_h(t0) && is_h(t1)) || (is_p(t0) && is_p(t1)) || (is_h(t0) && is_cp(t1)) || (is_cp(t0) && is_h(t1));
+}
+
+// fuse_special_pair_gates (:312-333)
+std::vector<Item> special_pairs(const std::vector<Item>& in) {
+  std::vector<Item> out;
+  for (size_t i = 0; i < in.size(); ++i) {
+    if (i + 1 < in.size() && in[i].kind == IT_GATE && in[i + 1].kind == IT_GATE &&
+        can_fuse_special(in[i].op[0], in[i + 1].op[0])) {
+      Item it;
+      it.kind = IT_PAIR;
+      it.op[0] = in[i].op[0];
+      it.op[1] = in[i + 1].op[0];
+      it.op[0].flags |= BF_OPF_FUSE_WITH_NEXT;
+      out.push_back(it);
+      ++i;
+      continue;
+    }
+    out.push_back(in[i]);
+  }
+  return out;
+}
+
+// 4x4 of a gate record on the pair (q_low, q_low + 1); try_pair_matrix
+// (:129-161) for the specialised form
+bool pair_4x4(const bf_op& g, int q_low, int q_high, bool special_only, Cplx* m) {
+  if (special_only && !is_special(g)) return false;
+  Gate2 gm;
+  gate_matrix(g.gate, g.arg, g.mat, gm);
+  if (control_kind(g) == 0) {
+    if (g.target != q_low && g.target != q_high) return false;
+    gate_to_4x4(gm, q_low, g.target, m);
+    return true;
+  }
+  if (control_kind(g) != 1) return false;
+  const int c = control_of(g);
+  if (c == g.target || (c != q_low && c != q_high) || (g.target != q_low && g.target != q_high)) return false;
+  cgate_to_4x4(gm, q_low, c, g.target, m);
+  return true;
+}
+
+void bounds(const bf_op& g, int* lo, int* hi) {  // gate_bounds (:106-117)
+  *lo = *hi = g.target;
+  if (control_kind(g) == 1) {
+    *lo = std::min(*lo, control_of(g));
+    *hi = std::max(*hi, control_of(g));
+  }
+}
+
+// fuse_contiguous_target_pairs (:539-687) and its specialised form (:689-876)
+std::vector<Item> contiguous_pairs(const std::vector<Item>& in, bool special) {
+  std::vector<Item> out;
+  bool pending = false, paired = false;
+  bf_op p{};
+  Cplx acc[16];
+  int lo = 0, hi = 0;
+  auto flush = [&]() {
+    if (paired) {
+      Item it;
+      it.kind = IT_UNITARY;
+      it.u = std::vector<Cplx>(std::begin(acc), std::end(acc));
+      it.target = lo;
+      it.m = 2;
+      out.push_back(it);
+    } else if (pending) {
+      out.push_back(gate_item(p));
+    }
+    pending = paired = false;
+  };
+  auto start = [&](const bf_op& g) {
+    flush();
+    p = g;
+    pending = true;
+  };
+  for (const Item& it : in) {
+    bool passes = it.kind != IT_GATE;
+    if (!passes) {
+      const bf_op& g = it.op[0];
+      passes = special ? (control_kind(g) == 2 || !is_special(g)) : control_kind(g) != 0;
+    }
+    if (passes) {
+      flush();
+      out.push_back(it);
+      continue;
+    }
+    const bf_op& g = it.op[0];
+    if (!pending) {
+      start(g);
+      continue;
+    }
+    if (!paired) {
+      const bool same = g.target == p.target &&
+                        (!special || (control_kind(g) == control_kind(p) && control_of(g) == control_of(p)));
+      if (!same) {
+        int l0, h0, l1, h1;
+        bounds(p, &l0, &h0);
+        bounds(g, &l1, &h1);
+        const int l = special ? std::min(l0, l1) : std::min(p.target, g.target);
+        const int h = special ? std::max(h0, h1) : std::max(p.target, g.target);
+        Cplx m0[16], m1[16];
+        if (h - l == 1 && pair_4x4(p, l, h, special, m0) && pair_4x4(g, l, h, special, m1)) {
+          matmul4(m1, m0, acc);
+          lo = l;
+          hi = h;
+          paired = true;
+          continue;
+        }
+      }
+      start(g);
+      continue;
+    }
+    Cplx m1[16], nxt[16];
+    if (pair_4x4(g, lo, hi, special, m1)) {
+      matmul4(m1, acc, nxt);
+      std::copy(nxt, nxt + 16, acc);
+      continue;
+    }
+    start(g);
+  }
+  flush();
+  return out;
+}
+
+// fuse_same_target_gates (:427-537) with flush_active (:335-392)
+std::vector<Item> same_target_runs(const std::vector<Item>& in) {
+  std::vector<Item> out;
+  bool active = false, phase = false;
+  int count = 0;
+  bf_op first{};
+  Gate2 prod;
+  double phase_sum = 0;
+  auto flush = [&]() {
+    if (!active) return;
+    if (phase) {
+      bf_op g = first;
+      g.gate = BF_GATE_P;
+      g.arg = phase_sum;
+      out.push_back(gate_item(g));
+    } else if (count == 1) {
+      out.push_back(gate_item(first));
+    } else {
+      Item it;
+      it.kind = control_kind(first) == 0 ? IT_UNITARY : IT_CUNITARY;
+      it.u = {prod[0][0], prod[0][1], prod[1][0], prod[1][1]};
+      it.target = first.target;
+      it.m = 1;
+      it.control = control_kind(first) == 0 ? -1 : control_of(first);
+      out.push_back(it);
+    }
+    active = false;
+  };
+  for (const Item& it : in) {
+    if (it.kind != IT_GATE || control_kind(it.op[0]) == 2) {
+      flush();
+      out.push_back(it);
+      continue;
+    }
+    const bf_op& g = it.op[0];
+    Gate2 gm;
+    gate_matrix(g.gate, g.arg, g.mat, gm);
+    if (active && g.target == first.target && control_kind(g) == control_kind(first) &&
+        control_of(g) == control_of(first)) {
+      Gate2 next;  // mul_gate(new, product) (:24-33)
+      for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j) {
+          Cplx sum{0, 0};
+          for (int k = 0; k < 2; ++k) {
+            sum.re = sum.re + (gm[i][k].re * prod[k][j].re - gm[i][k].im * prod[k][j].im);
+            sum.im = sum.im + (gm[i][k].re * prod[k][j].im + gm[i][k].im * prod[k][j].re);
+          }
+          next[i][j] = sum;
+        }
+      std::memcpy(prod, next, sizeof prod);
+      ++count;
+      if (phase && g.gate == BF_GATE_P) phase_sum += g.arg;
+      else phase = false;
+      continue;
+    }
+    flush();
+    active = true;
+    first = g;
+    count = 1;
+    std::memcpy(prod, gm, sizeof prod);
+    phase = g.gate == BF_GATE_P;
+    phase_sum = phase ? g.arg : 0.0;
+  }
+  flush();
+  return out;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1022,6 +1248,75 @@ double or_norm2(int32_t n, const double* re, const double* im) {
 int32_t or_num_cores(void) {
   unsigned c = std::thread::hardware_concurrency();
   return c ? (int32_t)c : 1;
+}
+
+// fuse_circuit / fuse_circuit_specialized_pairs (transformations_fusion.mojo:
+// 879-908): contiguous pairs (or special pairs), then same-target runs
+int or_fuse(int32_t mode, const bf_op* in, int64_t nin, bf_op* out, int64_t out_cap, double* mats,
+            int64_t mats_cap, int64_t* nout, char* err, size_t errlen) {
+  try {
+    if (!nout || (nin > 0 && !in)) fail(BF_EINVAL, "null argument");
+    std::vector<Item> items;
+    for (int64_t i = 0; i < nin; ++i) {
+      const bf_op& o = in[i];
+      if (o.kind == BF_OP_GATE && (o.flags & BF_OPF_FUSE_WITH_NEXT) && i + 1 < nin) {
+        Item it;  // an existing fused pair passes through
+        it.kind = IT_PAIR;
+        it.op[0] = o;
+        it.op[1] = in[i + 1];
+        items.push_back(it);
+        ++i;
+      } else if (o.kind == BF_OP_GATE) {
+        items.push_back(gate_item(o));
+      } else {
+        Item it;
+        it.kind = IT_OTHER;
+        it.op[0] = o;
+        items.push_back(it);
+      }
+    }
+    items = same_target_runs(mode == 1 ? special_pairs(items) : contiguous_pairs(items, false));
+    int64_t k = 0, d = 0;
+    auto put = [&](const bf_op& o) {
+      if (k < out_cap && out) out[k] = o;
+      ++k;
+    };
+    for (const Item& it : items) {
+      if (it.kind == IT_GATE || it.kind == IT_OTHER) {
+        put(it.op[0]);
+      } else if (it.kind == IT_PAIR) {
+        put(it.op[0]);
+        put(it.op[1]);
+      } else {
+        bf_op o;
+        std::memset(&o, 0, sizeof o);
+        o.kind = it.kind == IT_UNITARY ? BF_OP_UNITARY : BF_OP_CUNITARY;
+        o.target = it.target;
+        o.target2 = it.m;
+        if (it.kind == IT_CUNITARY) {
+          o.controls = 1ull << it.control;
+          o.ncontrols = 1;
+        }
+        const int64_t need = 2 * (int64_t)it.u.size();
+        if (mats && d + need <= mats_cap) {
+          for (size_t e = 0; e < it.u.size(); ++e) {
+            mats[d + 2 * (int64_t)e] = it.u[e].re;
+            mats[d + 2 * (int64_t)e + 1] = it.u[e].im;
+          }
+          o.data = mats + d;
+        }
+        d += need;
+        put(o);
+      }
+    }
+    *nout = k;
+    if (k > out_cap || (mats_cap < d)) fail(BF_EINVAL, "output too small: %lld ops, %lld doubles needed",
+                                           (long long)k, (long long)d);
+    return BF_OK;
+  } catch (const OrError& e) {
+    set_err(err, errlen, e.msg);
+    return e.code;
+  }
 }
 
 }  // extern "C"

@@ -69,6 +69,19 @@ double or_norm2(int32_t n, const double* re, const double* im);
 /* Online host cores the parallel port would use. */
 int32_t or_num_cores(void);
 
+/* The reference's circuit fusion rewrites (butterfly/core/
+ * transformations_fusion.mojo:879-908) over op records: mode 0
+ * fuse_circuit (adjacent-qubit pairs into 4x4 unitaries, then same-target
+ * runs), mode 1 fuse_circuit_specialized_pairs (special pairs into fused
+ * pair records, then same-target runs).  Writes the rewritten records to
+ * out (at most out_cap) and the matrices of the unitaries they produce to
+ * mats (interleaved doubles, at most mats_cap; the records' data point
+ * there); *nout = records produced.  A second restatement beside the host
+ * mirror's, to check it. */
+int or_fuse(int32_t mode, const bf_op* in, int64_t nin, bf_op* out,
+            int64_t out_cap, double* mats, int64_t mats_cap, int64_t* nout,
+            char* err, size_t errlen);
+
 #ifdef __cplusplus
 }
 #endif

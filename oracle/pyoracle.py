@@ -45,6 +45,9 @@ def lib() -> C.CDLL:
         L.or_topk.restype = None
         L.or_num_cores.argtypes = []
         L.or_num_cores.restype = C.c_int32
+        L.or_fuse.argtypes = [C.c_int32, C.POINTER(F.bf_op), C.c_int64, C.POINTER(F.bf_op), C.c_int64, C.c_void_p,
+                              C.c_int64, C.POINTER(C.c_int64), C.c_char_p, C.c_size_t]
+        L.or_fuse.restype = C.c_int
         _lib = L
     return _lib
 
@@ -138,3 +141,32 @@ def bit_reverse_indices(n: int) -> np.ndarray:
 
 def num_cores() -> int:
     return int(lib().or_num_cores())
+
+
+FUSE_CIRCUIT, FUSE_SPECIALIZED_PAIRS = 0, 1
+
+
+def fuse(circuit, mode: int) -> list[dict]:
+    """The oracle's restatement of the reference's fusion rewrites applied to
+    `circuit`'s records: the rewritten records as dicts (field -> value;
+    'data' holds the unitary's complex matrix, row-major)."""
+    arr, cnt, keep = circuit.to_ops()
+    cap = 2 * cnt + 2
+    out = (F.bf_op * cap)()
+    mats = np.zeros(32 * cap, dtype=np.float64)
+    nout = C.c_int64()
+    err = C.create_string_buffer(512)
+    rc = lib().or_fuse(mode, arr, cnt, out, cap, mats.ctypes.data, mats.size, C.byref(nout), err, len(err))
+    del keep
+    if rc != 0:
+        raise OracleError(rc, err.value.decode())
+    res = []
+    for o in out[:nout.value]:
+        d = {"kind": o.kind, "gate": o.gate, "target": o.target, "target2": o.target2, "controls": o.controls,
+             "ncontrols": o.ncontrols, "flags": o.flags, "arg": o.arg, "mat": list(o.mat)}
+        if o.kind in (F.BF_OP_UNITARY, F.BF_OP_CUNITARY):
+            dim = 1 << o.target2
+            flat = np.ctypeslib.as_array(o.data, shape=(2 * dim * dim,)).copy()
+            d["data"] = flat[0::2] + 1j * flat[1::2]
+        res.append(d)
+    return res

@@ -129,3 +129,43 @@ def test_p_run_collapse_keeps_the_angle_sum_exactly():
         qc.p(0, a)
     (g,) = FU.fuse_same_target_gates(qc.transformations)
     assert g.gate_info.arg == (math.pi / 3 + math.pi / 7) + -0.2
+
+
+def records(qc):
+    """A circuit's records as the oracle's fuse() reports them."""
+    arr, cnt, keep = qc.to_ops()
+    out = []
+    for o in arr[:cnt]:
+        d = {"kind": o.kind, "gate": o.gate, "target": o.target, "target2": o.target2, "controls": o.controls,
+             "ncontrols": o.ncontrols, "flags": o.flags, "arg": o.arg, "mat": list(o.mat)}
+        if o.kind in (bfy.F.BF_OP_UNITARY, bfy.F.BF_OP_CUNITARY):
+            dim = 1 << o.target2
+            flat = np.ctypeslib.as_array(o.data, shape=(2 * dim * dim,)).copy()
+            d["data"] = flat[0::2] + 1j * flat[1::2]
+        out.append(d)
+    del keep
+    return out
+
+
+@pytest.mark.parametrize("build", [
+    lambda: W.encode_value_circuit(12, 4.7),
+    lambda: W.random_layered_circuit(11, 5, seed=2),
+    lambda: W.qft_circuit(10),
+    lambda: W.grover_circuit(6, 17),
+])
+@pytest.mark.parametrize("mode", [O.FUSE_CIRCUIT, O.FUSE_SPECIALIZED_PAIRS])
+def test_host_rewrite_equals_the_oracle_restatement(build, mode):
+    """The host mirror's rewrite and the oracle's independent restatement
+    produce the same records: kinds, qubits, flags and angles exactly, the
+    unitaries' matrices to the last bits of their products."""
+    qc = build()
+    fq = (FU.fuse_circuit if mode == O.FUSE_CIRCUIT else FU.fuse_circuit_specialized_pairs)(qc)
+    mine, theirs = records(fq), O.fuse(qc, mode)
+    assert len(mine) == len(theirs)
+    for a, b in zip(mine, theirs):
+        for key in ("kind", "target", "target2", "controls", "ncontrols", "flags"):
+            assert a[key] == b[key], (key, a, b)
+        if a["kind"] == bfy.F.BF_OP_GATE:
+            assert a["gate"] == b["gate"] and a["arg"] == b["arg"] and a["mat"] == b["mat"]
+        elif "data" in a:
+            assert np.max(np.abs(a["data"] - b["data"])) <= 1e-15
