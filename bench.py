@@ -62,10 +62,14 @@ def per_gate_bytes_in_S(qc) -> float:
     for tr in qc.transformations:
         pair = [tr.first, tr.second] if isinstance(tr, bfy.FusedPairTransformation) else [tr]
         for g in pair:
-            if not isinstance(g, bfy.GateTransformation):
-                raise ValueError(f"per-gate byte count covers gate transformations only, not {type(g).__name__}")
-            f = 1.0 if g.gate_info.kind in (bfy.GateKind.P, bfy.GateKind.Z) else 2.0
-            total += f / (1 << len(g.controls))
+            if isinstance(g, bfy.GateTransformation):
+                f = 1.0 if g.gate_info.kind in (bfy.GateKind.P, bfy.GateKind.Z) else 2.0
+                total += f / (1 << len(g.controls))
+            elif isinstance(g, (bfy.ClassicalTransformation, bfy.QubitReversalTransformation,
+                                bfy.UnitaryTransformation, bfy.SwapTransformation)):
+                total += 2.0  # a permutation or dense unitary rewrites the whole state once
+            else:
+                raise ValueError(f"no per-gate byte count for {type(g).__name__}")
     return total
 
 
@@ -417,8 +421,8 @@ def run_batch_bench(count: int, reps: int, sample: int) -> dict:
     rng = np.random.Generator(np.random.PCG64(8))
     out = {"circuits": count, "qubits": "uniform 8..20", "mix": "half random layered depth 20, half value encoding"}
     batches = {}
-    for dtype in ("c64", "c128"):
-        b = B.Batch(circs, dtype=dtype)
+
+    def timed(b):
         stream = torch.cuda.ExternalStream(b.stream_ptr())
         b.run()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -428,11 +432,25 @@ def run_batch_bench(count: int, reps: int, sample: int) -> dict:
         e1.record(stream)
         e1.synchronize()
         b.sync()
-        ms = e0.elapsed_time(e1) / reps
+        return e0.elapsed_time(e1) / reps
+
+    for dtype in ("c64", "c128"):
+        t0 = time.perf_counter()
+        b = B.Batch(circs, dtype=dtype)  # tile widths tuned at creation
+        create_s = time.perf_counter() - t0
+        ms = timed(b)
         st = b.stats()
+        tuning = b.tuning()
         out[dtype] = {"ms_per_batch": ms, "circuits_per_s": count / (ms * 1e-3), "tasks": st["tasks"],
                       "passes": st["passes"], "graph": st["graph"], "state_bytes": st["state_bytes"],
-                      "launches_per_batch": 2}
+                      "launches_per_batch": 2, "create_s": create_s,
+                      "tuned_widths": {str(r["qubits"]): r["width"] for r in tuning if r["chosen"]},
+                      "tuning_ms": {f'{r["qubits"]}q_w{r["width"]}': round(r["ms"], 3) for r in tuning}}
+        fixed = B.Batch(circs, dtype=dtype, tile_qubits=12)
+        fms = timed(fixed)
+        fixed.close()
+        out[dtype]["fixed_width12_circuits_per_s"] = count / (fms * 1e-3)
+        out[dtype]["tuned_over_fixed"] = fms / ms
         batches[dtype] = b
     idx = rng.choice(count, size=min(sample, count), replace=False)
     worst = 0.0
@@ -448,7 +466,7 @@ def run_batch_bench(count: int, reps: int, sample: int) -> dict:
     return out
 
 
-def run_serving_bench(rate: float, seconds: float, drain: float, slots: int) -> dict:
+def run_serving_bench(rate: float, seconds: float, drain: float, slots: int, capacity_seconds: float = 8.0) -> dict:
     """Poisson arrivals (seeded) of mixed circuits, qubits log-uniform in
     [10, 28] (Grover, value encoding, random layered depth 10..40), each
     returning its top-16 outcomes; complex64 and complex128 runs."""
@@ -462,6 +480,22 @@ def run_serving_bench(rate: float, seconds: float, drain: float, slots: int) -> 
         srv.close()
     c64, c128 = out["c64"]["circuits_per_s"], out["c128"]["circuits_per_s"]
     out["c64_over_c128_circuits_per_s"] = c64 / c128 if c128 else None
+    # capacity: the same mix with a fixed number of requests in flight
+    cap = {"inflight": 2 * slots, "window_s": capacity_seconds}
+    if capacity_seconds > 0:
+        for dtype in ("c64", "c128"):
+            srv = SV.Server(slots=slots)
+            cap[dtype] = SV.closed_loop_run(srv, reqs, 2 * slots, capacity_seconds, 60.0, dtype=dtype)
+            srv.close()
+        a, b = cap["c64"]["circuits_per_s"], cap["c128"]["circuits_per_s"]
+        cap["c64_over_c128_circuits_per_s"] = a / b if b else None
+        la, lb = cap["c64"]["large"]["per_s"], cap["c128"]["large"]["per_s"]
+        cap["c64_over_c128_large_per_s"] = la / lb if lb else None
+        # complex64 served results against complex128 ones on a sample of the
+        # mix (up to 22 qubits)
+        sample = [r for r in reqs if r[1].num_qubits <= 22][:48]
+        cap["c64_vs_c128_top16"] = SV.top_probability_gap(sample)
+    out["capacity"] = cap
     return out
 
 
@@ -620,6 +654,7 @@ def run_ours(args) -> None:
     st.sync()
     barrier(world)
     st.launch_count(reset=True)
+    st.digit_tiles(reset=True)
     st.pass_timing(True)
     st.pass_times()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -631,6 +666,7 @@ def run_ours(args) -> None:
         e1.record(stream)
         e1.synchronize()
     launches = st.launch_count()
+    five_tiles, six_tiles = st.digit_tiles()
     pass_times = st.pass_times()
     st.pass_timing(False)
     ms = e0.elapsed_time(e1)
@@ -722,7 +758,7 @@ def run_ours(args) -> None:
     value_enc = (run_value_encoding_bench([20, 22, 24], [25], cpu=args.cpu_gates > 0)
                  if args.value_encoding and rank == 0 else None)
     batch = run_batch_bench(args.batch_count, 3, 256) if args.batch_count > 0 else None
-    serving = (run_serving_bench(args.serve_rate, args.serve_seconds, args.serve_seconds, 12)
+    serving = (run_serving_bench(args.serve_rate, args.serve_seconds, args.serve_seconds, 12, args.capacity_seconds)
                if args.serve_seconds > 0 else None)
     precision = (run_precision_bench(args.precision_qubits, args.precision_qubits - 1, LAYERS)
                  if args.precision_qubits > 0 and rank == 0 else None)
@@ -738,14 +774,16 @@ def run_ours(args) -> None:
         return
     value = pg_bytes * world / (ms_step * 1e-3) / 1e9
     digits = plan["block_passes"] > 0
-    arith = ("exact base-256 digit products on bf16 tensor cores (48-bit fixed point per block pass) and "
-             "double-float tile passes" if digits else "double-float arithmetic")
+    arith = ("exact base-256 digit products on bf16 tensor cores (per 4096-amplitude tile: a power-of-two scale "
+             "from the tile's norm and five or six digits, rounding unit at most 2^-48 of the state's scale per "
+             "block pass) and double-float tile passes" if digits else "double-float arithmetic")
     line = {
         "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fixed48+df64" if digits else "df64", "data": "synthetic",
         "config": workload_config(world),
-        "engine": {"arithmetic": f"FP64 storage; {arith}", "tile_qubits": K, "tensor_blocks": digits},
+        "engine": {"arithmetic": f"FP64 storage; {arith}", "tile_qubits": K, "tensor_blocks": digits,
+                   "digit_tiles_timed": {"five_digits": five_tiles, "six_digits": six_tiles}},
         "hbm": hbm_figure(plan, n, ms_step, world),
         "gate_passes_per_s": len(qc.transformations) * world / (ms_step * 1e-3),
         "circuits_per_s": world / (ms_step * 1e-3),
@@ -792,6 +830,8 @@ def main():
                     help="time the reference's value-encoding workload at 20/22/24 qubits and fused at 25 (0: skip)")
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--serve-rate", type=float, default=2000.0)
+    ap.add_argument("--capacity-seconds", type=float, default=8.0,
+                    help="closed-loop serving capacity run per dtype (0: skip)")
     ap.add_argument("--precision-qubits", type=int, default=33,
                     help="complex64 tensor-core vs CUDA-core run at this size (0: skip); fidelity at one qubit less")
     ap.add_argument("--qubits", type=int, default=N_QUBITS,

@@ -134,6 +134,9 @@ SIGNATURES = {
     "bf_server_stats": [C.c_void_p, C.POINTER(bf_server_counters)],
     "bf_server_destroy": [C.c_void_p],
     "bf_norm2_noalloc": [C.c_void_p, C.c_uint64, C.c_int32, C.c_void_p, C.c_void_p],
+    "bf_batch_tuning": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                        C.POINTER(C.c_int32)],
+    "bf_state_digit_tiles": [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.c_int32],
     "bf_validate": [C.c_int32, C.POINTER(bf_op), C.c_int64],
     "bf_plan_stats": [C.c_int32, C.POINTER(bf_op), C.c_int64, C.POINTER(bf_exec_opts), C.POINTER(C.c_int64),
                       C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_double), C.POINTER(C.c_int64),

@@ -50,6 +50,19 @@ class Batch:
         return {"tasks": t.value, "passes": p.value, "state_bytes": b.value, "graph": bool(g.value),
                 "launches": l.value}
 
+    def tuning(self) -> list[dict]:
+        """The autotuning record: per qubit count, each candidate tile width
+        with the time of one run of the sample, and which was chosen."""
+        cnt = C.c_int32()
+        F.check(F.lib().bf_batch_tuning(self._h, None, None, None, None, 0, C.byref(cnt)))
+        m = cnt.value
+        q, w, c = (np.zeros(max(m, 1), dtype=np.int32) for _ in range(3))
+        ms = np.zeros(max(m, 1), dtype=np.float64)
+        F.check(F.lib().bf_batch_tuning(self._h, q.ctypes.data, w.ctypes.data, ms.ctypes.data, c.ctypes.data, m,
+                                        C.byref(cnt)))
+        return [{"qubits": int(q[r]), "width": int(w[r]), "ms": float(ms[r]), "chosen": bool(c[r])}
+                for r in range(m)]
+
     def stream_ptr(self) -> int:
         s = C.c_void_p()
         F.check(F.lib().bf_batch_stream(self._h, C.byref(s)))

@@ -717,6 +717,13 @@ class QuantumState:
         F.check(F.lib().bf_state_pass_times(self.handle, cnt.ctypes.data, ms.ctypes.data))
         return {k: (int(cnt[i]), float(ms[i])) for i, k in enumerate(self.PASS_CLASSES) if cnt[i]}
 
+    def digit_tiles(self, reset: bool = False) -> tuple[int, int]:
+        """(five-digit, six-digit) tiles of the complex128 digit passes run on
+        this state; waits for the state's stream."""
+        five, six = C.c_uint64(), C.c_uint64()
+        F.check(F.lib().bf_state_digit_tiles(self.handle, C.byref(five), C.byref(six), 1 if reset else 0))
+        return five.value, six.value
+
     def close(self) -> None:
         if getattr(self, "_h", None):
             F.lib().bf_state_destroy(self._h)

@@ -70,6 +70,14 @@ void host_retire(State& st, void* p) {
   if (p) st.retired_host.push_back(p);
 }
 
+unsigned long long* digit_tile_counters(State& st) {
+  if (!st.d_digit_tiles) {
+    st.d_digit_tiles = static_cast<unsigned long long*>(dev_alloc(st, 2 * sizeof(unsigned long long)));
+    BF_CUDA(cudaMemsetAsync(st.d_digit_tiles, 0, 2 * sizeof(unsigned long long), st.stream));
+  }
+  return st.d_digit_tiles;
+}
+
 int* state_flag(State& st) {
   if (!st.d_flag) {
     st.d_flag = static_cast<int*>(dev_alloc(st, 16));
@@ -784,6 +792,7 @@ void release_state_members(State& st) {
     dev_free(st, st.d_flag);
     dev_free(st, st.d_aux);
     dev_free(st, st.d_scale);
+    dev_free(st, st.d_digit_tiles);
     cudaStreamSynchronize(st.stream);
   }
   delete st.plans;
@@ -1088,6 +1097,22 @@ int bf_state_pass_times(bf_state* hst, int64_t* counts, double* ms) {
   });
 }
 
+int bf_state_digit_tiles(bf_state* hst, uint64_t* five, uint64_t* six, int32_t reset) {
+  State* st = S_(hst);
+  return guarded([&]() {
+    if (!st || !five || !six) fail(BF_EINVAL, "null argument");
+    DeviceGuard dg(st->device);
+    unsigned long long h[2] = {0, 0};
+    if (st->d_digit_tiles) {
+      BF_CUDA(cudaMemcpyAsync(h, st->d_digit_tiles, sizeof h, cudaMemcpyDeviceToHost, st->stream));
+      if (reset) BF_CUDA(cudaMemsetAsync(st->d_digit_tiles, 0, sizeof h, st->stream));
+      BF_CUDA(cudaStreamSynchronize(st->stream));
+    }
+    *five = h[0];
+    *six = h[1];
+  });
+}
+
 int bf_execute(bf_state* hst, const bf_op* ops, int64_t nops, const bf_exec_opts* opts) {
   State* st = S_(hst);
   return guarded([&]() {
@@ -1200,6 +1225,14 @@ int bf_batch_stats(bf_batch* h, int64_t* tasks, int64_t* passes, uint64_t* state
   return guarded([&]() {
     if (!h) fail(BF_EINVAL, "batch is null");
     batch_stats(*B_(h), tasks, passes, state_bytes, graph, launches);
+  });
+}
+
+int bf_batch_tuning(bf_batch* h, int32_t* qubits, int32_t* widths, double* ms, int32_t* chosen, int32_t cap,
+                    int32_t* count) {
+  return guarded([&]() {
+    if (!h || !count) fail(BF_EINVAL, "null argument");
+    batch_tuning(*B_(h), qubits, widths, ms, chosen, cap, count);
   });
 }
 

@@ -138,6 +138,11 @@ __global__ void k_batch_basis<float2>(float2* pool, const uint64_t* offsets, int
   if (c < ncirc) pool[offsets[c]] = make_float2(1.0f, 0.0f);
 }
 
+struct BatchTuneRow {
+  int32_t qubits, width, circuits, chosen;
+  double ms;  // one run of the sample batch
+};
+
 struct Batch {
   int device = 0, num_sms = 0;
   int dtype = BF_C64, prec = PREC_F32;
@@ -161,6 +166,9 @@ struct Batch {
   cudaStream_t stream = nullptr;
   cudaGraphExec_t graph = nullptr;
   uint64_t launches = 0;
+  // autotuning record: per qubit count, the candidate tile widths timed on a
+  // sample of the batch's circuits of that size, and the width chosen
+  std::vector<BatchTuneRow> tuning;
   size_t amp_bytes() const { return dtype == BF_C128 ? 16 : 8; }
 };
 
@@ -252,8 +260,12 @@ static void dev_upload(T** dst, const std::vector<T>& v) {
   if (!v.empty()) BF_CUDA(cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
 }
 
-Batch* batch_create(int ncirc, const int32_t* nq, const bf_op* const* ops, const int64_t* nops, int dtype,
-                    const bf_exec_opts& o, int prec) {
+// Builds a batch whose circuits of n qubits use tiles of up to width_of_n[n]
+// qubits; the kernel's shared memory is at least smem_floor (so that sample
+// batches run at the occupancy of the widest candidate); `capture` records
+// the run into a CUDA graph.
+static Batch* build_batch(int ncirc, const int32_t* nq, const bf_op* const* ops, const int64_t* nops, int dtype,
+                          const bf_exec_opts& o, int prec, const int* width_of_n, size_t smem_floor, bool capture) {
   if (ncirc < 1) fail(BF_EINVAL, "a batch needs at least one circuit");
   if (!nq || !ops || !nops) fail(BF_EINVAL, "null argument");
   Batch* b = new Batch();
@@ -263,7 +275,6 @@ Batch* batch_create(int ncirc, const int32_t* nq, const bf_op* const* ops, const
     b->ncirc = ncirc;
     BF_CUDA(cudaGetDevice(&b->device));
     BF_CUDA(cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, b->device));
-    const int Kcap = o.tile_qubits > 0 ? o.tile_qubits : 12;
     std::vector<BatchPass> passes;
     std::vector<TileOp> prog;
     // per circuit: passes (each with its tile count)
@@ -284,7 +295,7 @@ Batch* batch_create(int ncirc, const int32_t* nq, const bf_op* const* ops, const
       b->nq.push_back(n);
       b->offsets.push_back(off);
       off += ((1ull << n) + 31) & ~31ull;  // 256-byte aligned starts
-      int K = std::min(n, Kcap);
+      int K = std::min(n, width_of_n[n]);
       for (auto& ps : plan_gates(n, gates, K, /*allow_single=*/false)) {
         BatchPass bp;
         std::memset(&bp, 0, sizeof bp);
@@ -307,7 +318,7 @@ Batch* batch_create(int ncirc, const int32_t* nq, const bf_op* const* ops, const
       }
     }
     b->pool_amps = off;
-    b->smem = std::max<size_t>(smem, kTileThreads * sizeof(double));  // the norm stage reduces in it
+    b->smem = std::max<size_t>(std::max(smem, smem_floor), kTileThreads * sizeof(double));  // the norm stage reduces in it
     // tasks, pass-major
     std::vector<BatchTask> tasks;
     size_t max_p = 0;
@@ -360,7 +371,7 @@ Batch* batch_create(int ncirc, const int32_t* nq, const bf_op* const* ops, const
     // capture one run into a graph; if this stack cannot capture it, runs
     // are enqueued directly
     cudaGraph_t g = nullptr;
-    if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+    if (capture && cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
       bool ok = true;
       try {
         enqueue(*b);
@@ -381,6 +392,130 @@ Batch* batch_create(int ncirc, const int32_t* nq, const bf_op* const* ops, const
     throw;
   }
   return b;
+}
+
+// Batch autotuning.  The candidates are tile widths 8..12 (at most n).  For
+// each qubit count n of the batch, a sample of its circuits of that size
+// (repeated when there are fewer, sized so that the sample fills the GPU as
+// the whole batch does) runs once per candidate, every candidate at the shared memory of the widest one, and
+// the width with the shortest run is kept.  This is the counterpart of the
+// reference's tunable grid split (grid_col_bits, executors.mojo:213-228),
+// chosen by measurement instead of a fixed rule.
+constexpr int kTuneSample = 192;
+constexpr int kTuneMinWidth = 8, kTuneMaxWidth = 12;
+
+template <class P>
+static size_t tile_smem_of(int K) {
+  return tile_smem_bytes<P>(K, std::min(K - 1, kTileLowQubits));
+}
+
+static double time_batch(Batch& b) {
+  cudaEvent_t e0, e1;
+  BF_CUDA(cudaEventCreate(&e0));
+  BF_CUDA(cudaEventCreate(&e1));
+  float best = 0.f;
+  try {
+    batch_run(b, true);  // warm-up
+    for (int r = 0; r < 2; ++r) {
+      BF_CUDA(cudaEventRecord(e0, b.stream));
+      batch_run(b, false);
+      BF_CUDA(cudaEventRecord(e1, b.stream));
+      batch_sync(b);
+      float ms = 0.f;
+      BF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      best = r == 0 ? ms : std::min(best, ms);
+    }
+  } catch (...) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    throw;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return best;
+}
+
+static void tune_widths(int ncirc, const int32_t* nq, const bf_op* const* ops, const int64_t* nops, int dtype,
+                        const bf_exec_opts& o, int prec, int* width_of_n, std::vector<BatchTuneRow>& rows) {
+  size_t floor = 0;
+  switch (prec) {
+    case PREC_F64: floor = tile_smem_of<PolF64>(kTuneMaxWidth); break;
+    case PREC_DF: floor = tile_smem_of<PolDF>(kTuneMaxWidth); break;
+    default: floor = tile_smem_of<PolF32>(kTuneMaxWidth); break;
+  }
+  for (int n = 1; n <= 30; ++n) {
+    std::vector<int> members;
+    for (int c = 0; c < ncirc; ++c)
+      if (nq[c] == n) members.push_back(c);
+    if (members.empty() || n <= kTuneMinWidth) continue;
+    // enough circuits that a pass level holds about 4096 tiles of 2^8
+    // amplitudes, 16 to kTuneSample of them
+    const int sample = std::max(16, std::min(kTuneSample, 4096 >> std::min(n - kTuneMinWidth, 12)));
+    std::vector<int32_t> snq;
+    std::vector<const bf_op*> sops;
+    std::vector<int64_t> snops;
+    for (int k = 0; k < sample; ++k) {
+      const int c = members[(size_t)k % members.size()];
+      snq.push_back(n);
+      sops.push_back(ops[c]);
+      snops.push_back(nops[c]);
+    }
+    double best = 0;
+    int best_w = width_of_n[n];
+    const size_t first = rows.size();
+    for (int w = kTuneMinWidth; w <= std::min(n, kTuneMaxWidth); ++w) {
+      int widths[31];
+      for (int m = 0; m <= 30; ++m) widths[m] = w;
+      Batch* t = build_batch(sample, snq.data(), sops.data(), snops.data(), dtype, o, prec, widths, floor, false);
+      double ms = 0;
+      try {
+        ms = time_batch(*t);
+      } catch (...) {
+        free_batch(t);
+        throw;
+      }
+      free_batch(t);
+      rows.push_back(BatchTuneRow{n, w, sample, 0, ms});
+      if (w == kTuneMinWidth || ms < best) {
+        best = ms;
+        best_w = w;
+      }
+    }
+    width_of_n[n] = best_w;
+    for (size_t r = first; r < rows.size(); ++r) rows[r].chosen = rows[r].width == best_w ? 1 : 0;
+  }
+}
+
+Batch* batch_create(int ncirc, const int32_t* nq, const bf_op* const* ops, const int64_t* nops, int dtype,
+                    const bf_exec_opts& o, int prec) {
+  if (ncirc < 1) fail(BF_EINVAL, "a batch needs at least one circuit");
+  if (!nq || !ops || !nops) fail(BF_EINVAL, "null argument");
+  // widths: the caller's, or 12 refined by measurement (o.tile_qubits == 0)
+  int width_of_n[31];
+  for (int m = 0; m <= 30; ++m) width_of_n[m] = o.tile_qubits > 0 ? o.tile_qubits : 12;
+  std::vector<BatchTuneRow> rows;
+  if (o.tile_qubits == 0) {
+    for (int c = 0; c < ncirc; ++c) {
+      if (nq[c] < 1 || nq[c] > 30) fail(BF_EINVAL, "circuit %d: num_qubits must be in [1, 30], got %d", c, nq[c]);
+      validate_ops(nq[c], ops[c], nops[c]);
+    }
+    tune_widths(ncirc, nq, ops, nops, dtype, o, prec, width_of_n, rows);
+  }
+  Batch* b = build_batch(ncirc, nq, ops, nops, dtype, o, prec, width_of_n, 0, true);
+  b->tuning = std::move(rows);
+  return b;
+}
+
+void batch_tuning(const Batch& b, int32_t* qubits, int32_t* widths, double* ms, int32_t* chosen, int32_t cap,
+                  int32_t* count) {
+  const int32_t m = (int32_t)b.tuning.size();
+  if (count) *count = m;
+  for (int32_t r = 0; r < m && r < cap; ++r) {
+    if (qubits) qubits[r] = b.tuning[r].qubits;
+    if (widths) widths[r] = b.tuning[r].width;
+    if (ms) ms[r] = b.tuning[r].ms;
+    if (chosen) chosen[r] = b.tuning[r].chosen;
+  }
 }
 
 void batch_run(Batch& b, bool sync) {

@@ -255,6 +255,8 @@ struct State {
   size_t aux_cap = 0;
   // scale exponent of the complex128 digit passes (device int)
   int* d_scale = nullptr;
+  // digit passes' tiles run with five and with six digits (device u64 x 2)
+  unsigned long long* d_digit_tiles = nullptr;
   // recent plans and the one whose program is on the device
   PlanCache* plans = nullptr;
   uint64_t uploaded_plan = 0;
@@ -299,6 +301,8 @@ void launch_block_pass(State& st, const Blk5* d_blocks, int nblocks, const unsig
 void launch_block_pass_digits(State& st, const Blk5* d_blocks, int nblocks, const unsigned char* d_images,
                               const uint16_t* d_offsets, const TilePass& p, const int* d_exp);
 void launch_digit_scale(State& st, int* d_exp);
+// the device counters of five- and six-digit tiles (allocated and zeroed on first use)
+unsigned long long* digit_tile_counters(State& st);
 void launch_norm2_partials(State& st, unsigned blocks);  // into st.d_partial (ensure_partials first)
 void launch_bitrev_full(State& s);
 void launch_permute(State& s, const int32_t* src_bit_of_dst);  // dst bit j <- src bit perm[j]
@@ -367,6 +371,8 @@ void batch_stats(const Batch& b, int64_t* tasks, int64_t* passes, uint64_t* stat
                  uint64_t* launches);
 void* batch_stream(const Batch& b);
 int batch_device(const Batch& b);
+void batch_tuning(const Batch& b, int32_t* qubits, int32_t* widths, double* ms, int32_t* chosen, int32_t cap,
+                  int32_t* count);
 
 // Wire formats (wire.cpp).
 struct OpList;

@@ -35,6 +35,7 @@
 // waits (bounded) for its own copy in flight, frees its tensor memory and
 // returns.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 
 #include "amp_math.cuh"
@@ -355,47 +356,65 @@ __global__ void __launch_bounds__(kBlkThreads, 2) k_tblock(const BlkPassArgs a) 
 }
 
 // ---- complex128: digit blocks on the bf16 tensor cores -----------------------
-// A complex128 value x becomes 6 signed base-256 digits, x / scale =
-// 2^-8 sum_i d_i 2^-8i with d_i integers of at most 8 bits plus sign, each
-// exact in bf16; the matrix likewise (r = 2^-8 sum_j e_j 2^-8j).  For every
-// digit level s = i + j <= 6 the 4 MMAs of each pair (i, j) (kind::f16, bf16
-// inputs, K = 16) accumulate sum_K d_i e_j into one FP32 accumulator; every
-// product and partial sum is an integer below 2^24, so the accumulation is
-// exact whatever the order.  The epilogue turns the 7 level sums back into
-// the next block's digits by carries between levels (FP32 on exact
-// integers), or after the last block into the FP64 result.  scale is a power
-// of two at least twice the state's norm, so every amplitude of a unitary
-// circuit stays below scale / 2; a pass runs in this form only when all its
-// blocks are unitary.  Dropping the levels s >= 7 and rounding below the
-// sixth digit leave errors of about 2^-48 scale per block.
+// A complex128 value x of a tile becomes D signed base-256 digits, x / s_t =
+// 2^-8 sum_i d_i 2^-8i (i < D) with d_i integers of at most 8 bits plus
+// sign, each exact in bf16; the matrix likewise as six digits (r = 2^-8
+// sum_j e_j 2^-8j).  For every digit level s = i + j <= D the 4 MMAs of each
+// kept pair (i, j) (kind::f16, bf16 inputs, K = 16) accumulate sum_K d_i e_j
+// into one FP32 accumulator; every product and partial sum is an integer
+// below 2^24, so the accumulation is exact whatever the order.  The
+// epilogue turns the D + 1 level sums back into the next block's digits by
+// carries between levels (FP32 on exact integers), or after the last block
+// into the FP64 result.
+//
+// The scale s_t = 2^e_t is the tile's own: a block pass mixes amplitudes
+// only within a tile, so the tile's norm is the same after every block, and
+// s_t >= 2 ||tile|| keeps every value below s_t / 2 through the pass.  The
+// bound comes from an exact integer sum over the tile (sq_bound), so it does
+// not depend on the order of the reduction.  A tile takes D = 5 digits (20
+// digit pairs) when e_t is at least 8 below the state's exponent e_g (s_g =
+// 2^e_g >= 2 ||state||, from the norm before the first digit pass), so its
+// rounding unit 2^-40 s_t is no coarser than six digits at the state's
+// scale; otherwise D = 6 (26 pairs) at min(e_t, e_g).  The choice is
+// uniform within a CTA's tile.  Dropping the levels s > D and rounding
+// below the last digit leave errors of about one unit of 2^-8D s_t per
+// block.  A pass runs in this form only when all its blocks are unitary.
 constexpr uint32_t kDgPlane = 16384;                       // 128 rows x 64 bf16
-constexpr uint32_t kDgSmemB = kDigits * kDgPlane;          // 6 A planes, then B
+constexpr uint32_t kDgSmemB = kDigits * kDgPlane;          // 6 A planes (5 used by five-digit tiles), then B
 constexpr uint32_t kDgSmemHoff = kDgSmemB + 2 * kDigitImageBytes;  // two image buffers
-constexpr uint32_t kDgSmemBar = kDgSmemHoff + 128 * 8;  // 2 image barriers, 7 level barriers, tmem slot
-constexpr uint32_t kDgSmemBlk = kDgSmemBar + 128;             // the pass's block descriptors
+constexpr uint32_t kDgSmemBar = kDgSmemHoff + 128 * 8;  // 2 image barriers, 1 MMA barrier, tmem slot
+constexpr uint32_t kDgSmemRed = kDgSmemBar + 128;       // 32 x u64: the tile norm bound per warp
+constexpr uint32_t kDgSmemBlk = kDgSmemRed + 256;       // the pass's block descriptors
 static_assert(sizeof(Blk5) == 32 && kDgSmemBlk % 16 == 0, "block descriptors are copied as 16-byte words");
 constexpr uint32_t kDgSmemUsed = kDgSmemBlk + kMaxPassBlocks * sizeof(Blk5);
 constexpr uint32_t kDgSmemAlloc = kDgSmemUsed + 1024;
-constexpr uint32_t kDgTmemCols = 512;                      // 7 levels x 64 columns
-constexpr int kDgLevels = 7;
+constexpr uint32_t kDgTmemCols = 512;                      // up to 7 levels x 64 columns
 constexpr int kDgThreads = kDigitThreads;                  // 32 warps: 8 per 32-lane group of D
 constexpr int kDgCols = 64 / (kDgThreads / 128);           // FP32 columns of a level per warp
 constexpr int kDgCplx = kDgCols / 2;                       // complex results per thread per block
 constexpr int kDgLoadIters = 4096 / (2 * kDgThreads);      // amplitude pairs per thread per tile
+constexpr int kDgFewDigits = 5;                            // digits of a tile with a small norm
+constexpr int kDgFewDigitsSlack = 8;                       // e_t <= e_g - 8 for five digits
 static_assert(kDgCols == 8 && kDgLoadIters * 2 == kBlockTableEntries / kDgThreads, "digit kernel thread layout");
 
-// The MMA groups of one block: A plane i against B planes j0 .. j0+nj-1
-// (i + j <= 6: the 26 digit pairs kept), in issue order.
+// The MMA groups of one block: A plane i against B planes j0 .. j0+nj-1, in
+// issue order; the first group to reach a level initialises it.  Six
+// digits: the 26 pairs with i + j <= 6.  Five digits: the 20 pairs with
+// i <= 4, j <= 5, i + j <= 5.
 struct DgGroup {
   int i, j0, nj, init;
 };
-#define BF_DG_GROUPS                                                                                  \
+#define BF_DG_GROUPS6                                                                                 \
   {                                                                                                   \
     {0, 0, 4, 1}, {0, 4, 2, 1}, /* levels 0..5 first written */                                       \
         {1, 5, 1, 1},           /* level 6 first written */                                           \
         {1, 0, 4, 0}, {1, 4, 1, 0}, {2, 0, 4, 0}, {2, 4, 1, 0}, {3, 0, 4, 0}, {4, 0, 3, 0}, {5, 0, 2, 0} \
   }
-constexpr int kDgGroups = 10;
+#define BF_DG_GROUPS5                                                                                 \
+  {                                                                                                   \
+    {0, 0, 4, 1}, {0, 4, 2, 1}, /* levels 0..5 first written */                                       \
+        {1, 0, 4, 0}, {1, 4, 1, 0}, {2, 0, 4, 0}, {3, 0, 3, 0}, {4, 0, 2, 0}                          \
+  }
 
 // 8 columns of the thread's TMEM lane
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
@@ -428,9 +447,11 @@ struct DgPassArgs {
   uint64_t ntiles;
   int32_t nblocks;
   int32_t q[kBlockTileQubits];
-  const int* scale_exp;         // device: scale = 2^scale_exp
+  const int* scale_exp;         // device: the state's scale 2^e_g
   int* flag;
   uint32_t spin_limit;
+  int32_t few_digits_slack;     // five digits when e_t <= e_g - slack
+  unsigned long long* digit_tiles;  // optional: [0] five-digit tiles, [1] six-digit tiles (counted per CTA)
 };
 
 __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
@@ -492,33 +513,47 @@ __device__ __forceinline__ float byte_digit(uint32_t w, int j) {
   return __int_as_float((int)__byte_perm(w, 0x4B400000u, 0x7640u + (uint32_t)j)) - 12583040.0f;
 }
 
-// V = round(x * 2^sh), |V| < 2^47, as 6 balanced base-256 digits d (d[5]
-// the lowest): with W = V + 0x808080808080 every byte of W is its digit plus
-// 128 (the added 128s absorb the borrows), and the top digit is W / 2^40 -
-// 128.  False when |x * 2^sh| >= 2^47 (the scale does not cover x).
+// V = round(x * 2^sh) to nearest, ties to even, |V| < 2^(8D - 1), as D
+// balanced base-256 digits d (d[D-1] the lowest).  Ties are frequent: a value
+// written by an earlier pass at one tile's scale is exact at that scale, and
+// a tile of this pass may have a coarser one, so the dropped bits are often
+// exactly one half; rounding them to even keeps the rounding unbiased (away
+// from zero would grow every such magnitude, and the norm with them).
+// With W = V + 128 (1 + 2^8 + ... + 2^(8(D-1))) every
+// byte of W is its digit plus 128 (the added 128s absorb the borrows), and
+// the top digit is W / 2^(8(D-1)) - 128.  False when |x * 2^sh| >= 2^(8D-1)
+// (the scale does not cover x).
+template <int D>
 __device__ __forceinline__ bool digits_of(double x, int sh, float* d) {
+  static_assert(D == 5 || D == 6, "five or six digits");
   const long long b = __double_as_longlong(x);
   const int ex = (int)((uint32_t)(b >> 52) & 0x7ffu);
   const int k = ex - 1075 + sh;  // |x| 2^sh = m 2^k
   long long V = 0;
   bool ok = true;
   if (ex != 0 && k > -64) {
-    if (k > -6) {
+    if (k > 8 * D - 54) {
       ok = false;
     } else {
       const long long m = (b & 0x000FFFFFFFFFFFFFll) | 0x0010000000000000ll;
-      V = (m + (1ll << (-k - 1))) >> (-k);
+      // add half - 1 plus the kept low bit: rounds up above one half, and at
+      // exactly one half only when the kept part is odd
+      V = (m + (1ll << (-k - 1)) - 1 + ((m >> (-k)) & 1)) >> (-k);
     }
   }
   if (b < 0) V = -V;
-  const unsigned long long W = (unsigned long long)(V + 0x808080808080ll);
+  const unsigned long long W = (unsigned long long)(V + (D == 6 ? 0x808080808080ll : 0x8080808080ll));
   const uint32_t wl = (uint32_t)W, wh = (uint32_t)(W >> 32);
-  d[5] = byte_digit(wl, 0);
-  d[4] = byte_digit(wl, 1);
-  d[3] = byte_digit(wl, 2);
-  d[2] = byte_digit(wl, 3);
-  d[1] = byte_digit(wh, 0);
-  d[0] = __int_as_float((int)(0x4B400000u | (wh >> 8))) - 12583040.0f;
+  d[D - 1] = byte_digit(wl, 0);
+  d[D - 2] = byte_digit(wl, 1);
+  d[D - 3] = byte_digit(wl, 2);
+  d[D - 4] = byte_digit(wl, 3);
+  if (D == 6) {
+    d[1] = byte_digit(wh, 0);
+    d[0] = __int_as_float((int)(0x4B400000u | (wh >> 8))) - 12583040.0f;
+  } else {
+    d[0] = __int_as_float((int)(0x4B400000u | wh)) - 12583040.0f;
+  }
   return ok;
 }
 
@@ -534,17 +569,259 @@ __device__ __forceinline__ double double_of(long long V, int e) {
   return __longlong_as_double((long long)(sgn | ((unsigned long long)E << 52) | mant));
 }
 
+// An integer upper bound of x^2 in units of 2^(2 eg - 50): with ex the
+// biased exponent of x and m8 its top 8 mantissa bits, |x| < (257 + m8)
+// 2^(ex - 1031), so x^2 < (257 + m8)^2 2^k units with k = 2 (ex - eg) -
+// 2012, rounded up.  Zero gives 0, a subnormal 1.  |x| < 2^(eg - 1) makes
+// k <= 30, so a tile's sum stays below 2^62; integer sums are exact and
+// independent of the order of the reduction.
+__device__ __forceinline__ unsigned long long sq_bound(double x, int eg) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+  if (b == 0) return 0;
+  const int ex = (int)(b >> 52);
+  if (ex == 0) return 1;
+  const uint32_t u = 257u + (uint32_t)((b >> 44) & 255u);
+  const unsigned long long u2 = (unsigned long long)(u * u);
+  const int k = 2 * (ex - eg) - 2012;
+  if (k >= 0) return u2 << (k < 30 ? k : 30);
+  if (k <= -19) return 1;
+  return (u2 + (1ull << -k) - 1) >> -k;
+}
+
+// The tile's scale exponent e_t from its bound S (units 2^(2 eg - 50)):
+// ||tile||^2 <= S 2^(2 eg - 50) < 2^(L + 2 eg - 50) with L the bit length of
+// S, so 2^(2 e_t) >= 4 ||tile||^2 holds when 2 e_t >= L + 2 eg - 48, i.e.
+// for e_t = eg - 24 + ceil(L / 2).
+__device__ __forceinline__ int tile_scale_exp(unsigned long long S, int eg) {
+  const int L = S ? 64 - __clzll((long long)S) : 0;
+  return eg - 24 + ((L + 1) >> 1);
+}
+
+template <int D>
+__device__ __forceinline__ DgGroup dg_group(int gi) {
+  if constexpr (D == 6) {
+    constexpr DgGroup g[10] = BF_DG_GROUPS6;
+    return g[gi];
+  } else {
+    constexpr DgGroup g[7] = BF_DG_GROUPS5;
+    return g[gi];
+  }
+}
+template <int D>
+constexpr int kDgGroupCount = D == 6 ? 10 : 7;
+
+// The CTA's pipeline state, carried from tile to tile.  Block k of the CTA
+// (counting every tile's blocks) uses image buffer k & 1, whose barrier is
+// then in its phase (k >> 1) & 1, and the MMA barrier in phase k & 1.
+struct DgPipe {
+  uint32_t kimg;       // blocks this CTA has run
+  int b_in_flight;     // thread 0: image loads not yet waited for (by buffer bit)
+  bool issued;         // thread 0: MMAs issued for the current block
+  int mma_lost_phase;  // thread 0: MMA phase whose wait expired
+  bool range_ok;
+};
+
+// What every tile of the launch shares.
+struct DgFixed {
+  unsigned char* sm;
+  const Blk5* blk;
+  const uint64_t* hoff;
+  uint32_t sA, sB, tmem, tlane, bar_b, bar_mma, idesc_base;
+  uint64_t free_pos, grid_base;  // next tile's base: ((base | ~free_pos) + grid_base) & free_pos
+};
+
+// One tile in D digits at scale 2^e: the loaded values v into the A planes,
+// the pass's blocks, the FP64 results back to the state.  False when a
+// bounded wait expired (the CTA then stops).
+template <int D>
+__device__ __forceinline__ bool dg_tile(const DgPassArgs& a, const DgFixed& f, DgPipe& p, const double2* v,
+                                        const uint2& load_dest, uint64_t obase, bool has_next, int e) {
+  const int tid = threadIdx.x;
+  const int sh = 8 * D - e;  // x / 2^e * 2^(8D) = x * 2^sh
+  unsigned char* sm = f.sm;
+#pragma unroll
+  for (int el = 0; el < 2 * kDgLoadIters; ++el) {
+    float dr[D], di[D];
+    p.range_ok &= digits_of<D>(v[el].x, sh, dr);
+    p.range_ok &= digits_of<D>(v[el].y, sh, di);
+    const uint32_t off = dest_at4(load_dest, el) << 2;
+#pragma unroll
+    for (int q = 0; q < D; ++q)
+      *reinterpret_cast<uint32_t*>(sm + (uint32_t)q * kDgPlane + off) = pack_bf16(dr[q], di[q]);
+  }
+  fence_proxy_async();
+  __syncthreads();
+
+  for (int bi = 0; bi < a.nblocks; ++bi) {
+    const bool more = bi + 1 < a.nblocks;
+    const uint2 dest = my_dests4(a.offsets, f.blk[bi].offs);
+    bool lost = false;
+    const uint32_t kb = p.kimg & 1u;
+    const uint32_t ph_mma = p.kimg & 1u;
+    const uint32_t sBk = f.sB + kb * kDigitImageBytes;
+    if (tid == 0) {
+      if (mbar_wait(f.bar_b + 8u * kb, (p.kimg >> 1) & 1u, a.spin_limit)) {
+        p.b_in_flight &= ~(1 << kb);
+        tc_fence_after();
+        p.issued = true;
+        // A plane i against nj stacked B planes j0.. (N = 64 nj) writes
+        // levels i + j0 .. i + j0 + nj - 1, which are consecutive 64-column
+        // ranges of tensor memory; the first group to reach a level
+        // initialises it (at K step 0), the others accumulate.
+#pragma unroll
+        for (int gi = 0; gi < kDgGroupCount<D>; ++gi) {
+          const DgGroup gr = dg_group<D>(gi);
+          const uint32_t idn = f.idesc_base | ((uint32_t)(8 * gr.nj) << 17);
+#pragma unroll
+          for (int ks = 0; ks < 4; ++ks) {
+            const uint64_t ad = sdesc(f.sA + (uint32_t)gr.i * kDgPlane + (uint32_t)ks * 32u);
+            const uint64_t bd = sdesc(sBk + (uint32_t)gr.j0 * 8192u + (uint32_t)ks * 32u);
+            mma_bf16(f.tmem + 64u * (uint32_t)(gr.i + gr.j0), ad, bd, idn, (gr.init && ks == 0) ? 0u : 1u);
+          }
+        }
+        mma_commit(f.bar_mma);
+        // the next block's image into the other buffer, whose last reader
+        // (the previous block's MMAs) has completed
+        const Blk5* nb = nullptr;
+        uint64_t nbase = obase;
+        if (more) {
+          nb = &f.blk[bi + 1];
+        } else if (has_next) {
+          nb = &f.blk[0];
+          nbase = ((obase | ~f.free_pos) + f.grid_base) & f.free_pos;
+        }
+        if (nb) {
+          load_image_bytes(f.sB + (kb ^ 1u) * kDigitImageBytes,
+                           a.images + (size_t)(nb->img + variant_of(*nb, nbase)) * kDigitImageBytes,
+                           f.bar_b + 8u * (kb ^ 1u), kDigitImageBytes);
+          p.b_in_flight |= 1 << (kb ^ 1u);
+        }
+      } else {
+        lost = true;  // the image never arrived: no MMAs; the MMA wait below expires
+      }
+    }
+    ++p.kimg;
+    // Level s holds digit position s + 1 of the result.  From the lowest
+    // level up: t = sum + carry, digit = t - 256 round(t / 256), carry the
+    // rest; positions D and D + 1 only round; position 0 is the last carry.
+    if (!mbar_wait(f.bar_mma, ph_mma, a.spin_limit)) lost = true;
+    tc_fence_after();
+    float carry[kDgCols];
+#pragma unroll
+    for (int c = 0; c < kDgCols; ++c) carry[c] = 0.f;
+    auto carry_step = [&](float* d) {
+#pragma unroll
+      for (int c = 0; c < kDgCols; ++c) {
+        const float t = __fadd_rn(d[c], carry[c]);
+        const float q = rint_div256(t);
+        d[c] = __fmaf_rn(q, -256.0f, t);
+        carry[c] = q;
+      }
+    };
+    if (more) {
+      // positions 1 .. D-1 and 0 become the next block's A planes
+      auto level = [&](const int s, float* d) {
+        carry_step(d);
+        if (s + 1 <= D - 1) {
+#pragma unroll
+          for (int c = 0; c < kDgCplx; ++c)
+            *reinterpret_cast<uint32_t*>(sm + (uint32_t)(s + 1) * kDgPlane + (dest_at4(dest, c) << 2)) =
+                pack_bf16(d[2 * c], d[2 * c + 1]);
+        }
+      };
+#pragma unroll
+      for (int s = D; s >= 1; s -= 2) {
+        float d0[kDgCols], d1[kDgCols];
+        tmem_ld8x2(f.tlane + 64u * (uint32_t)s, f.tlane + 64u * (uint32_t)(s - 1), d0, d1);
+        level(s, d0);
+        level(s - 1, d1);
+      }
+      if ((D + 1) & 1) {
+        float d0[kDgCols];
+        tmem_ld8(f.tlane, d0);
+        level(0, d0);
+      }
+#pragma unroll
+      for (int c = 0; c < kDgCplx; ++c)
+        *reinterpret_cast<uint32_t*>(sm + (dest_at4(dest, c) << 2)) = pack_bf16(carry[2 * c], carry[2 * c + 1]);
+      fence_proxy_async();
+    } else {
+      // after the last block the result is V = hi 2^24 + lo, the three
+      // lowest positions in lo and the others in hi (32-bit each)
+      int lo[kDgCols], hi[kDgCols];
+#pragma unroll
+      for (int c = 0; c < kDgCols; ++c) {
+        lo[c] = 0;
+        hi[c] = 0;
+      }
+      auto level = [&](const int s, float* d) {
+        carry_step(d);
+        const int pos = s + 1;
+        if (pos <= D - 1) {
+          if (pos >= D - 3) {
+#pragma unroll
+            for (int c = 0; c < kDgCols; ++c) lo[c] += int_of_small(d[c]) * (1 << (8 * (D - 1 - pos)));
+          } else {
+#pragma unroll
+            for (int c = 0; c < kDgCols; ++c) hi[c] += int_of_small(d[c]) * (1 << (8 * (D - 4 - pos)));
+          }
+        }
+      };
+#pragma unroll
+      for (int s = D; s >= 1; s -= 2) {
+        float d0[kDgCols], d1[kDgCols];
+        tmem_ld8x2(f.tlane + 64u * (uint32_t)s, f.tlane + 64u * (uint32_t)(s - 1), d0, d1);
+        level(s, d0);
+        level(s - 1, d1);
+      }
+      if ((D + 1) & 1) {
+        float d0[kDgCols];
+        tmem_ld8(f.tlane, d0);
+        level(0, d0);
+      }
+      double2* stage = reinterpret_cast<double2*>(sm);
+#pragma unroll
+      for (int c = 0; c < kDgCplx; ++c) {
+        const long long vr = (long long)(hi[2 * c] + int_of_small(carry[2 * c]) * (1 << (8 * (D - 4)))) *
+                                 16777216ll +
+                             (long long)lo[2 * c];
+        const long long vi = (long long)(hi[2 * c + 1] + int_of_small(carry[2 * c + 1]) * (1 << (8 * (D - 4)))) *
+                                 16777216ll +
+                             (long long)lo[2 * c + 1];
+        stage[dest_at4(dest, c)] = make_double2(double_of(vr, e - 8 * D), double_of(vi, e - 8 * D));
+      }
+    }
+    if (tid == 0 && lost && p.issued) p.mma_lost_phase = (int)ph_mma;
+    tc_fence_before();
+    if (__syncthreads_or(lost ? 1 : 0)) {
+      if (tid == 0) atomicExch(a.flag, 1);
+      return false;
+    }
+  }
+  const double2* stage = reinterpret_cast<const double2*>(sm);
+#pragma unroll
+  for (int it = 0; it < kDgLoadIters; ++it) {
+    const uint32_t i0 = (uint32_t)(it * kDgThreads + tid) * 2u;
+    double2* dst = a.s + (obase | (i0 & 31u) | f.hoff[i0 >> 5]);
+    const uint32_t sl = block_stage_slot(i0);
+    __stcs(dst, stage[sl]);
+    __stcs(dst + 1, stage[sl + 1]);
+  }
+  __syncthreads();
+  return true;
+}
+
 __global__ void __launch_bounds__(kDgThreads, 1) k_tblock_dg(const DgPassArgs a) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* sm = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
   uint64_t* hoff = reinterpret_cast<uint64_t*>(sm + kDgSmemHoff);
   uint64_t* bars = reinterpret_cast<uint64_t*>(sm + kDgSmemBar);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + kDgSmemBar + 72);
+  unsigned long long* red = reinterpret_cast<unsigned long long*>(sm + kDgSmemRed);
   Blk5* blk = reinterpret_cast<Blk5*>(sm + kDgSmemBlk);
-  // bar_b + 8 k: image buffer k; bar_lvl + 8 s: the MMAs of level s (issued
-  // from level 6 down, so a level's completion implies every higher level's)
-  const uint32_t bar_b = smem_u32(&bars[0]), bar_lvl = smem_u32(&bars[2]);
-  const int tid = threadIdx.x, warp = tid >> 5;
+  // bars[0], bars[1]: image buffers; bars[2]: the MMAs of a block
+  const uint32_t bar_b = smem_u32(&bars[0]), bar_mma = smem_u32(&bars[2]);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
@@ -555,7 +832,7 @@ __global__ void __launch_bounds__(kDgThreads, 1) k_tblock_dg(const DgPassArgs a)
   if (tid == 32) {
     mbar_init(bar_b, 1);
     mbar_init(bar_b + 8u, 1);
-    for (int l = 0; l < kDgLevels; ++l) mbar_init(bar_lvl + 8u * (uint32_t)l, 1);
+    mbar_init(bar_mma, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   for (int h = tid; h < 128; h += kDgThreads) {
@@ -571,21 +848,28 @@ __global__ void __launch_bounds__(kDgThreads, 1) k_tblock_dg(const DgPassArgs a)
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   const uint32_t colh = (uint32_t)(warp >> 2);  // 8 column groups of 8
-  const uint32_t tlane = tmem + ((32u * (warp & 3)) << 16) + (uint32_t)kDgCols * colh;
-  const int e_scale = *a.scale_exp;
-  const int sh = 48 - e_scale;  // x / scale * 2^48 = x * 2^sh
-
+  DgFixed f;
+  f.sm = sm;
+  f.blk = blk;
+  f.hoff = hoff;
+  f.sA = smem_u32(sm);
+  f.sB = smem_u32(sm + kDgSmemB);
+  f.tmem = tmem;
+  f.tlane = tmem + ((32u * (warp & 3)) << 16) + (uint32_t)kDgCols * colh;
+  f.bar_b = bar_b;
+  f.bar_mma = bar_mma;
   // kind::f16: D FP32, A and B BF16, both K-major, M = 128 (N set per MMA)
-  const uint32_t idesc_base = (1u << 4) | (1u << 7) | (1u << 10) | ((128u >> 4) << 24);
-  const uint32_t sA = smem_u32(sm), sB = smem_u32(sm + kDgSmemB);
+  f.idesc_base = (1u << 4) | (1u << 7) | (1u << 10) | ((128u >> 4) << 24);
+  const int eg = *a.scale_exp;
 
-  uint32_t ph_b0 = 0, ph_b1 = 0, ph_mma = 0;
-  uint32_t kimg = 0;          // blocks this CTA has run: image buffer kimg & 1
-  int b_in_flight = 0;        // thread 0: image loads not yet waited for (by buffer bit)
-  bool issued = false;        // thread 0: MMAs issued for the current block
-  int mma_lost_phase = -1;    // thread 0: level-0 phase whose wait expired
-  bool failed = false;
-  bool range_ok = true;
+  DgPipe p;
+  p.kimg = 0;
+  p.b_in_flight = 0;
+  p.issued = false;
+  p.mma_lost_phase = -1;
+  p.range_ok = true;
+  uint32_t* tiles_by_digits = reinterpret_cast<uint32_t*>(sm + kDgSmemBar + 80);  // five, six (thread 0)
+  if (tid == 0) tiles_by_digits[0] = tiles_by_digits[1] = 0;
 
   auto tile_base = [&](uint64_t tile) {
     uint64_t ob = tile;
@@ -601,20 +885,24 @@ __global__ void __launch_bounds__(kDgThreads, 1) k_tblock_dg(const DgPassArgs a)
   const uint64_t free_pos = ((a.ntiles << kBlockTileQubits) - 1) & ~tpos;
   const uint64_t grid_base = tile_base(gridDim.x);
   auto step_base = [&](uint64_t b) { return ((b | ~free_pos) + grid_base) & free_pos; };
+  f.free_pos = free_pos;
+  f.grid_base = grid_base;
+  f.free_pos = free_pos;
+  f.grid_base = grid_base;
   uint64_t tile = blockIdx.x;
   uint64_t obase = tile_base(tile);
   if (tid == 0 && tile < a.ntiles) {
     const Blk5& b0 = blk[0];
-    load_image_bytes(sB, a.images + (size_t)(b0.img + variant_of(b0, obase)) * kDigitImageBytes, bar_b,
+    load_image_bytes(f.sB, a.images + (size_t)(b0.img + variant_of(b0, obase)) * kDigitImageBytes, bar_b,
                      kDigitImageBytes);
-    b_in_flight |= 1;
+    p.b_in_flight |= 1;
   }
   const uint2 load_dest = my_dests4(a.offsets, blk[0].load_offs);
 
+  bool failed = false;
   for (; tile < a.ntiles && !failed; tile += gridDim.x, obase = step_base(obase)) {
     const bool has_next = tile + gridDim.x < a.ntiles;
-    // load: 4 amplitudes per thread (all loads issued first), each as 6
-    // digit pairs (re, im) into the planes
+    // load: 4 amplitudes per thread, all loads issued first
     double2 v[2 * kDgLoadIters];
 #pragma unroll
     for (int it = 0; it < kDgLoadIters; ++it) {
@@ -629,164 +917,44 @@ __global__ void __launch_bounds__(kDgThreads, 1) k_tblock_dg(const DgPassArgs a)
       const double2* row = a.s + (step_base(obase) | hoff[tid]);
       asm volatile("cp.async.bulk.prefetch.L2.global [%0], 512;" ::"l"(row) : "memory");
     }
+    // the tile's norm bound, summed exactly over the CTA
+    unsigned long long sb = 0;
 #pragma unroll
-    for (int e = 0; e < 2 * kDgLoadIters; ++e) {
-      float dr[kDigits], di[kDigits];
-      range_ok &= digits_of(v[e].x, sh, dr);
-      range_ok &= digits_of(v[e].y, sh, di);
-      const uint32_t off = dest_at4(load_dest, e) << 2;
+    for (int el = 0; el < 2 * kDgLoadIters; ++el) sb += sq_bound(v[el].x, eg) + sq_bound(v[el].y, eg);
 #pragma unroll
-      for (int p = 0; p < kDigits; ++p)
-        *reinterpret_cast<uint32_t*>(sm + (uint32_t)p * kDgPlane + off) = pack_bf16(dr[p], di[p]);
-    }
-    fence_proxy_async();
+    for (int o = 16; o > 0; o >>= 1) sb += __shfl_xor_sync(0xffffffffu, sb, o);
+    if (lane == 0) red[warp] = sb;
     __syncthreads();
-
-    for (int bi = 0; bi < a.nblocks; ++bi) {
-      const bool more = bi + 1 < a.nblocks;
-      const uint2 dest = my_dests4(a.offsets, blk[bi].offs);
-      bool lost = false;
-      const uint32_t kb = kimg & 1u;
-      const uint32_t sBk = sB + kb * kDigitImageBytes;
-      if (tid == 0) {
-        if (mbar_wait(bar_b + 8u * kb, kb ? ph_b1 : ph_b0, a.spin_limit)) {
-          b_in_flight &= ~(1 << kb);
-          tc_fence_after();
-          issued = true;
-          // A plane i against nj stacked B planes j0.. (N = 64 nj) writes
-          // levels i + j0 .. i + j0 + nj - 1, which are consecutive 64-column
-          // ranges of tensor memory; the first group to reach a level
-          // initialises it (at K step 0), the others accumulate.
-          constexpr DgGroup groups[kDgGroups] = BF_DG_GROUPS;
+    sb = red[lane];
 #pragma unroll
-          for (int gi = 0; gi < kDgGroups; ++gi) {
-            const DgGroup gr = groups[gi];
-            const uint32_t idn = idesc_base | ((uint32_t)(8 * gr.nj) << 17);
-#pragma unroll
-            for (int ks = 0; ks < 4; ++ks) {
-              const uint64_t ad = sdesc(sA + (uint32_t)gr.i * kDgPlane + (uint32_t)ks * 32u);
-              const uint64_t bd = sdesc(sBk + (uint32_t)gr.j0 * 8192u + (uint32_t)ks * 32u);
-              mma_bf16(tmem + 64u * (uint32_t)(gr.i + gr.j0), ad, bd, idn, (gr.init && ks == 0) ? 0u : 1u);
-            }
-          }
-          mma_commit(bar_lvl);
-          // the next block's image into the other buffer, whose last reader
-          // (the previous block's MMAs) has completed
-          const Blk5* nb = nullptr;
-          uint64_t nbase = obase;
-          if (more) {
-            nb = &blk[bi + 1];
-          } else if (has_next) {
-            nb = &blk[0];
-            nbase = step_base(obase);
-          }
-          if (nb) {
-            load_image_bytes(sB + (kb ^ 1u) * kDigitImageBytes,
-                             a.images + (size_t)(nb->img + variant_of(*nb, nbase)) * kDigitImageBytes,
-                             bar_b + 8u * (kb ^ 1u), kDigitImageBytes);
-            b_in_flight |= 1 << (kb ^ 1u);
-          }
-        } else {
-          lost = true;  // the image never arrived: no MMAs; every level wait below expires
-        }
-      }
-      if (kb) ph_b1 ^= 1u; else ph_b0 ^= 1u;
-      ++kimg;
-      // Level s holds digit position s + 1 of the result.  From the lowest
-      // level up: t = sum + carry, digit = t - 256 round(t / 256), carry the
-      // rest; positions 6 and 7 only round; position 0 is the last carry.
-      // after the last block the result is V = hi 2^24 + lo with hi =
-      // carry 2^16 + d1 2^8 + d2 and lo = d3 2^16 + d4 2^8 + d5 (32-bit)
-      float carry[kDgCols];
-      int lo[kDgCols], hi[kDgCols];
-#pragma unroll
-      for (int v = 0; v < kDgCols; ++v) {
-        carry[v] = 0.f;
-        lo[v] = 0;
-        hi[v] = 0;
-      }
-      auto level = [&](const int s, float* d) {
-        const int pos = s + 1;
-#pragma unroll
-        for (int v = 0; v < kDgCols; ++v) {
-          const float t = __fadd_rn(d[v], carry[v]);
-          const float q = rint_div256(t);
-          d[v] = __fmaf_rn(q, -256.0f, t);
-          carry[v] = q;
-        }
-        if (pos <= kDigits - 1) {
-          if (more) {
-#pragma unroll
-            for (int c = 0; c < kDgCplx; ++c)
-              *reinterpret_cast<uint32_t*>(sm + (uint32_t)pos * kDgPlane + (dest_at4(dest, c) << 2)) =
-                  pack_bf16(d[2 * c], d[2 * c + 1]);
-          } else if (pos >= 3) {
-#pragma unroll
-            for (int v = 0; v < kDgCols; ++v) lo[v] += int_of_small(d[v]) * (1 << (8 * (kDigits - 1 - pos)));
-          } else {
-#pragma unroll
-            for (int v = 0; v < kDgCols; ++v) hi[v] += int_of_small(d[v]) * (1 << (8 * (2 - pos)));
-          }
-        }
-      };
-      if (!mbar_wait(bar_lvl, ph_mma, a.spin_limit)) lost = true;
-      tc_fence_after();
-#pragma unroll
-      for (int s = kDgLevels - 1; s >= 1; s -= 2) {
-        float d0[kDgCols], d1[kDgCols];
-        tmem_ld8x2(tlane + 64u * (uint32_t)s, tlane + 64u * (uint32_t)(s - 1), d0, d1);
-        level(s, d0);
-        level(s - 1, d1);
-      }
-      if (kDgLevels & 1) {
-        float d0[kDgCols];
-        tmem_ld8(tlane, d0);
-        level(0, d0);
-      }
-      // position 0: the remaining carry
-      if (more) {
-#pragma unroll
-        for (int c = 0; c < kDgCplx; ++c)
-          *reinterpret_cast<uint32_t*>(sm + (dest_at4(dest, c) << 2)) = pack_bf16(carry[2 * c], carry[2 * c + 1]);
-        fence_proxy_async();
-      } else {
-        double2* stage = reinterpret_cast<double2*>(sm);
-#pragma unroll
-        for (int c = 0; c < kDgCplx; ++c) {
-          const long long vr =
-              (long long)(hi[2 * c] + int_of_small(carry[2 * c]) * 65536) * 16777216ll + (long long)lo[2 * c];
-          const long long vi =
-              (long long)(hi[2 * c + 1] + int_of_small(carry[2 * c + 1]) * 65536) * 16777216ll + (long long)lo[2 * c + 1];
-          stage[dest_at4(dest, c)] = make_double2(double_of(vr, e_scale - 48), double_of(vi, e_scale - 48));
-        }
-      }
-      if (tid == 0 && lost && issued) mma_lost_phase = (int)ph_mma;
-      ph_mma ^= 1u;
-      tc_fence_before();
-      if (__syncthreads_or(lost ? 1 : 0)) {
-        if (tid == 0) atomicExch(a.flag, 1);
-        failed = true;
-        break;
-      }
+    for (int o = 16; o > 0; o >>= 1) sb += __shfl_xor_sync(0xffffffffu, sb, o);
+    const int et = tile_scale_exp(sb, eg);
+    bool ok;
+    if (et <= eg - a.few_digits_slack) {
+      if (tid == 0) ++tiles_by_digits[0];
+      ok = dg_tile<kDgFewDigits>(a, f, p, v, load_dest, obase, has_next, et);
+    } else {
+      if (tid == 0) ++tiles_by_digits[1];
+      ok = dg_tile<kDigits>(a, f, p, v, load_dest, obase, has_next, et < eg ? et : eg);
     }
-    if (failed) break;
-    const double2* stage = reinterpret_cast<const double2*>(sm);
-#pragma unroll
-    for (int it = 0; it < kDgLoadIters; ++it) {
-      const uint32_t i0 = (uint32_t)(it * kDgThreads + tid) * 2u;
-      double2* dst = a.s + (obase | (i0 & 31u) | hoff[i0 >> 5]);
-      const uint32_t sl = block_stage_slot(i0);
-      __stcs(dst, stage[sl]);
-      __stcs(dst + 1, stage[sl + 1]);
-    }
-    __syncthreads();
+    if (!ok) failed = true;
   }
-  if (!range_ok) atomicExch(a.flag, 2);
+  if (!p.range_ok) atomicExch(a.flag, 2);
+  if (tid == 0 && a.digit_tiles) {
+    atomicAdd(a.digit_tiles, (unsigned long long)tiles_by_digits[0]);
+    atomicAdd(a.digit_tiles + 1, (unsigned long long)tiles_by_digits[1]);
+  }
 
   if (tid == 0) {
-    if ((b_in_flight & 1) && !mbar_wait(bar_b, ph_b0, a.spin_limit)) atomicExch(a.flag, 1);
-    if ((b_in_flight & 2) && !mbar_wait(bar_b + 8u, ph_b1, a.spin_limit)) atomicExch(a.flag, 1);
-    if (mma_lost_phase >= 0 && !mbar_wait(bar_lvl, (uint32_t)mma_lost_phase, a.spin_limit)) atomicExch(a.flag, 1);
+    // a load in flight into buffer k completes the phase of the next block
+    // that would have used it
+    for (uint32_t k = 0; k < 2; ++k) {
+      if (!(p.b_in_flight & (1 << k))) continue;
+      const uint32_t next_use = (p.kimg & 1u) == k ? p.kimg : p.kimg + 1;
+      if (!mbar_wait(bar_b + 8u * k, (next_use >> 1) & 1u, a.spin_limit)) atomicExch(a.flag, 1);
+    }
+    if (p.mma_lost_phase >= 0 && !mbar_wait(bar_mma, (uint32_t)p.mma_lost_phase, a.spin_limit))
+      atomicExch(a.flag, 1);
   }
   tc_fence_before();
   __syncthreads();
@@ -845,6 +1013,12 @@ void launch_block_pass_digits(State& st, const Blk5* d_blocks, int nblocks, cons
   a.scale_exp = d_exp;
   a.flag = state_flag(st);
   a.spin_limit = 1u << 24;
+  // five-digit tiles need a scale 2^8 below the state's; a test may move the
+  // threshold (a negative slack makes every tile five-digit) to exercise both
+  // forms on small states
+  const char* slack = std::getenv("BFGPU_DIGIT_SLACK");
+  a.few_digits_slack = (slack && *slack) ? std::atoi(slack) : kDgFewDigitsSlack;
+  a.digit_tiles = digit_tile_counters(st);
   static PerDeviceOnce configured;
   configured.run(st.device, [] {
     BF_CUDA(cudaFuncSetAttribute(k_tblock_dg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDgSmemAlloc));

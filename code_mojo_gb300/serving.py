@@ -172,3 +172,84 @@ def poisson_run(server: Server, requests, rate: float, duration_s: float, drain_
             "completed_by_qubits": {int(k): int(v) for k, v in zip(*np.unique(nq, return_counts=True))},
             "peak_state_bytes": int(st["peak_bytes"]),
             "small": split(lambda c: c <= LARGE_COST), "large": split(lambda c: c > LARGE_COST)}
+
+
+def closed_loop_run(server: Server, requests, inflight: int, duration_s: float, drain_s: float,
+                    dtype: str = "c64") -> dict:
+    """Capacity of the server on a request mix: `inflight` requests are kept
+    submitted at all times (a completed one is replaced by the next of the
+    list, cycling) for `duration_s` seconds, then the rest drain (bounded by
+    `drain_s`).  Reports the completions per second of the window and the
+    latency percentiles of the requests completed in it; with a closed loop
+    the queue never grows beyond `inflight`, so these are engine figures,
+    not queueing ones."""
+    t0 = time.perf_counter()
+    cost = {}
+    nxt = 0
+
+    def submit_next():
+        nonlocal nxt
+        kind, ops = requests[nxt % len(requests)]
+        nxt += 1
+        rid = server.submit(ops, dtype)
+        cost[rid] = (1 << ops.num_qubits) * max(1, len(ops))
+
+    for _ in range(inflight):
+        submit_next()
+    in_window = []
+    while time.perf_counter() - t0 < duration_s:
+        got = server.poll()
+        if not got:
+            time.sleep(0.0005)
+            continue
+        now = time.perf_counter() - t0
+        for r in got:
+            if r.id not in cost:
+                raise RuntimeError(f"result {r.id} was never submitted in this run")
+            in_window.append((now, r))
+            if now < duration_s:
+                submit_next()
+    window = time.perf_counter() - t0
+    drained = server.wait_idle(drain_s)
+    server.poll(1 << 16)
+    ok = [r for _, r in in_window if r.status == 0]
+    lat = np.array([r.latency_s for r in ok]) * 1e3
+
+    def split(pred):
+        la = np.array([r.latency_s for r in ok if pred(cost[r.id])]) * 1e3
+        return {"completed": int(len(la)), "per_s": len(la) / window,
+                "p50_ms": float(np.percentile(la, 50)) if len(la) else None,
+                "p99_ms": float(np.percentile(la, 99)) if len(la) else None}
+
+    nq = np.array([r.num_qubits for r in ok])
+    return {"dtype": dtype, "inflight": inflight, "window_s": window, "submitted": nxt, "completed": len(ok),
+            "failed": sum(1 for _, r in in_window if r.status != 0), "drained_after": drained,
+            "circuits_per_s": len(ok) / window,
+            "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
+            "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
+            "completed_by_qubits": {int(k): int(v) for k, v in zip(*np.unique(nq, return_counts=True))},
+            "small": split(lambda c: c <= LARGE_COST), "large": split(lambda c: c > LARGE_COST)}
+
+
+def top_probability_gap(reqs, inflight: int = 8, slots: int = 8) -> dict:
+    """complex64 against complex128 served results of the same requests: the
+    largest difference of the top-16 probabilities at the complex128 result's
+    indices, and whether the two top sets agree up to ties within 1e-6."""
+    res = {}
+    for dtype in ("c64", "c128"):
+        srv = Server(slots=slots)
+        ids = [srv.submit(ops, dtype) for _, ops in reqs]
+        srv.wait_idle(600)
+        by = {r.id: r for r in srv.poll(1 << 16)}
+        srv.close()
+        res[dtype] = [by[i] for i in ids]
+    worst, agree = 0.0, 0
+    for a, b in zip(res["c64"], res["c128"]):
+        pa = dict(zip(a.top_index.tolist(), a.top_prob.tolist()))
+        kth = float(b.top_prob[-1])
+        same = all(i in pa or float(p) <= kth + 1e-6 for i, p in zip(b.top_index.tolist(), b.top_prob.tolist()))
+        agree += int(same)
+        for i, p in zip(b.top_index.tolist(), b.top_prob.tolist()):
+            if i in pa:
+                worst = max(worst, abs(pa[i] - float(p)))
+    return {"requests": len(reqs), "max_top16_prob_gap": worst, "top_sets_agree": agree}

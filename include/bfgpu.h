@@ -230,6 +230,12 @@ enum {
 };
 int bf_state_pass_timing(bf_state* st, int32_t enable);
 int bf_state_pass_times(bf_state* st, int64_t* counts, double* ms);
+/* complex128 digit passes: how many 4096-amplitude tiles ran with five and
+ * with six base-256 digits since the state was created (or since the last
+ * reset).  A tile takes five digits when its own scale (a power of two at
+ * least twice the tile's norm) is 2^8 or more below the state's; waits for
+ * the state's stream.  No counterpart in the reference. */
+int bf_state_digit_tiles(bf_state* st, uint64_t* five, uint64_t* six, int32_t reset);
 
 /* ---- reductions ---------------------------------------------------------- */
 /* sum |amp|^2, accumulated in FP64 (state.mojo:482-501 accumulates in the
@@ -266,7 +272,9 @@ int bf_probs_topk(bf_state* st, int32_t k, uint64_t* indices, double* probs);
  * No single counterpart in the reference (its benches run circuits one at a
  * time through execute).  Many small circuits (1..30 qubits each, gate
  * transformations only) run from |0...0> in ONE persistent cooperative
- * launch: each circuit is planned into tile passes, every tile of every pass
+ * launch: each circuit is planned into tile passes (tile width
+ * opts->tile_qubits, or with 0 a width per qubit count picked by timing the
+ * candidates at creation, see bf_batch_tuning), every tile of every pass
  * is a task, tasks are taken from an atomic ticket in pass-major order and a
  * task waits (bounded) for its circuit's previous pass.  The run is captured
  * into a CUDA graph at creation and replayed by bf_batch_run.
@@ -285,6 +293,13 @@ int bf_batch_stats(bf_batch* b, int64_t* tasks, int64_t* passes,
                    uint64_t* state_bytes, int32_t* graph_captured,
                    uint64_t* launches);
 int bf_batch_stream(bf_batch* b, void** stream);
+/* The autotuning record of a batch created with opts->tile_qubits == 0.
+ * For every qubit count n above 8 in the batch, each candidate tile width
+ * (8..min(n, 12)) was timed on a sample of the batch's n-qubit circuits at
+ * creation (one run of the sample, ms), and the fastest was kept for those
+ * circuits (chosen = 1).  Writes up to cap rows and the row count. */
+int bf_batch_tuning(bf_batch* b, int32_t* qubits, int32_t* widths, double* ms,
+                    int32_t* chosen, int32_t cap, int32_t* count);
 int bf_batch_destroy(bf_batch* b);
 
 /* ---- serving: continuous batching of requests ------------------------------

@@ -14,18 +14,24 @@
 // and single-gate steps are applied gate by gate.
 //
 // Mode digits-exact follows the complex128 digit kernel's arithmetic step
-// by step instead: the scale from the norm before the first digit pass,
-// each value rounded to six balanced base-256 digits, exact integer level
-// sums of the 26 digit pairs, the carries with round-half-even, and the
-// FP64 result after the last block, so that the model gives the bits the
-// kernel gives.
+// by step instead: the state's scale from the norm before the first digit
+// pass; per tile, the exact integer bound of its norm, its own scale and its
+// digit count (five when that scale is 2^8 or more below the state's, six
+// otherwise; BFGPU_DIGIT_SLACK moves the threshold as it does for the
+// kernel); each value rounded to that many balanced base-256 digits, exact
+// integer level sums of the kept digit pairs (20 or 26), the carries with
+// round-half-even, and the FP64 result after the last block, so that the
+// model gives the bits the kernel gives.  It prints the passes by kind and
+// the tiles run with five and with six digits.
 //
 //   block_model <digits|digits-exact|tf32> <ops file (binary op list)> <state in> <state out>
 //
 // The state files hold 2^n interleaved complex128 values.
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <iterator>
@@ -101,17 +107,48 @@ static void decode_image(const unsigned char* img, bool digits, cd* u) {
 
 // ---- the digit kernel's arithmetic ------------------------------------------
 
-// round(x * 2^sh) (half away from zero on the magnitude) as six balanced
-// base-256 digits, d[5] the lowest
-static void value_digits_of(double x, int sh, int* d) {
-  long long V = (long long)std::llround(std::ldexp(std::fabs(x), sh));
+// round(x * 2^sh) (to nearest, ties to even, on the magnitude) as D balanced
+// base-256 digits, d[D-1] the lowest
+static void value_digits_of(double x, int sh, int D, int* d) {
+  long long V = (long long)std::nearbyint(std::ldexp(std::fabs(x), sh));
   if (x < 0) V = -V;
-  for (int j = kDigits - 1; j >= 1; --j) {
+  for (int j = D - 1; j >= 1; --j) {
     const long long t = ((V & 255) ^ 128) - 128;
     d[j] = (int)t;
     V = (V - t) >> 8;
   }
   d[0] = (int)V;
+}
+
+// the kernel's integer bound of x^2 in units of 2^(2 eg - 50): (257 + the
+// top 8 mantissa bits)^2 2^k, k = 2 (ex - eg) - 2012, rounded up
+static unsigned long long sq_bound(double x, int eg) {
+  unsigned long long b;
+  std::memcpy(&b, &x, 8);
+  b &= 0x7FFFFFFFFFFFFFFFull;
+  if (b == 0) return 0;
+  const int ex = (int)(b >> 52);
+  if (ex == 0) return 1;
+  const unsigned long long u = 257u + ((b >> 44) & 255u);
+  const int k = 2 * (ex - eg) - 2012;
+  if (k >= 0) return (u * u) << std::min(k, 30);
+  if (k <= -19) return 1;
+  return (u * u + (1ull << -k) - 1) >> -k;
+}
+
+// digits and scale exponent of a tile from its bound S: e_t = eg - 24 +
+// ceil((bit length of S) / 2); five digits when e_t <= eg - slack
+static void tile_digits(unsigned long long S, int eg, int slack, int* D, int* e) {
+  int L = 0;
+  while (L < 64 && (S >> L) != 0) ++L;
+  const int et = eg - 24 + ((L + 1) >> 1);
+  if (et <= eg - slack) {
+    *D = 5;
+    *e = et;
+  } else {
+    *D = 6;
+    *e = std::min(et, eg);
+  }
 }
 
 // the six digits e_0..e_5 of every entry of an image's 64x64 real matrix, [n][k]
@@ -132,9 +169,8 @@ static void image_digits(const unsigned char* img, int (*b)[64][64]) {
 
 static void run_digit_pass_exact(std::vector<cd>& s, int n, const TilePass& tp, const std::vector<Blk5>& blocks,
                                  const std::vector<unsigned char>& images, const std::vector<uint16_t>& offsets,
-                                 int e_scale) {
+                                 int e_scale, int slack, long long* tiles_by_digits) {
   const int T = kDigitThreads, E = kBlockTableEntries / T;
-  const int sh = 48 - e_scale;
   std::vector<int> g_of(4096), j_of(4096);
   for (uint32_t g = 0; g < 128; ++g)
     for (uint32_t j = 0; j < 32; ++j) {
@@ -159,12 +195,18 @@ static void run_digit_pass_exact(std::vector<cd>& s, int n, const TilePass& tp, 
     for (int j = 0; j < kBlockTileQubits; ++j) obase = insert_zero(obase, tp.q[j]);
     auto gi = [&](uint32_t i) { return obase | (i & 31u) | hoff[i >> 5]; };
     const uint16_t* load = offsets.data() + (size_t)blocks[0].load_offs * kBlockTableEntries;
+    unsigned long long S = 0;
+    for (uint32_t i = 0; i < 4096; ++i) S += sq_bound(s[gi(i)].real(), e_scale) + sq_bound(s[gi(i)].imag(), e_scale);
+    int D = kDigits, et = e_scale;
+    tile_digits(S, e_scale, slack, &D, &et);
+    ++tiles_by_digits[D == 5 ? 0 : 1];
+    const int sh = 8 * D - et;
     for (int t = 0; t < T; ++t)
       for (int e = 0; e < E; ++e) {
         const uint32_t i = (uint32_t)(((e >> 1) * T + t) * 2 + (e & 1));
         Slot& sl = opnd[load[t * E + e]];
-        value_digits_of(s[gi(i)].real(), sh, sl.re);
-        value_digits_of(s[gi(i)].imag(), sh, sl.im);
+        value_digits_of(s[gi(i)].real(), sh, D, sl.re);
+        value_digits_of(s[gi(i)].imag(), sh, D, sl.im);
       }
     for (size_t bi = 0; bi < blocks.size(); ++bi) {
       const Blk5& bk = blocks[bi];
@@ -173,7 +215,7 @@ static void run_digit_pass_exact(std::vector<cd>& s, int n, const TilePass& tp, 
       for (int k = 0; k < bk.nout; ++k) v |= (uint32_t)((obase >> bk.outpos[k]) & 1ull) << k;
       image_digits(images.data() + (size_t)(bk.img + v) * kDigitImageBytes, b);
       for (int slot = 0; slot < 4096; ++slot)
-        for (int i = 0; i < kDigits; ++i) {
+        for (int i = 0; i < D; ++i) {
           a[((size_t)i * 128 + g_of[slot]) * 64 + 2 * j_of[slot]] = opnd[slot].re[i];
           a[((size_t)i * 128 + g_of[slot]) * 64 + 2 * j_of[slot] + 1] = opnd[slot].im[i];
         }
@@ -186,34 +228,35 @@ static void run_digit_pass_exact(std::vector<cd>& s, int n, const TilePass& tp, 
           long long V[2];
           for (int d = 0; d < 2; ++d) {
             const int nn = 2 * jo + d;
-            long long D[7];
-            for (int lv = 0; lv < 7; ++lv) {
-              D[lv] = 0;
-              for (int i = 0; i <= lv && i < kDigits; ++i) {
+            // levels 0..D: the pairs i < D, j < 6 with i + j = level
+            long long Lv[kDigits + 1];
+            for (int lv = 0; lv <= D; ++lv) {
+              Lv[lv] = 0;
+              for (int i = 0; i <= lv && i < D; ++i) {
                 const int j = lv - i;
                 if (j >= kDigits) continue;
                 const int* ar = &a[((size_t)i * 128 + g) * 64];
-                for (int k = 0; k < 64; ++k) D[lv] += (long long)ar[k] * b[j][nn][k];
+                for (int k = 0; k < 64; ++k) Lv[lv] += (long long)ar[k] * b[j][nn][k];
               }
             }
             // carries from the lowest level up, rounding half to even
             double carry = 0;
-            for (int lv = 6; lv >= 0; --lv) {
-              const double t2 = (double)D[lv] + carry;
+            for (int lv = D; lv >= 0; --lv) {
+              const double t2 = (double)Lv[lv] + carry;
               const double q = std::nearbyint(t2 / 256.0);
-              if (lv + 1 <= kDigits - 1) dig[d][lv + 1] = (int)(t2 - 256.0 * q);
+              if (lv + 1 <= D - 1) dig[d][lv + 1] = (int)(t2 - 256.0 * q);
               carry = q;
             }
             dig[d][0] = (int)carry;
             V[d] = 0;
-            for (int p2 = 0; p2 < kDigits; ++p2) V[d] = V[d] * 256 + dig[d][p2];
+            for (int p2 = 0; p2 < D; ++p2) V[d] = V[d] * 256 + dig[d][p2];
           }
           const uint16_t to = dest[t * E + e];
           if (last) {
-            stage_re[to] = std::ldexp((double)V[0], e_scale - 48);
-            stage_im[to] = std::ldexp((double)V[1], e_scale - 48);
+            stage_re[to] = std::ldexp((double)V[0], et - 8 * D);
+            stage_im[to] = std::ldexp((double)V[1], et - 8 * D);
           } else {
-            for (int p2 = 0; p2 < kDigits; ++p2) {
+            for (int p2 = 0; p2 < D; ++p2) {
               next[to].re[p2] = dig[0][p2];
               next[to].im[p2] = dig[1][p2];
             }
@@ -292,6 +335,11 @@ int main(int argc, char** argv) {
   const bool exact = std::strcmp(argv[1], "digits-exact") == 0;
   const bool digits = exact || std::strcmp(argv[1], "digits") == 0;
   int e_scale = 0;  // the digit scale, from the norm before the first digit pass
+  // five-digit tiles need a scale 2^slack below the state's (as the kernel,
+  // including its test override)
+  const char* slack_env = std::getenv("BFGPU_DIGIT_SLACK");
+  const int slack = (slack_env && *slack_env) ? std::atoi(slack_env) : 8;
+  long long tiles_by_digits[2] = {0, 0};
   std::ifstream fo(argv[2], std::ios::binary);
   std::vector<char> blob((std::istreambuf_iterator<char>(fo)), {});
   bf_oplist* list = nullptr;
@@ -328,7 +376,7 @@ int main(int argc, char** argv) {
           std::frexp(std::sqrt(nrm2) * (1.0 + 1e-6), &k);
           e_scale = nrm2 > 0 ? k + 1 : 1;
         }
-        run_digit_pass_exact(s, n, ps.tile, blocks, images, offsets, e_scale);
+        run_digit_pass_exact(s, n, ps.tile, blocks, images, offsets, e_scale, slack, tiles_by_digits);
       } else {
         run_block_pass(s, n, ps.tile, blocks, images, offsets, digits);
       }
@@ -340,6 +388,6 @@ int main(int argc, char** argv) {
   }
   std::ofstream fw(argv[4], std::ios::binary);
   fw.write(reinterpret_cast<const char*>(s.data()), (std::streamsize)(s.size() * sizeof(cd)));
-  std::printf("%d %d %d\n", block_passes, tile_passes, gate_steps);
+  std::printf("%d %d %d %lld %lld\n", block_passes, tile_passes, gate_steps, tiles_by_digits[0], tiles_by_digits[1]);
   return 0;
 }

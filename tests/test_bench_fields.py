@@ -49,8 +49,9 @@ def test_per_gate_bytes_of_the_layered_circuit_from_the_gates_alone(bench):
     from code_mojo_gb300 import workloads as W
     # 40 layers x (30 U3 at 2S + 15 CX at S)
     assert bench.per_gate_bytes_in_S(W.random_layered_circuit(30, 40, 0)) == 3000.0
-    # QFT-20: 20 H (2S) + 190 CP (S/2)
+    # QFT-20: 20 H (2S) + 190 CP (S/2), and the bit reversal (2S)
     assert bench.per_gate_bytes_in_S(W.qft_circuit(20, with_bit_reversal=False)) == 20 * 2 + 190 * 0.5
+    assert bench.per_gate_bytes_in_S(W.qft_circuit(20)) == 20 * 2 + 190 * 0.5 + 2
 
 
 def test_hbm_figure_of_the_fused_step(bench):

@@ -34,13 +34,22 @@ def model(tmp_path_factory):
     return exe
 
 
-def run_model(exe, fmt, qc, re, im, tmp_path):
+def run_model(exe, fmt, qc, re, im, tmp_path, slack=None, tiles=False):
+    import os
     ops, sin, sout = tmp_path / "ops.bin", tmp_path / "in.bin", tmp_path / "out.bin"
     ops.write_bytes(bfy.serialize(qc))
     (re + 1j * im).astype(np.complex128).tofile(sin)
-    r = subprocess.run([str(exe), fmt, str(ops), str(sin), str(sout)], check=True, capture_output=True, text=True)
-    block_passes, tile_passes, gate_steps = (int(x) for x in r.stdout.split())
-    return np.fromfile(sout, dtype=np.complex128), block_passes
+    env = dict(os.environ)
+    env.pop("BFGPU_DIGIT_SLACK", None)
+    if slack is not None:
+        env["BFGPU_DIGIT_SLACK"] = str(slack)
+    r = subprocess.run([str(exe), fmt, str(ops), str(sin), str(sout)], check=True, capture_output=True, text=True,
+                       env=env)
+    fields = [int(x) for x in r.stdout.split()]
+    out = np.fromfile(sout, dtype=np.complex128)
+    if tiles:
+        return out, fields[0], (fields[3], fields[4])
+    return out, fields[0]
 
 
 def random_controlled_circuit(n, count, seed):
@@ -116,3 +125,49 @@ def test_block_passes_match_the_oracle(model, fmt, name, tmp_path):
         assert block_passes > 0
     # digit images hold the matrices to 48 bits; TF32 hi + lo parts to about 2^-22
     assert err <= (1e-12 if fmt == "digits" else 1e-5), err
+
+
+@pytest.mark.parametrize("slack,tol", [(-100, 5e-11), (2, 3e-11)])
+def test_five_digit_tiles_match_the_oracle(model, slack, tol, tmp_path):
+    """Tiles in five digits (scale from the tile's own norm bound): forced on
+    every tile (slack -100: the tile's scale may then be above the state's,
+    a rounding unit of 2^-40 of it per block), and on the tiles whose scale
+    is 2^2 below the state's (16 qubits: a tile holds a quarter of the
+    norm)."""
+    qc = CIRCUITS["layered16x40"]() if slack == 2 else CIRCUITS["layered14"]()
+    n = qc.num_qubits
+    re, im = W.random_normal_state(n, 7)
+    got, _, (five, six) = run_model(model, "digits-exact", qc, re, im, tmp_path, slack=slack, tiles=True)
+    assert five > 0 and (six == 0 if slack < 0 else True)
+    r, i = O.run(qc, re, im)
+    assert float(np.max(np.abs(got - (r + 1j * i)))) <= tol
+
+
+def test_default_threshold_keeps_six_digits_on_small_states(model, tmp_path):
+    """At 13 qubits a tile holds half the state's norm: its scale is within
+    2^8 of the state's, so every tile keeps six digits."""
+    qc = CIRCUITS["layered13"]()
+    re, im = W.random_normal_state(13, 7)
+    _, _, (five, six) = run_model(model, "digits-exact", qc, re, im, tmp_path, tiles=True)
+    assert five == 0 and six > 0
+
+
+def test_rescaled_tiles_keep_the_norm(model, tmp_path):
+    """Tiles of consecutive passes have different scales, so the load often
+    drops exactly one half of a unit; it rounds those ties to even.  The
+    circuit followed by its adjoint keeps the norm and returns the state."""
+    from code_mojo_gb300 import opsarray as OA
+    n = 16
+    fwd = W.random_layered_circuit(n, 12, seed=6)
+    inv = bfy.QuantumCircuit(n)
+    for tr in reversed(fwd.transformations):
+        g = tr.gate_info
+        inv.add(tr.controls, tr.target, bfy.Custom_Gate(g.gate.conj().T) if g.kind == bfy.GateKind.CUSTOM else g)
+    qc = bfy.QuantumCircuit(n)
+    qc.transformations = fwd.transformations + inv.transformations
+    re, im = W.random_normal_state(n, 3)
+    got, _, (five, six) = run_model(model, "digits-exact", qc, re, im, tmp_path, slack=2, tiles=True)
+    assert five > 0
+    assert abs(float(np.sum(np.abs(got) ** 2)) - 1.0) <= 2e-12
+    assert float(np.max(np.abs(got - (re + 1j * im)))) <= 5e-11
+    del OA

@@ -90,3 +90,28 @@ def test_batch_at_full_spec_matches_the_oracle_per_circuit(dtype):
             assert d <= 1e-6, (int(c), n, d)
         worst = max(worst, d)
     b.close()
+
+
+def test_batch_autotuning_record_and_result():
+    """With tile_qubits = 0 a batch times the candidate tile widths per qubit
+    count at creation and keeps the fastest; the tuned batch still matches
+    the oracle circuit by circuit."""
+    circs = W.batch_workload(count=40, seed=9, nmin=6, nmax=13, depth=6)
+    b = B.Batch(circs, dtype="c128")
+    rows = b.tuning()
+    sizes = sorted({qc.num_qubits for qc in circs if qc.num_qubits > 8})
+    assert sorted({r["qubits"] for r in rows}) == sizes
+    for n in sizes:
+        cand = [r for r in rows if r["qubits"] == n]
+        assert [r["width"] for r in cand] == list(range(8, min(n, 12) + 1))
+        assert sum(r["chosen"] for r in cand) == 1 and all(r["ms"] > 0 for r in cand)
+        best = min(cand, key=lambda r: r["ms"])
+        assert best["chosen"]
+    b.run()
+    for c, qc in enumerate(circs):
+        assert np.max(np.abs(b.download(c) - expected(qc))) <= 1e-12
+    b.close()
+    # a fixed width records no tuning
+    f = B.Batch(circs[:4], dtype="c64", tile_qubits=10)
+    assert f.tuning() == []
+    f.close()

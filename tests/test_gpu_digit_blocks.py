@@ -216,12 +216,16 @@ def test_plan_cache_tells_circuits_apart():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("slack", [None, -100, 1])
 @pytest.mark.parametrize("layers,seed", [(8, 0), (12, 1), (16, 0)])
-def test_digit_passes_equal_the_arithmetic_model_bit_for_bit(layers, seed, tmp_path):
+def test_digit_passes_equal_the_arithmetic_model_bit_for_bit(layers, seed, slack, tmp_path, monkeypatch):
     """The GPU's digit passes give exactly the bits of the host model of the
-    digit arithmetic (tests/block_model.cpp, digits-exact): the same scale,
-    48-bit digits, exact level sums and half-even carries.  The circuits are
-    planned as block passes only, so no double-float pass is involved."""
+    digit arithmetic (tests/block_model.cpp, digits-exact): the same state
+    and tile scales, digit counts, digits, exact level sums and half-even
+    carries.  The circuits are planned as block passes only, so no
+    double-float pass is involved.  The default threshold keeps six digits
+    at 13 qubits; a slack of -100 makes every tile five-digit, and 1 mixes
+    the two forms by tile where the tiles' norms differ."""
     import shutil
     import subprocess
     from pathlib import Path
@@ -236,15 +240,38 @@ def test_digit_passes_equal_the_arithmetic_model_bit_for_bit(layers, seed, tmp_p
     subprocess.run(["g++", "-O2", "-std=c++17", "-I", "/usr/local/cuda/include", "-I", str(root / "include"),
                     str(root / "tests" / "block_model.cpp"), "-o", str(exe), "-L", str(lib.parent), "-lbfgpu",
                     f"-Wl,-rpath,{lib.parent}"], check=True, capture_output=True)
+    import os
     n = 13
     qc = W.random_layered_circuit(n, layers, seed=seed)
     plan = bfy.plan_stats(qc, ctx(True))
     assert plan["block_passes"] == plan["tile_passes"] > 0 and plan["gate_kernels"] == 0
     re, im = W.random_normal_state(n, 7)
+    # a state whose norm is spread unevenly over the tiles, so that a
+    # middle slack gives both digit counts
+    re[: 1 << 12] *= 3.0
+    im[: 1 << 12] *= 3.0
     (tmp_path / "ops.bin").write_bytes(bfy.serialize(qc))
     (re + 1j * im).astype(np.complex128).tofile(tmp_path / "in.bin")
-    subprocess.run([str(exe), "digits-exact", str(tmp_path / "ops.bin"), str(tmp_path / "in.bin"),
-                    str(tmp_path / "out.bin")], check=True, capture_output=True)
+    env = dict(os.environ)
+    env.pop("BFGPU_DIGIT_SLACK", None)
+    if slack is None:
+        monkeypatch.delenv("BFGPU_DIGIT_SLACK", raising=False)
+    else:
+        env["BFGPU_DIGIT_SLACK"] = str(slack)
+        monkeypatch.setenv("BFGPU_DIGIT_SLACK", str(slack))
+    r = subprocess.run([str(exe), "digits-exact", str(tmp_path / "ops.bin"), str(tmp_path / "in.bin"),
+                        str(tmp_path / "out.bin")], check=True, capture_output=True, text=True, env=env)
+    five_model, six_model = (int(x) for x in r.stdout.split()[3:5])
     model = np.fromfile(tmp_path / "out.bin", dtype=np.complex128)
-    got = run(qc, re, im)
+    st = bfy.QuantumState.from_soa(re, im)
+    st.digit_tiles(reset=True)
+    bfy.execute(st, qc, ctx(True))
+    got = st.to_complex()
+    five, six = st.digit_tiles()
+    st.close()
+    assert (five, six) == (five_model, six_model)
+    if slack is None:
+        assert five == 0 and six > 0
+    elif slack < 0:
+        assert six == 0 and five > 0
     assert np.array_equal(got, model)

@@ -392,6 +392,7 @@ def test_random_layered_30q_40_layers_matches_the_oracle(capsys):
     qc = W.random_layered_circuit(n, 40, seed=0)
     st = bfy.QuantumState(n)
     bfy.execute(st, qc)
+    five, six = st.digit_tiles()
     plan = bfy.plan_stats(qc)
     re, im = O.basis(n)
     O.run_inplace(qc, re, im, strategy=O.OR_SIMD_PARALLEL, threads=O.num_cores(), chunks=O.num_cores())
@@ -403,8 +404,8 @@ def test_random_layered_30q_40_layers_matches_the_oracle(capsys):
         worst = max(worst, float(np.max(np.abs((gr - re[off:off + blk]) + 1j * (gi - im[off:off + blk])))))
     st.close()
     with capsys.disabled():
-        print(f"\n30-qubit 40-layer circuit ({plan['block_passes']} digit passes, {plan['blocks']} blocks): "
-              f"max|d amp| against the oracle = {worst:.3e}")
+        print(f"\n30-qubit 40-layer circuit ({plan['block_passes']} digit passes, {plan['blocks']} blocks; "
+              f"tiles in five / six digits: {five} / {six}): max|d amp| against the oracle = {worst:.3e}")
     assert worst <= TOL128
 
 

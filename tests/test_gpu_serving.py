@@ -139,3 +139,23 @@ def test_served_complex64_results_match_the_oracle():
         assert np.max(np.abs(p[idx] - r.top_prob)) <= 1e-6, (i, kind, ops.num_qubits)
         kth = np.sort(p)[::-1][len(idx) - 1]
         assert np.all(p[idx] >= kth - 1e-6), (i, kind)
+
+
+def test_closed_loop_capacity_run():
+    """The capacity run keeps a fixed number of requests in flight: every
+    completion in the window is replaced, nothing fails, and the server is
+    idle after the drain."""
+    reqs = small_mix(32, seed=21)
+    srv = SV.Server(slots=4)
+    r = SV.closed_loop_run(srv, reqs, inflight=6, duration_s=1.0, drain_s=30.0, dtype="c64")
+    st = srv.stats()
+    srv.close()
+    assert r["failed"] == 0 and r["completed"] > 6 and r["drained_after"]
+    assert r["submitted"] >= r["completed"] and r["submitted"] <= r["completed"] + 6 + 64
+    assert st["queued"] == 0 and st["running"] == 0
+    assert r["circuits_per_s"] > 0 and r["p99_ms"] >= r["p50_ms"] > 0
+
+
+def test_complex64_and_complex128_served_results_agree():
+    gap = SV.top_probability_gap(small_mix(12, seed=23), slots=4)
+    assert gap["top_sets_agree"] == 12 and gap["max_top16_prob_gap"] <= 1e-6
