@@ -356,35 +356,37 @@ __global__ void __launch_bounds__(kBlkThreads, 2) k_tblock(const BlkPassArgs a) 
 }
 
 // ---- complex128: digit blocks on the bf16 tensor cores -----------------------
-// A complex128 value x of a tile becomes D signed base-256 digits, x / s_t =
-// 2^-8 sum_i d_i 2^-8i (i < D) with d_i integers of at most 8 bits plus
-// sign, each exact in bf16; the matrix likewise as six digits (r = 2^-8
-// sum_j e_j 2^-8j).  For every digit level s = i + j <= D the 4 MMAs of each
-// kept pair (i, j) (kind::f16, bf16 inputs, K = 16) accumulate sum_K d_i e_j
-// into one FP32 accumulator; every product and partial sum is an integer
-// below 2^24, so the accumulation is exact whatever the order.  The
-// epilogue turns the D + 1 level sums back into the next block's digits by
-// carries between levels (FP32 on exact integers), or after the last block
-// into the FP64 result.
+// A complex128 value x becomes D signed base-256 digits, x / s = 2^-8 sum_i
+// d_i 2^-8(i + 6 - D) (i < D) with d_i integers of at most 8 bits plus sign,
+// each exact in bf16; the matrix likewise as six digits (r = 2^-8 sum_j e_j
+// 2^-8j).  For every digit level s = i + j <= D the 4 MMAs of each kept pair
+// (i, j) (kind::f16, bf16 inputs, K = 16) accumulate sum_K d_i e_j into one
+// FP32 accumulator; every product and partial sum is an integer below 2^24,
+// so the accumulation is exact whatever the order.  The epilogue turns the
+// D + 1 level sums back into the next block's digits by carries between
+// levels (FP32 on exact integers), or after the last block into the FP64
+// result.
 //
-// The scale s_t = 2^e_t is the tile's own: a block pass mixes amplitudes
-// only within a tile, so the tile's norm is the same after every block, and
-// s_t >= 2 ||tile|| keeps every value below s_t / 2 through the pass.  The
-// bound comes from an exact integer sum over the tile (sq_bound), so it does
-// not depend on the order of the reduction.  A tile takes D = 5 digits (20
-// digit pairs) when e_t is at least 8 below the state's exponent e_g (s_g =
-// 2^e_g >= 2 ||state||, from the norm before the first digit pass), so its
-// rounding unit 2^-40 s_t is no coarser than six digits at the state's
-// scale; otherwise D = 6 (26 pairs) at min(e_t, e_g).  The choice is
-// uniform within a CTA's tile.  Dropping the levels s > D and rounding
-// below the last digit leave errors of about one unit of 2^-8D s_t per
-// block.  A pass runs in this form only when all its blocks are unitary.
+// The state is a fixed-point number: one scale s = 2^e (s >= 2 ||state||,
+// from the norm before the first digit pass) and the unit 2^-48 s, so every
+// amplitude of a unitary circuit is an integer V of that unit with |V| <
+// 2^47 (six digits).  A block pass mixes amplitudes only within a tile, so
+// a tile's norm is the same after every block; when it is below 2^-9 s,
+// every value of the tile stays below 2^39 units through the pass and the
+// top digit is zero: the tile runs in D = 5 digits (20 digit pairs instead
+// of 26) with the same unit, so the five- and six-digit forms hold the same
+// integers and give the same bits.  The norm test is an exact integer bound
+// per warp (sq_bound_units), decided at the barrier that follows the
+// conversion: a tile that fails it is converted again in six digits.  On
+// the 30-qubit circuit a tile holds about 2^-9 of the norm, so nearly every
+// tile runs five digits.  Dropping the levels s > D and rounding below the
+// unit leave errors of about one unit per block.  A pass runs in this form
+// only when all its blocks are unitary.
 constexpr uint32_t kDgPlane = 16384;                       // 128 rows x 64 bf16
 constexpr uint32_t kDgSmemB = kDigits * kDgPlane;          // 6 A planes (5 used by five-digit tiles), then B
 constexpr uint32_t kDgSmemHoff = kDgSmemB + 2 * kDigitImageBytes;  // two image buffers
-constexpr uint32_t kDgSmemBar = kDgSmemHoff + 128 * 8;  // 2 image barriers, 1 MMA barrier, tmem slot
-constexpr uint32_t kDgSmemRed = kDgSmemBar + 128;       // 32 x u64: the tile norm bound per warp
-constexpr uint32_t kDgSmemBlk = kDgSmemRed + 256;       // the pass's block descriptors
+constexpr uint32_t kDgSmemBar = kDgSmemHoff + 128 * 8;  // 2 image barriers, 1 MMA barrier, tmem slot, tile counts
+constexpr uint32_t kDgSmemBlk = kDgSmemBar + 128;       // the pass's block descriptors
 static_assert(sizeof(Blk5) == 32 && kDgSmemBlk % 16 == 0, "block descriptors are copied as 16-byte words");
 constexpr uint32_t kDgSmemUsed = kDgSmemBlk + kMaxPassBlocks * sizeof(Blk5);
 constexpr uint32_t kDgSmemAlloc = kDgSmemUsed + 1024;
@@ -394,7 +396,7 @@ constexpr int kDgCols = 64 / (kDgThreads / 128);           // FP32 columns of a 
 constexpr int kDgCplx = kDgCols / 2;                       // complex results per thread per block
 constexpr int kDgLoadIters = 4096 / (2 * kDgThreads);      // amplitude pairs per thread per tile
 constexpr int kDgFewDigits = 5;                            // digits of a tile with a small norm
-constexpr int kDgFewDigitsSlack = 8;                       // e_t <= e_g - 8 for five digits
+constexpr uint32_t kDgWarpBound = 1u << 27;                // a warp's norm bound below this: five digits
 static_assert(kDgCols == 8 && kDgLoadIters * 2 == kBlockTableEntries / kDgThreads, "digit kernel thread layout");
 
 // The MMA groups of one block: A plane i against B planes j0 .. j0+nj-1, in
@@ -450,7 +452,8 @@ struct DgPassArgs {
   const int* scale_exp;         // device: the state's scale 2^e_g
   int* flag;
   uint32_t spin_limit;
-  int32_t few_digits_slack;     // five digits when e_t <= e_g - slack
+  int32_t scale_shift;          // added to the state's scale exponent (0; a test moves it)
+  int32_t five_digits;          // 1: tiles below the norm bound run five digits; 0: six always
   unsigned long long* digit_tiles;  // optional: [0] five-digit tiles, [1] six-digit tiles (counted per CTA)
 };
 
@@ -514,12 +517,12 @@ __device__ __forceinline__ float byte_digit(uint32_t w, int j) {
 }
 
 // V = round(x * 2^sh) to nearest, ties to even, |V| < 2^(8D - 1), as D
-// balanced base-256 digits d (d[D-1] the lowest).  Ties are frequent: a value
-// written by an earlier pass at one tile's scale is exact at that scale, and
-// a tile of this pass may have a coarser one, so the dropped bits are often
-// exactly one half; rounding them to even keeps the rounding unbiased (away
-// from zero would grow every such magnitude, and the norm with them).
-// With W = V + 128 (1 + 2^8 + ... + 2^(8(D-1))) every
+// balanced base-256 digits d (d[D-1] the lowest).  A value a digit pass wrote
+// is an integer of the unit already and converts exactly; other values (the
+// first digit pass of a circuit) round once, and ties round to even so that
+// the rounding has no bias (away from zero would grow every tie's
+// magnitude, and the norm with them).  With W = V + 128 (1 + 2^8 + ... +
+// 2^(8(D-1))) every
 // byte of W is its digit plus 128 (the added 128s absorb the borrows), and
 // the top digit is W / 2^(8(D-1)) - 128.  False when |x * 2^sh| >= 2^(8D-1)
 // (the scale does not cover x).
@@ -569,32 +572,25 @@ __device__ __forceinline__ double double_of(long long V, int e) {
   return __longlong_as_double((long long)(sgn | ((unsigned long long)E << 52) | mant));
 }
 
-// An integer upper bound of x^2 in units of 2^(2 eg - 50): with ex the
-// biased exponent of x and m8 its top 8 mantissa bits, |x| < (257 + m8)
-// 2^(ex - 1031), so x^2 < (257 + m8)^2 2^k units with k = 2 (ex - eg) -
-// 2012, rounded up.  Zero gives 0, a subnormal 1.  |x| < 2^(eg - 1) makes
-// k <= 30, so a tile's sum stays below 2^62; integer sums are exact and
-// independent of the order of the reduction.
-__device__ __forceinline__ unsigned long long sq_bound(double x, int eg) {
+// An integer upper bound of x^2 in units of 2^(2e - 50) (s = 2^e the
+// state's scale), clamped to kDgWarpBound: with ex the biased exponent of x
+// and m8 its top 8 mantissa bits, |x| < (257 + m8) 2^(ex - 1031), so x^2 <
+// (257 + m8)^2 2^k units with k = 2 (ex - e) - 2012, rounded up.  Zero gives
+// 0, a subnormal 1.  A tile whose warps each sum below kDgWarpBound units
+// has ||tile||^2 < 32 * 2^27 * 2^(2e - 50) = (2^-9 s)^2.  Integer sums are
+// exact and independent of the reduction order.
+__device__ __forceinline__ uint32_t sq_bound_units(double x, int e) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
   if (b == 0) return 0;
   const int ex = (int)(b >> 52);
   if (ex == 0) return 1;
   const uint32_t u = 257u + (uint32_t)((b >> 44) & 255u);
-  const unsigned long long u2 = (unsigned long long)(u * u);
-  const int k = 2 * (ex - eg) - 2012;
-  if (k >= 0) return u2 << (k < 30 ? k : 30);
+  const uint32_t u2 = u * u;  // below 2^19
+  const int k = 2 * (ex - e) - 2012;
+  if (k >= 11) return kDgWarpBound;               // u2 >= 2^16: the term alone reaches the bound
+  if (k >= 0) return min(u2 << k, kDgWarpBound);  // below 2^29 before the min
   if (k <= -19) return 1;
-  return (u2 + (1ull << -k) - 1) >> -k;
-}
-
-// The tile's scale exponent e_t from its bound S (units 2^(2 eg - 50)):
-// ||tile||^2 <= S 2^(2 eg - 50) < 2^(L + 2 eg - 50) with L the bit length of
-// S, so 2^(2 e_t) >= 4 ||tile||^2 holds when 2 e_t >= L + 2 eg - 48, i.e.
-// for e_t = eg - 24 + ceil(L / 2).
-__device__ __forceinline__ int tile_scale_exp(unsigned long long S, int eg) {
-  const int L = S ? 64 - __clzll((long long)S) : 0;
-  return eg - 24 + ((L + 1) >> 1);
+  return (u2 + (1u << -k) - 1) >> -k;
 }
 
 template <int D>
@@ -630,82 +626,117 @@ struct DgFixed {
   uint64_t free_pos, grid_base;  // next tile's base: ((base | ~free_pos) + grid_base) & free_pos
 };
 
-// One tile in D digits at scale 2^e: the loaded values v into the A planes,
-// the pass's blocks, the FP64 results back to the state.  False when a
-// bounded wait expired (the CTA then stops).
-template <int D>
-__device__ __forceinline__ bool dg_tile(const DgPassArgs& a, const DgFixed& f, DgPipe& p, const double2* v,
-                                        const uint2& load_dest, uint64_t obase, bool has_next, int e) {
-  const int tid = threadIdx.x;
-  const int sh = 8 * D - e;  // x / 2^e * 2^(8D) = x * 2^sh
-  unsigned char* sm = f.sm;
-#pragma unroll
-  for (int el = 0; el < 2 * kDgLoadIters; ++el) {
-    float dr[D], di[D];
-    p.range_ok &= digits_of<D>(v[el].x, sh, dr);
-    p.range_ok &= digits_of<D>(v[el].y, sh, di);
-    const uint32_t off = dest_at4(load_dest, el) << 2;
-#pragma unroll
-    for (int q = 0; q < D; ++q)
-      *reinterpret_cast<uint32_t*>(sm + (uint32_t)q * kDgPlane + off) = pack_bf16(dr[q], di[q]);
+// The MMA groups of a five-digit block in the order in which the previous
+// block's epilogue produces its A planes: stage 0 once planes 4 and 3 are
+// written, stage 1 once planes 2 and 1 are, stage 2 once plane 0 is; each
+// level is initialised by the first group that reaches it in this order.
+// The 20 digit pairs are those of BF_DG_GROUPS5, split finer.
+#define BF_DG_STAGED5                                                          \
+  {                                                                            \
+    {4, 0, 2, 1}, {3, 0, 1, 1}, {3, 1, 2, 0},                 /* stage 0 */   \
+        {2, 0, 1, 1}, {2, 1, 3, 0}, {1, 0, 1, 1}, {1, 1, 4, 0}, /* stage 1 */ \
+        {0, 0, 1, 1}, {0, 1, 4, 0}, {0, 5, 1, 0}              /* stage 2 */   \
   }
-  fence_proxy_async();
-  __syncthreads();
+__device__ __forceinline__ DgGroup dg_staged5(int gi) {
+  constexpr DgGroup g[10] = BF_DG_STAGED5;
+  return g[gi];
+}
 
+// the 4 MMAs (K = 16 each) of one group: A plane i against nj stacked B
+// planes j0.. (N = 64 nj) into levels i + j0 .. i + j0 + nj - 1, consecutive
+// 64-column ranges of tensor memory; an initialising group overwrites at
+// K step 0, the others accumulate
+__device__ __forceinline__ void dg_mma_group(const DgFixed& f, uint32_t sBk, const DgGroup gr) {
+  const uint32_t idn = f.idesc_base | ((uint32_t)(8 * gr.nj) << 17);
+#pragma unroll
+  for (int ks = 0; ks < 4; ++ks) {
+    const uint64_t ad = sdesc(f.sA + (uint32_t)gr.i * kDgPlane + (uint32_t)ks * 32u);
+    const uint64_t bd = sdesc(sBk + (uint32_t)gr.j0 * 8192u + (uint32_t)ks * 32u);
+    mma_bf16(f.tmem + 64u * (uint32_t)(gr.i + gr.j0), ad, bd, idn, (gr.init && ks == 0) ? 0u : 1u);
+  }
+}
+
+// Thread 0, before the first MMA of the CTA's block k: waits (bounded) for
+// its image in buffer k & 1; false when the wait expired.
+__device__ __forceinline__ bool dg_wait_image(const DgFixed& f, const DgPassArgs& a, DgPipe& p, uint32_t k) {
+  const uint32_t kb = k & 1u;
+  if (!mbar_wait(f.bar_b + 8u * kb, (k >> 1) & 1u, a.spin_limit)) return false;
+  p.b_in_flight &= ~(1 << kb);
+  tc_fence_after();
+  return true;
+}
+
+// Thread 0, after the last MMA of the CTA's block k (block bi of the pass):
+// commits them to the MMA barrier and loads the image of the block after it
+// (the pass's next block, or the next tile's first) into the other buffer,
+// whose last reader (block k - 1's MMAs) has completed.
+__device__ __forceinline__ void dg_commit(const DgFixed& f, const DgPassArgs& a, DgPipe& p, uint32_t k, int bi,
+                                          uint64_t obase, bool has_next) {
+  mma_commit(f.bar_mma);
+  p.issued = true;
+  const Blk5* nb = nullptr;
+  uint64_t nbase = obase;
+  if (bi + 1 < a.nblocks) {
+    nb = &f.blk[bi + 1];
+  } else if (has_next) {
+    nb = &f.blk[0];
+    nbase = ((obase | ~f.free_pos) + f.grid_base) & f.free_pos;
+  }
+  if (nb) {
+    const uint32_t kn = (k + 1) & 1u;
+    load_image_bytes(f.sB + kn * kDigitImageBytes,
+                     a.images + (size_t)(nb->img + variant_of(*nb, nbase)) * kDigitImageBytes, f.bar_b + 8u * kn,
+                     kDigitImageBytes);
+    p.b_in_flight |= 1 << kn;
+  }
+}
+
+__device__ __forceinline__ void named_bar_sync(uint32_t id, uint32_t n) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+__device__ __forceinline__ void named_bar_arrive(uint32_t id, uint32_t n) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
+// The pass's blocks on one tile whose A planes hold its D digits, then its
+// FP64 results (unit 2^(e - 48)) back to the state.  False when a bounded
+// wait expired (the CTA then stops).
+//
+// A five-digit block's epilogue issues the next block's MMAs as their A
+// planes appear (BF_DG_STAGED5): thread 0 waits at a named barrier that the
+// other warps pass without waiting (bar.arrive) once they have written the
+// planes and read the tensor-memory levels the stage overwrites, so that
+// the first stages run on the tensor cores under the rest of the epilogue.
+template <int D>
+__device__ __forceinline__ bool dg_tile(const DgPassArgs& a, const DgFixed& f, DgPipe& p, uint64_t obase,
+                                        bool has_next, int e) {
+  constexpr bool kStaged = D == kDgFewDigits;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  unsigned char* sm = f.sm;
+  // the tile's first block: every group, after the conversion's barrier
+  bool issue_lost = false;  // thread 0: the image of the block to run never arrived
+  if (tid == 0) {
+    if (dg_wait_image(f, a, p, p.kimg)) {
+      const uint32_t sBk = f.sB + (p.kimg & 1u) * kDigitImageBytes;
+#pragma unroll
+      for (int gi = 0; gi < kDgGroupCount<D>; ++gi) dg_mma_group(f, sBk, dg_group<D>(gi));
+      dg_commit(f, a, p, p.kimg, 0, obase, has_next);
+    } else {
+      issue_lost = true;
+    }
+  }
   for (int bi = 0; bi < a.nblocks; ++bi) {
     const bool more = bi + 1 < a.nblocks;
+    const uint32_t k = p.kimg;  // this block
+    const uint32_t sBn = f.sB + ((k + 1) & 1u) * kDigitImageBytes;
     const uint2 dest = my_dests4(a.offsets, f.blk[bi].offs);
-    bool lost = false;
-    const uint32_t kb = p.kimg & 1u;
-    const uint32_t ph_mma = p.kimg & 1u;
-    const uint32_t sBk = f.sB + kb * kDigitImageBytes;
-    if (tid == 0) {
-      if (mbar_wait(f.bar_b + 8u * kb, (p.kimg >> 1) & 1u, a.spin_limit)) {
-        p.b_in_flight &= ~(1 << kb);
-        tc_fence_after();
-        p.issued = true;
-        // A plane i against nj stacked B planes j0.. (N = 64 nj) writes
-        // levels i + j0 .. i + j0 + nj - 1, which are consecutive 64-column
-        // ranges of tensor memory; the first group to reach a level
-        // initialises it (at K step 0), the others accumulate.
-#pragma unroll
-        for (int gi = 0; gi < kDgGroupCount<D>; ++gi) {
-          const DgGroup gr = dg_group<D>(gi);
-          const uint32_t idn = f.idesc_base | ((uint32_t)(8 * gr.nj) << 17);
-#pragma unroll
-          for (int ks = 0; ks < 4; ++ks) {
-            const uint64_t ad = sdesc(f.sA + (uint32_t)gr.i * kDgPlane + (uint32_t)ks * 32u);
-            const uint64_t bd = sdesc(sBk + (uint32_t)gr.j0 * 8192u + (uint32_t)ks * 32u);
-            mma_bf16(f.tmem + 64u * (uint32_t)(gr.i + gr.j0), ad, bd, idn, (gr.init && ks == 0) ? 0u : 1u);
-          }
-        }
-        mma_commit(f.bar_mma);
-        // the next block's image into the other buffer, whose last reader
-        // (the previous block's MMAs) has completed
-        const Blk5* nb = nullptr;
-        uint64_t nbase = obase;
-        if (more) {
-          nb = &f.blk[bi + 1];
-        } else if (has_next) {
-          nb = &f.blk[0];
-          nbase = ((obase | ~f.free_pos) + f.grid_base) & f.free_pos;
-        }
-        if (nb) {
-          load_image_bytes(f.sB + (kb ^ 1u) * kDigitImageBytes,
-                           a.images + (size_t)(nb->img + variant_of(*nb, nbase)) * kDigitImageBytes,
-                           f.bar_b + 8u * (kb ^ 1u), kDigitImageBytes);
-          p.b_in_flight |= 1 << (kb ^ 1u);
-        }
-      } else {
-        lost = true;  // the image never arrived: no MMAs; the MMA wait below expires
-      }
-    }
-    ++p.kimg;
+    bool lost = issue_lost;     // no MMAs were issued: the wait below expires too
+    bool next_ok = true;        // thread 0: the next block's image arrived
+    if (!mbar_wait(f.bar_mma, k & 1u, a.spin_limit)) lost = true;
+    tc_fence_after();
     // Level s holds digit position s + 1 of the result.  From the lowest
     // level up: t = sum + carry, digit = t - 256 round(t / 256), carry the
     // rest; positions D and D + 1 only round; position 0 is the last carry.
-    if (!mbar_wait(f.bar_mma, ph_mma, a.spin_limit)) lost = true;
-    tc_fence_after();
     float carry[kDgCols];
 #pragma unroll
     for (int c = 0; c < kDgCols; ++c) carry[c] = 0.f;
@@ -729,12 +760,35 @@ __device__ __forceinline__ bool dg_tile(const DgPassArgs& a, const DgFixed& f, D
                 pack_bf16(d[2 * c], d[2 * c + 1]);
         }
       };
+      // the planes written so far and the levels read so far are handed to
+      // thread 0, which issues groups [g0, g1) of the staged order
+      auto handoff = [&](const uint32_t id, const int g0, const int g1) {
+        fence_proxy_async();
+        tc_fence_before();
+        if (warp == 0) {
+          named_bar_sync(id, kDgThreads);
+          if (tid == 0 && !issue_lost) {
+            tc_fence_after();
+            if (g0 == 0) next_ok = dg_wait_image(f, a, p, k + 1);
+            if (next_ok) {
+#pragma unroll
+              for (int gi = g0; gi < g1; ++gi) dg_mma_group(f, sBn, dg_staged5(gi));
+            }
+          }
+        } else {
+          named_bar_arrive(id, kDgThreads);
+        }
+      };
 #pragma unroll
       for (int s = D; s >= 1; s -= 2) {
         float d0[kDgCols], d1[kDgCols];
         tmem_ld8x2(f.tlane + 64u * (uint32_t)s, f.tlane + 64u * (uint32_t)(s - 1), d0, d1);
         level(s, d0);
         level(s - 1, d1);
+        if constexpr (kStaged) {
+          if (s == 3) handoff(1, 0, 3);  // planes 4, 3 written; levels 5..2 read
+          if (s == 1) handoff(2, 3, 7);  // planes 2, 1 written; every level read
+        }
       }
       if ((D + 1) & 1) {
         float d0[kDgCols];
@@ -788,14 +842,38 @@ __device__ __forceinline__ bool dg_tile(const DgPassArgs& a, const DgFixed& f, D
         const long long vi = (long long)(hi[2 * c + 1] + int_of_small(carry[2 * c + 1]) * (1 << (8 * (D - 4)))) *
                                  16777216ll +
                              (long long)lo[2 * c + 1];
-        stage[dest_at4(dest, c)] = make_double2(double_of(vr, e - 8 * D), double_of(vi, e - 8 * D));
+        stage[dest_at4(dest, c)] = make_double2(double_of(vr, e - 48), double_of(vi, e - 48));
       }
     }
-    if (tid == 0 && lost && p.issued) p.mma_lost_phase = (int)ph_mma;
+    if (tid == 0 && lost && p.issued) p.mma_lost_phase = (int)(k & 1u);
+    ++p.kimg;
     tc_fence_before();
     if (__syncthreads_or(lost ? 1 : 0)) {
       if (tid == 0) atomicExch(a.flag, 1);
       return false;
+    }
+    // the next block's remaining MMAs: every group of a six-digit block,
+    // the last stage of a five-digit one
+    issue_lost = false;
+    if (more && tid == 0) {
+      tc_fence_after();
+      if (kStaged) {
+        if (next_ok) {
+#pragma unroll
+          for (int gi = 7; gi < 10; ++gi) dg_mma_group(f, sBn, dg_staged5(gi));
+          dg_commit(f, a, p, k + 1, bi + 1, obase, has_next);
+        } else {
+          issue_lost = true;
+        }
+      } else {
+        if (dg_wait_image(f, a, p, k + 1)) {
+#pragma unroll
+          for (int gi = 0; gi < kDgGroupCount<D>; ++gi) dg_mma_group(f, sBn, dg_group<D>(gi));
+          dg_commit(f, a, p, k + 1, bi + 1, obase, has_next);
+        } else {
+          issue_lost = true;
+        }
+      }
     }
   }
   const double2* stage = reinterpret_cast<const double2*>(sm);
@@ -817,7 +895,6 @@ __global__ void __launch_bounds__(kDgThreads, 1) k_tblock_dg(const DgPassArgs a)
   uint64_t* hoff = reinterpret_cast<uint64_t*>(sm + kDgSmemHoff);
   uint64_t* bars = reinterpret_cast<uint64_t*>(sm + kDgSmemBar);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + kDgSmemBar + 72);
-  unsigned long long* red = reinterpret_cast<unsigned long long*>(sm + kDgSmemRed);
   Blk5* blk = reinterpret_cast<Blk5*>(sm + kDgSmemBlk);
   // bars[0], bars[1]: image buffers; bars[2]: the MMAs of a block
   const uint32_t bar_b = smem_u32(&bars[0]), bar_mma = smem_u32(&bars[2]);
@@ -860,7 +937,8 @@ __global__ void __launch_bounds__(kDgThreads, 1) k_tblock_dg(const DgPassArgs a)
   f.bar_mma = bar_mma;
   // kind::f16: D FP32, A and B BF16, both K-major, M = 128 (N set per MMA)
   f.idesc_base = (1u << 4) | (1u << 7) | (1u << 10) | ((128u >> 4) << 24);
-  const int eg = *a.scale_exp;
+  const int e = *a.scale_exp + a.scale_shift;
+  const int sh = 48 - e;  // x / 2^e * 2^48 = x * 2^sh: the value in units
 
   DgPipe p;
   p.kimg = 0;
@@ -885,8 +963,6 @@ __global__ void __launch_bounds__(kDgThreads, 1) k_tblock_dg(const DgPassArgs a)
   const uint64_t free_pos = ((a.ntiles << kBlockTileQubits) - 1) & ~tpos;
   const uint64_t grid_base = tile_base(gridDim.x);
   auto step_base = [&](uint64_t b) { return ((b | ~free_pos) + grid_base) & free_pos; };
-  f.free_pos = free_pos;
-  f.grid_base = grid_base;
   f.free_pos = free_pos;
   f.grid_base = grid_base;
   uint64_t tile = blockIdx.x;
@@ -917,25 +993,47 @@ __global__ void __launch_bounds__(kDgThreads, 1) k_tblock_dg(const DgPassArgs a)
       const double2* row = a.s + (step_base(obase) | hoff[tid]);
       asm volatile("cp.async.bulk.prefetch.L2.global [%0], 512;" ::"l"(row) : "memory");
     }
-    // the tile's norm bound, summed exactly over the CTA
-    unsigned long long sb = 0;
+    // Five digits unless a value needs six or the tile's norm may reach
+    // 2^-9 s: each warp sums its exact bound (a thread's own sum is clamped
+    // just below the bound, and flagged when it reaches it, so that the warp
+    // sum cannot overflow), and the barrier after the conversion ORs the
+    // verdicts.
+    bool six = false;
+    uint32_t tb = 0;
 #pragma unroll
-    for (int el = 0; el < 2 * kDgLoadIters; ++el) sb += sq_bound(v[el].x, eg) + sq_bound(v[el].y, eg);
+    for (int el = 0; el < 2 * kDgLoadIters; ++el) {
+      float dr[kDgFewDigits], di[kDgFewDigits];
+      six |= !digits_of<kDgFewDigits>(v[el].x, sh, dr);
+      six |= !digits_of<kDgFewDigits>(v[el].y, sh, di);
+      tb += sq_bound_units(v[el].x, e) + sq_bound_units(v[el].y, e);
+      const uint32_t off = dest_at4(load_dest, el) << 2;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) sb += __shfl_xor_sync(0xffffffffu, sb, o);
-    if (lane == 0) red[warp] = sb;
-    __syncthreads();
-    sb = red[lane];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) sb += __shfl_xor_sync(0xffffffffu, sb, o);
-    const int et = tile_scale_exp(sb, eg);
+      for (int q = 0; q < kDgFewDigits; ++q)
+        *reinterpret_cast<uint32_t*>(sm + (uint32_t)q * kDgPlane + off) = pack_bf16(dr[q], di[q]);
+    }
+    const bool big = tb >= kDgWarpBound;
+    const uint32_t ws = __reduce_add_sync(0xffffffffu, big ? kDgWarpBound - 1 : tb);
+    six |= big || ws >= kDgWarpBound || !a.five_digits;
+    fence_proxy_async();
     bool ok;
-    if (et <= eg - a.few_digits_slack) {
-      if (tid == 0) ++tiles_by_digits[0];
-      ok = dg_tile<kDgFewDigits>(a, f, p, v, load_dest, obase, has_next, et);
-    } else {
+    if (__syncthreads_or(six ? 1 : 0)) {
+#pragma unroll
+      for (int el = 0; el < 2 * kDgLoadIters; ++el) {
+        float dr[kDigits], di[kDigits];
+        p.range_ok &= digits_of<kDigits>(v[el].x, sh, dr);
+        p.range_ok &= digits_of<kDigits>(v[el].y, sh, di);
+        const uint32_t off = dest_at4(load_dest, el) << 2;
+#pragma unroll
+        for (int q = 0; q < kDigits; ++q)
+          *reinterpret_cast<uint32_t*>(sm + (uint32_t)q * kDgPlane + off) = pack_bf16(dr[q], di[q]);
+      }
+      fence_proxy_async();
+      __syncthreads();
       if (tid == 0) ++tiles_by_digits[1];
-      ok = dg_tile<kDigits>(a, f, p, v, load_dest, obase, has_next, et < eg ? et : eg);
+      ok = dg_tile<kDigits>(a, f, p, obase, has_next, e);
+    } else {
+      if (tid == 0) ++tiles_by_digits[0];
+      ok = dg_tile<kDgFewDigits>(a, f, p, obase, has_next, e);
     }
     if (!ok) failed = true;
   }
@@ -1013,11 +1111,14 @@ void launch_block_pass_digits(State& st, const Blk5* d_blocks, int nblocks, cons
   a.scale_exp = d_exp;
   a.flag = state_flag(st);
   a.spin_limit = 1u << 24;
-  // five-digit tiles need a scale 2^8 below the state's; a test may move the
-  // threshold (a negative slack makes every tile five-digit) to exercise both
-  // forms on small states
-  const char* slack = std::getenv("BFGPU_DIGIT_SLACK");
-  a.few_digits_slack = (slack && *slack) ? std::atoi(slack) : kDgFewDigitsSlack;
+  // A test may raise the scale by 2^shift (a coarser unit) so that the
+  // tiles of a small state fall below 2^-9 of it and run five digits.
+  const char* shift = std::getenv("BFGPU_DIGIT_SCALE_SHIFT");
+  a.scale_shift = (shift && *shift) ? std::atoi(shift) : 0;
+  // five-digit tiles hold the same integers as six-digit ones; a test may
+  // turn them off to compare the two bit for bit
+  const char* five = std::getenv("BFGPU_DIGIT_FIVE");
+  a.five_digits = (five && *five == '0') ? 0 : 1;
   a.digit_tiles = digit_tile_counters(st);
   static PerDeviceOnce configured;
   configured.run(st.device, [] {

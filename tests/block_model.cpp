@@ -15,10 +15,11 @@
 //
 // Mode digits-exact follows the complex128 digit kernel's arithmetic step
 // by step instead: the state's scale from the norm before the first digit
-// pass; per tile, the exact integer bound of its norm, its own scale and its
-// digit count (five when that scale is 2^8 or more below the state's, six
-// otherwise; BFGPU_DIGIT_SLACK moves the threshold as it does for the
-// kernel); each value rounded to that many balanced base-256 digits, exact
+// pass and its unit 2^-48 of it (BFGPU_DIGIT_SCALE_SHIFT raises the scale as
+// it does for the kernel); per tile, the digit count (five when every warp's
+// exact integer bound puts the tile's norm below 2^-9 of the scale and every
+// value fits, six otherwise); each value rounded to that many balanced
+// base-256 digits of the unit, exact
 // integer level sums of the kept digit pairs (20 or 26), the carries with
 // round-half-even, and the FP64 result after the last block, so that the
 // model gives the bits the kernel gives.  It prints the passes by kind and
@@ -120,35 +121,48 @@ static void value_digits_of(double x, int sh, int D, int* d) {
   d[0] = (int)V;
 }
 
-// the kernel's integer bound of x^2 in units of 2^(2 eg - 50): (257 + the
-// top 8 mantissa bits)^2 2^k, k = 2 (ex - eg) - 2012, rounded up
-static unsigned long long sq_bound(double x, int eg) {
+// the kernel's integer bound of x^2 in units of 2^(2e - 50), clamped to
+// 2^27: (257 + the top 8 mantissa bits)^2 2^k, k = 2 (ex - e) - 2012,
+// rounded up
+static uint32_t sq_bound_units(double x, int e) {
+  const uint32_t cap = 1u << 27;
   unsigned long long b;
   std::memcpy(&b, &x, 8);
   b &= 0x7FFFFFFFFFFFFFFFull;
   if (b == 0) return 0;
   const int ex = (int)(b >> 52);
   if (ex == 0) return 1;
-  const unsigned long long u = 257u + ((b >> 44) & 255u);
-  const int k = 2 * (ex - eg) - 2012;
-  if (k >= 0) return (u * u) << std::min(k, 30);
+  const uint32_t u = 257u + (uint32_t)((b >> 44) & 255u);
+  const uint32_t u2 = u * u;
+  const int k = 2 * (ex - e) - 2012;
+  if (k >= 11) return cap;
+  if (k >= 0) return std::min(u2 << k, cap);
   if (k <= -19) return 1;
-  return (u * u + (1ull << -k) - 1) >> -k;
+  return (u2 + (1u << -k) - 1) >> -k;
 }
 
-// digits and scale exponent of a tile from its bound S: e_t = eg - 24 +
-// ceil((bit length of S) / 2); five digits when e_t <= eg - slack
-static void tile_digits(unsigned long long S, int eg, int slack, int* D, int* e) {
-  int L = 0;
-  while (L < 64 && (S >> L) != 0) ++L;
-  const int et = eg - 24 + ((L + 1) >> 1);
-  if (et <= eg - slack) {
-    *D = 5;
-    *e = et;
-  } else {
-    *D = 6;
-    *e = std::min(et, eg);
+// the kernel's digit count for a tile: five unless a value needs six digits
+// (|x| 2^sh >= 2^39) or a warp's bound (its threads' sums, each clamped just
+// below 2^27 and flagged when it reaches it) reaches 2^27
+static int tile_digit_count(const std::vector<double>& vals_by_thread, int e, int sh) {
+  const uint32_t cap = 1u << 27;
+  bool six = false;
+  const int T = kDigitThreads, per = (int)(vals_by_thread.size() / T);
+  for (int w = 0; w < T / 32 && !six; ++w) {
+    uint32_t ws = 0;
+    for (int l = 0; l < 32; ++l) {
+      uint32_t tb = 0;
+      for (int k = 0; k < per; ++k) {
+        const double x = vals_by_thread[(size_t)(w * 32 + l) * per + k];
+        tb += sq_bound_units(x, e);
+        if (std::ldexp(std::fabs(x), sh) >= 549755813888.0) six = true;  // 2^39
+      }
+      if (tb >= cap) six = true;
+      ws += tb >= cap ? cap - 1 : tb;
+    }
+    if (ws >= cap) six = true;
   }
+  return six ? 6 : 5;
 }
 
 // the six digits e_0..e_5 of every entry of an image's 64x64 real matrix, [n][k]
@@ -169,7 +183,7 @@ static void image_digits(const unsigned char* img, int (*b)[64][64]) {
 
 static void run_digit_pass_exact(std::vector<cd>& s, int n, const TilePass& tp, const std::vector<Blk5>& blocks,
                                  const std::vector<unsigned char>& images, const std::vector<uint16_t>& offsets,
-                                 int e_scale, int slack, long long* tiles_by_digits) {
+                                 int e_scale, bool five_digits, long long* tiles_by_digits) {
   const int T = kDigitThreads, E = kBlockTableEntries / T;
   std::vector<int> g_of(4096), j_of(4096);
   for (uint32_t g = 0; g < 128; ++g)
@@ -195,12 +209,18 @@ static void run_digit_pass_exact(std::vector<cd>& s, int n, const TilePass& tp, 
     for (int j = 0; j < kBlockTileQubits; ++j) obase = insert_zero(obase, tp.q[j]);
     auto gi = [&](uint32_t i) { return obase | (i & 31u) | hoff[i >> 5]; };
     const uint16_t* load = offsets.data() + (size_t)blocks[0].load_offs * kBlockTableEntries;
-    unsigned long long S = 0;
-    for (uint32_t i = 0; i < 4096; ++i) S += sq_bound(s[gi(i)].real(), e_scale) + sq_bound(s[gi(i)].imag(), e_scale);
-    int D = kDigits, et = e_scale;
-    tile_digits(S, e_scale, slack, &D, &et);
+    // the values each thread loads, in its order: amplitudes i0, i0 + 1 of
+    // i0 = (it * T + t) * 2, real then imaginary part
+    const int sh = 48 - e_scale;
+    std::vector<double> by_thread((size_t)T * E * 2);
+    for (int t = 0; t < T; ++t)
+      for (int e = 0; e < E; ++e) {
+        const uint32_t i = (uint32_t)(((e >> 1) * T + t) * 2 + (e & 1));
+        by_thread[((size_t)t * E + e) * 2] = s[gi(i)].real();
+        by_thread[((size_t)t * E + e) * 2 + 1] = s[gi(i)].imag();
+      }
+    const int D = five_digits ? tile_digit_count(by_thread, e_scale, sh) : 6;
     ++tiles_by_digits[D == 5 ? 0 : 1];
-    const int sh = 8 * D - et;
     for (int t = 0; t < T; ++t)
       for (int e = 0; e < E; ++e) {
         const uint32_t i = (uint32_t)(((e >> 1) * T + t) * 2 + (e & 1));
@@ -253,8 +273,8 @@ static void run_digit_pass_exact(std::vector<cd>& s, int n, const TilePass& tp, 
           }
           const uint16_t to = dest[t * E + e];
           if (last) {
-            stage_re[to] = std::ldexp((double)V[0], et - 8 * D);
-            stage_im[to] = std::ldexp((double)V[1], et - 8 * D);
+            stage_re[to] = std::ldexp((double)V[0], e_scale - 48);
+            stage_im[to] = std::ldexp((double)V[1], e_scale - 48);
           } else {
             for (int p2 = 0; p2 < D; ++p2) {
               next[to].re[p2] = dig[0][p2];
@@ -335,10 +355,12 @@ int main(int argc, char** argv) {
   const bool exact = std::strcmp(argv[1], "digits-exact") == 0;
   const bool digits = exact || std::strcmp(argv[1], "digits") == 0;
   int e_scale = 0;  // the digit scale, from the norm before the first digit pass
-  // five-digit tiles need a scale 2^slack below the state's (as the kernel,
-  // including its test override)
-  const char* slack_env = std::getenv("BFGPU_DIGIT_SLACK");
-  const int slack = (slack_env && *slack_env) ? std::atoi(slack_env) : 8;
+  // the kernel's test overrides: the scale raised by 2^shift, five-digit
+  // tiles turned off
+  const char* shift_env = std::getenv("BFGPU_DIGIT_SCALE_SHIFT");
+  const int scale_shift = (shift_env && *shift_env) ? std::atoi(shift_env) : 0;
+  const char* five_env = std::getenv("BFGPU_DIGIT_FIVE");
+  const bool five_digits = !(five_env && *five_env == '0');
   long long tiles_by_digits[2] = {0, 0};
   std::ifstream fo(argv[2], std::ios::binary);
   std::vector<char> blob((std::istreambuf_iterator<char>(fo)), {});
@@ -376,7 +398,8 @@ int main(int argc, char** argv) {
           std::frexp(std::sqrt(nrm2) * (1.0 + 1e-6), &k);
           e_scale = nrm2 > 0 ? k + 1 : 1;
         }
-        run_digit_pass_exact(s, n, ps.tile, blocks, images, offsets, e_scale, slack, tiles_by_digits);
+        run_digit_pass_exact(s, n, ps.tile, blocks, images, offsets, e_scale + scale_shift, five_digits,
+                             tiles_by_digits);
       } else {
         run_block_pass(s, n, ps.tile, blocks, images, offsets, digits);
       }

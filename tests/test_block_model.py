@@ -34,15 +34,16 @@ def model(tmp_path_factory):
     return exe
 
 
-def run_model(exe, fmt, qc, re, im, tmp_path, slack=None, tiles=False):
+def run_model(exe, fmt, qc, re, im, tmp_path, shift=None, tiles=False):
     import os
     ops, sin, sout = tmp_path / "ops.bin", tmp_path / "in.bin", tmp_path / "out.bin"
     ops.write_bytes(bfy.serialize(qc))
     (re + 1j * im).astype(np.complex128).tofile(sin)
     env = dict(os.environ)
-    env.pop("BFGPU_DIGIT_SLACK", None)
-    if slack is not None:
-        env["BFGPU_DIGIT_SLACK"] = str(slack)
+    env.pop("BFGPU_DIGIT_SCALE_SHIFT", None)
+    env.pop("BFGPU_DIGIT_FIVE", None)
+    if shift is not None:
+        env["BFGPU_DIGIT_SCALE_SHIFT"] = str(shift)
     r = subprocess.run([str(exe), fmt, str(ops), str(sin), str(sout)], check=True, capture_output=True, text=True,
                        env=env)
     fields = [int(x) for x in r.stdout.split()]
@@ -127,35 +128,53 @@ def test_block_passes_match_the_oracle(model, fmt, name, tmp_path):
     assert err <= (1e-12 if fmt == "digits" else 1e-5), err
 
 
-@pytest.mark.parametrize("slack,tol", [(-100, 5e-11), (2, 3e-11)])
-def test_five_digit_tiles_match_the_oracle(model, slack, tol, tmp_path):
-    """Tiles in five digits (scale from the tile's own norm bound): forced on
-    every tile (slack -100: the tile's scale may then be above the state's,
-    a rounding unit of 2^-40 of it per block), and on the tiles whose scale
-    is 2^2 below the state's (16 qubits: a tile holds a quarter of the
-    norm)."""
-    qc = CIRCUITS["layered16x40"]() if slack == 2 else CIRCUITS["layered14"]()
+@pytest.mark.parametrize("shift,tol", [(10, 5e-9), (6, 1e-10)])
+def test_five_digit_tiles_match_the_oracle(model, shift, tol, tmp_path):
+    """Tiles in five digits: with the scale raised by 2^10 (a unit of
+    2^-38 of the norm) every tile of a 14-qubit state falls below 2^-9 of
+    it; with 2^6 the tiles of a 16-qubit state (a quarter of the norm each)
+    do.  The error follows the coarser unit."""
+    qc = CIRCUITS["layered16x40"]() if shift == 6 else CIRCUITS["layered14"]()
     n = qc.num_qubits
     re, im = W.random_normal_state(n, 7)
-    got, _, (five, six) = run_model(model, "digits-exact", qc, re, im, tmp_path, slack=slack, tiles=True)
-    assert five > 0 and (six == 0 if slack < 0 else True)
+    got, _, (five, six) = run_model(model, "digits-exact", qc, re, im, tmp_path, shift=shift, tiles=True)
+    assert five > 0 and six == 0
     r, i = O.run(qc, re, im)
     assert float(np.max(np.abs(got - (r + 1j * i)))) <= tol
 
 
-def test_default_threshold_keeps_six_digits_on_small_states(model, tmp_path):
-    """At 13 qubits a tile holds half the state's norm: its scale is within
-    2^8 of the state's, so every tile keeps six digits."""
+def test_default_scale_keeps_six_digits_on_small_states(model, tmp_path):
+    """At 13 qubits a tile holds half the state's norm, far above 2^-9 of
+    the scale, so every tile keeps six digits."""
     qc = CIRCUITS["layered13"]()
     re, im = W.random_normal_state(13, 7)
     _, _, (five, six) = run_model(model, "digits-exact", qc, re, im, tmp_path, tiles=True)
     assert five == 0 and six > 0
 
 
-def test_rescaled_tiles_keep_the_norm(model, tmp_path):
-    """Tiles of consecutive passes have different scales, so the load often
-    drops exactly one half of a unit; it rounds those ties to even.  The
-    circuit followed by its adjoint keeps the norm and returns the state."""
+def test_tiles_below_the_bound_run_five_digits_at_the_state_unit(model, tmp_path):
+    """A 16-qubit state whose norm sits almost entirely on qubit 15 = 0: the
+    passes' tiles on the other half hold far less than 2^-9 of the scale and
+    run five digits, at the same unit as the six-digit tiles, so the result
+    stays within 1e-12 of the oracle."""
+    n = 16
+    qc = W.random_layered_circuit(n, 2, seed=5)
+    re, im = W.random_normal_state(n, 8)
+    re[1 << 15:] *= 1e-4
+    im[1 << 15:] *= 1e-4
+    s = np.sqrt(np.sum(re * re + im * im))
+    re, im = re / s, im / s
+    got, _, (five, six) = run_model(model, "digits-exact", qc, re, im, tmp_path, tiles=True)
+    r, i = O.run(qc, re, im)
+    assert float(np.max(np.abs(got - (r + 1j * i)))) <= 1e-12
+    assert five > 0 and six > 0
+
+
+def test_five_digit_round_trip_keeps_the_norm(model, tmp_path):
+    """Five-digit tiles (scale raised by 2^6 at 16 qubits): the circuit
+    followed by its adjoint keeps the norm and returns the state; the load
+    of a value that a digit pass wrote is exact, and the first pass's
+    rounding of the input ties to even."""
     from code_mojo_gb300 import opsarray as OA
     n = 16
     fwd = W.random_layered_circuit(n, 12, seed=6)
@@ -166,8 +185,8 @@ def test_rescaled_tiles_keep_the_norm(model, tmp_path):
     qc = bfy.QuantumCircuit(n)
     qc.transformations = fwd.transformations + inv.transformations
     re, im = W.random_normal_state(n, 3)
-    got, _, (five, six) = run_model(model, "digits-exact", qc, re, im, tmp_path, slack=2, tiles=True)
+    got, _, (five, six) = run_model(model, "digits-exact", qc, re, im, tmp_path, shift=6, tiles=True)
     assert five > 0
-    assert abs(float(np.sum(np.abs(got) ** 2)) - 1.0) <= 2e-12
-    assert float(np.max(np.abs(got - (re + 1j * im)))) <= 5e-11
+    assert abs(float(np.sum(np.abs(got) ** 2)) - 1.0) <= 1e-11
+    assert float(np.max(np.abs(got - (re + 1j * im)))) <= 2e-10
     del OA

@@ -9,6 +9,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
+from code_mojo_gb300 import _ffi as F
 from code_mojo_gb300 import butterfly as bfy
 from code_mojo_gb300 import workloads as W
 from oracle import pyoracle as O
@@ -216,16 +217,16 @@ def test_plan_cache_tells_circuits_apart():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("slack", [None, -100, 1])
+@pytest.mark.parametrize("shift", [None, 10, 7])
 @pytest.mark.parametrize("layers,seed", [(8, 0), (12, 1), (16, 0)])
-def test_digit_passes_equal_the_arithmetic_model_bit_for_bit(layers, seed, slack, tmp_path, monkeypatch):
+def test_digit_passes_equal_the_arithmetic_model_bit_for_bit(layers, seed, shift, tmp_path, monkeypatch):
     """The GPU's digit passes give exactly the bits of the host model of the
-    digit arithmetic (tests/block_model.cpp, digits-exact): the same state
-    and tile scales, digit counts, digits, exact level sums and half-even
+    digit arithmetic (tests/block_model.cpp, digits-exact): the same scale
+    and unit, digit counts per tile, digits, exact level sums and half-even
     carries.  The circuits are planned as block passes only, so no
-    double-float pass is involved.  The default threshold keeps six digits
-    at 13 qubits; a slack of -100 makes every tile five-digit, and 1 mixes
-    the two forms by tile where the tiles' norms differ."""
+    double-float pass is involved.  At 13 qubits every tile keeps six
+    digits; with the scale raised by 2^10 every tile runs five, and with
+    2^7 the tiles run five or six by their norms."""
     import shutil
     import subprocess
     from pathlib import Path
@@ -253,12 +254,14 @@ def test_digit_passes_equal_the_arithmetic_model_bit_for_bit(layers, seed, slack
     (tmp_path / "ops.bin").write_bytes(bfy.serialize(qc))
     (re + 1j * im).astype(np.complex128).tofile(tmp_path / "in.bin")
     env = dict(os.environ)
-    env.pop("BFGPU_DIGIT_SLACK", None)
-    if slack is None:
-        monkeypatch.delenv("BFGPU_DIGIT_SLACK", raising=False)
+    env.pop("BFGPU_DIGIT_SCALE_SHIFT", None)
+    env.pop("BFGPU_DIGIT_FIVE", None)
+    monkeypatch.delenv("BFGPU_DIGIT_FIVE", raising=False)
+    if shift is None:
+        monkeypatch.delenv("BFGPU_DIGIT_SCALE_SHIFT", raising=False)
     else:
-        env["BFGPU_DIGIT_SLACK"] = str(slack)
-        monkeypatch.setenv("BFGPU_DIGIT_SLACK", str(slack))
+        env["BFGPU_DIGIT_SCALE_SHIFT"] = str(shift)
+        monkeypatch.setenv("BFGPU_DIGIT_SCALE_SHIFT", str(shift))
     r = subprocess.run([str(exe), "digits-exact", str(tmp_path / "ops.bin"), str(tmp_path / "in.bin"),
                         str(tmp_path / "out.bin")], check=True, capture_output=True, text=True, env=env)
     five_model, six_model = (int(x) for x in r.stdout.split()[3:5])
@@ -270,8 +273,38 @@ def test_digit_passes_equal_the_arithmetic_model_bit_for_bit(layers, seed, slack
     five, six = st.digit_tiles()
     st.close()
     assert (five, six) == (five_model, six_model)
-    if slack is None:
+    if shift is None:
         assert five == 0 and six > 0
-    elif slack < 0:
+    elif shift == 10:
         assert six == 0 and five > 0
     assert np.array_equal(got, model)
+
+
+@pytest.mark.gpu
+def test_five_digit_tiles_give_the_six_digit_bits(monkeypatch):
+    """Five-digit tiles hold the same fixed-point integers as six-digit ones
+    (their top digit is zero) and keep the same digit pairs, so a 27-qubit
+    circuit gives the same bits with five-digit tiles allowed (most tiles
+    take them) and forbidden."""
+    n = 27
+    qc = W.random_layered_circuit(n, 6, seed=3)
+    out = {}
+    monkeypatch.delenv("BFGPU_DIGIT_SCALE_SHIFT", raising=False)
+    for five in ("1", "0"):
+        monkeypatch.setenv("BFGPU_DIGIT_FIVE", five)
+        st = bfy.QuantumState(n)
+        st.digit_tiles(reset=True)
+        bfy.execute(st, qc, ctx(True))
+        counts = st.digit_tiles()
+        blk = 1 << 22
+        h = np.empty(1 << n, dtype=np.complex128)
+        for off in range(0, 1 << n, blk):
+            re = np.empty(blk)
+            im = np.empty(blk)
+            F.check(F.lib().bf_state_download_range(st.handle, off, blk, re.ctypes.data, im.ctypes.data))
+            h[off:off + blk] = re + 1j * im
+        st.close()
+        out[five] = (counts, h)
+    monkeypatch.delenv("BFGPU_DIGIT_FIVE", raising=False)
+    assert out["1"][0][0] > 0 and out["0"][0][0] == 0
+    assert np.array_equal(out["1"][1], out["0"][1])
