@@ -164,7 +164,7 @@ typedef struct bf_exec_opts {
                                 into 5-qubit blocks applied as tensor-core
                                 GEMMs (states of >= 12 qubits; per pass, where
                                 cheaper): 3xTF32 for complex64; for complex128
-                                exact products of 6 base-256 digits in bf16
+                                exact products of five or six base-256 digits in bf16
                                 (circuits of norm-preserving ops only).
                                 0: CUDA-core tile passes only               */
   int32_t plan_dtype;        /* bf_plan_stats only: plan as for a BF_C128
@@ -232,9 +232,9 @@ int bf_state_pass_timing(bf_state* st, int32_t enable);
 int bf_state_pass_times(bf_state* st, int64_t* counts, double* ms);
 /* complex128 digit passes: how many 4096-amplitude tiles ran with five and
  * with six base-256 digits since the state was created (or since the last
- * reset).  A tile takes five digits when its own scale (a power of two at
- * least twice the tile's norm) is 2^8 or more below the state's; waits for
- * the state's stream.  No counterpart in the reference. */
+ * reset).  A tile takes five digits (the same fixed-point values, its top
+ * digit being zero) when its norm is below 2^-9 of the state's digit scale;
+ * waits for the state's stream.  No counterpart in the reference. */
 int bf_state_digit_tiles(bf_state* st, uint64_t* five, uint64_t* six, int32_t reset);
 
 /* ---- reductions ---------------------------------------------------------- */
