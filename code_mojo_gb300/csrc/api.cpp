@@ -348,6 +348,10 @@ static double cuda_core_units(const TilePass& tp) {
 // pass's fixed cost)
 constexpr double kDigitBlockUnits = 5.0;
 
+// A block pass costs about this many blocks besides its blocks (loading,
+// converting and storing the tile).
+constexpr double kPassCostBlocks = 2.5;
+
 // True when every op keeps the state's norm (unitary gates and unitaries to
 // 1e-12, permutations and the classical Grover and modexp passes; not
 // measurement): the digit form's scale, taken from the norm before the
@@ -390,11 +394,15 @@ static void build_steps(int n, const bf_op* ops, int64_t nops, const bf_exec_opt
   tensor = tensor && fused && n >= kBlockTileQubits;
   if (tensor && format == BLOCK_DIGITS) tensor = norm_preserving(ops, nops);
   const double block_units = format == BLOCK_DIGITS ? kDigitBlockUnits : kBlockUnits;
+  // a pass's own cost in blocks (load, conversion, stores); BFGPU_PASS_COST
+  // overrides it for planner experiments
+  const char* pc = std::getenv("BFGPU_PASS_COST");
+  const double pass_cost = (pc && *pc) ? std::atof(pc) : kPassCostBlocks;
   const int K = tensor ? kBlockTileQubits : (o.tile_qubits > 0 ? o.tile_qubits : 11);
   std::vector<GateInstr> run;
   auto flush = [&]() {
     if (run.empty()) return;
-    for (auto& ps : plan_gates(n, run, K, true, tensor ? block_units : 0.0)) {
+    for (auto& ps : plan_gates(n, run, K, true, tensor ? block_units : 0.0, pass_cost)) {
       Step s;
       if (ps.is_tile && tensor && ps.tile.K == kBlockTileQubits && ps.tile.L == kTileLowQubits) {
         size_t b0 = pg.blocks.size(), i0 = pg.images.size(), o0 = pg.offsets.size();

@@ -349,9 +349,10 @@ struct PlanStep {
 // block_units > 0: tile passes may run as tensor-core blocks, one block
 // costing that many dense gates of the CUDA-core tile kernel; a pass whose
 // blocks would be cheaper gets its tile chosen for work per unit of
-// block-pass time rather than work per pass
+// block-pass time rather than work per pass, a pass costing pass_cost
+// blocks besides its blocks
 std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int K, bool allow_single = true,
-                                 double block_units = 0);
+                                 double block_units = 0, double pass_cost = 2.5);
 
 // bf_execute's body on a prepared state; stream, event and SM count of a
 // state; releasing every buffer a state owns (api.cpp).

@@ -320,7 +320,7 @@ static double pass_core_units(const std::vector<const GateInstr*>& remaining, ui
 }
 
 std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int K, bool allow_single,
-                                 double block_units) {
+                                 double block_units, double pass_cost) {
   std::vector<PlanStep> steps;
   if (gates.empty()) return steps;
   K = std::max(1, std::min(K, std::min(n, kMaxTileQubits)));
@@ -335,7 +335,7 @@ std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int
     // gates that could still join (first come), then single swaps of a chosen
     // qubit for another target while that improves the pass: more work, or
     // for passes that run as tensor-core blocks more work per unit of time
-    // (a pass costs about as much as 2.5 blocks besides its blocks)
+    // (a pass costs about as much as pass_cost blocks besides its blocks)
     uint64_t inQ = low;
     int nQ = L;
     // the qubits the remaining gates touch: once the deferred gates act
@@ -397,15 +397,15 @@ std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int
       const uint64_t by_work = search(start, work);
       if (block_units > 0) {
         // Passes that may run as tensor-core blocks: the tile that takes the
-        // most work per unit of time as blocks (a pass costs about 2.5 blocks
-        // besides its blocks), kept when its blocks beat the CUDA-core kernel
+        // most work per unit of time as blocks (a pass costs about pass_cost
+        // blocks besides its blocks), kept when its blocks beat the CUDA-core kernel
         // on the same gates and it does more work per unit of time than the
         // most-work tile does on the CUDA cores (same pass cost; a block
         // costs block_units dense gates).
-        auto block_rate = [&](uint64_t c) { return work(c) / (2.5 + pass_blocks(remaining, c, all)); };
+        auto block_rate = [&](uint64_t c) { return work(c) / (pass_cost + pass_blocks(remaining, c, all)); };
         const uint64_t set = search(start, block_rate);
         const double core = pass_core_units(remaining, set, all);
-        const double core_rate = work(by_work) / (2.5 + pass_core_units(remaining, by_work, all) / block_units);
+        const double core_rate = work(by_work) / (pass_cost + pass_core_units(remaining, by_work, all) / block_units);
         if ((double)pass_blocks(remaining, set, all) * block_units < core && block_rate(set) >= core_rate) {
           inQ = set;
           chosen = true;
