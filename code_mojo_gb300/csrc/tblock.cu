@@ -626,22 +626,6 @@ struct DgFixed {
   uint64_t free_pos, grid_base;  // next tile's base: ((base | ~free_pos) + grid_base) & free_pos
 };
 
-// The MMA groups of a five-digit block in the order in which the previous
-// block's epilogue produces its A planes: stage 0 once planes 4 and 3 are
-// written, stage 1 once planes 2 and 1 are, stage 2 once plane 0 is; each
-// level is initialised by the first group that reaches it in this order.
-// The 20 digit pairs are those of BF_DG_GROUPS5, split finer.
-#define BF_DG_STAGED5                                                          \
-  {                                                                            \
-    {4, 0, 2, 1}, {3, 0, 1, 1}, {3, 1, 2, 0},                 /* stage 0 */   \
-        {2, 0, 1, 1}, {2, 1, 3, 0}, {1, 0, 1, 1}, {1, 1, 4, 0}, /* stage 1 */ \
-        {0, 0, 1, 1}, {0, 1, 4, 0}, {0, 5, 1, 0}              /* stage 2 */   \
-  }
-__device__ __forceinline__ DgGroup dg_staged5(int gi) {
-  constexpr DgGroup g[10] = BF_DG_STAGED5;
-  return g[gi];
-}
-
 // the 4 MMAs (K = 16 each) of one group: A plane i against nj stacked B
 // planes j0.. (N = 64 nj) into levels i + j0 .. i + j0 + nj - 1, consecutive
 // 64-column ranges of tensor memory; an initialising group overwrites at
@@ -691,27 +675,13 @@ __device__ __forceinline__ void dg_commit(const DgFixed& f, const DgPassArgs& a,
   }
 }
 
-__device__ __forceinline__ void named_bar_sync(uint32_t id, uint32_t n) {
-  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
-}
-__device__ __forceinline__ void named_bar_arrive(uint32_t id, uint32_t n) {
-  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
-}
-
 // The pass's blocks on one tile whose A planes hold its D digits, then its
 // FP64 results (unit 2^(e - 48)) back to the state.  False when a bounded
 // wait expired (the CTA then stops).
-//
-// A five-digit block's epilogue issues the next block's MMAs as their A
-// planes appear (BF_DG_STAGED5): thread 0 waits at a named barrier that the
-// other warps pass without waiting (bar.arrive) once they have written the
-// planes and read the tensor-memory levels the stage overwrites, so that
-// the first stages run on the tensor cores under the rest of the epilogue.
 template <int D>
 __device__ __forceinline__ bool dg_tile(const DgPassArgs& a, const DgFixed& f, DgPipe& p, uint64_t obase,
                                         bool has_next, int e) {
-  constexpr bool kStaged = D == kDgFewDigits;
-  const int tid = threadIdx.x, warp = tid >> 5;
+  const int tid = threadIdx.x;
   unsigned char* sm = f.sm;
   // the tile's first block: every group, after the conversion's barrier
   bool issue_lost = false;  // thread 0: the image of the block to run never arrived
@@ -731,7 +701,6 @@ __device__ __forceinline__ bool dg_tile(const DgPassArgs& a, const DgFixed& f, D
     const uint32_t sBn = f.sB + ((k + 1) & 1u) * kDigitImageBytes;
     const uint2 dest = my_dests4(a.offsets, f.blk[bi].offs);
     bool lost = issue_lost;     // no MMAs were issued: the wait below expires too
-    bool next_ok = true;        // thread 0: the next block's image arrived
     if (!mbar_wait(f.bar_mma, k & 1u, a.spin_limit)) lost = true;
     tc_fence_after();
     // Level s holds digit position s + 1 of the result.  From the lowest
@@ -760,35 +729,12 @@ __device__ __forceinline__ bool dg_tile(const DgPassArgs& a, const DgFixed& f, D
                 pack_bf16(d[2 * c], d[2 * c + 1]);
         }
       };
-      // the planes written so far and the levels read so far are handed to
-      // thread 0, which issues groups [g0, g1) of the staged order
-      auto handoff = [&](const uint32_t id, const int g0, const int g1) {
-        fence_proxy_async();
-        tc_fence_before();
-        if (warp == 0) {
-          named_bar_sync(id, kDgThreads);
-          if (tid == 0 && !issue_lost) {
-            tc_fence_after();
-            if (g0 == 0) next_ok = dg_wait_image(f, a, p, k + 1);
-            if (next_ok) {
-#pragma unroll
-              for (int gi = g0; gi < g1; ++gi) dg_mma_group(f, sBn, dg_staged5(gi));
-            }
-          }
-        } else {
-          named_bar_arrive(id, kDgThreads);
-        }
-      };
 #pragma unroll
       for (int s = D; s >= 1; s -= 2) {
         float d0[kDgCols], d1[kDgCols];
         tmem_ld8x2(f.tlane + 64u * (uint32_t)s, f.tlane + 64u * (uint32_t)(s - 1), d0, d1);
         level(s, d0);
         level(s - 1, d1);
-        if constexpr (kStaged) {
-          if (s == 3) handoff(1, 0, 3);  // planes 4, 3 written; levels 5..2 read
-          if (s == 1) handoff(2, 3, 7);  // planes 2, 1 written; every level read
-        }
       }
       if ((D + 1) & 1) {
         float d0[kDgCols];
@@ -852,27 +798,16 @@ __device__ __forceinline__ bool dg_tile(const DgPassArgs& a, const DgFixed& f, D
       if (tid == 0) atomicExch(a.flag, 1);
       return false;
     }
-    // the next block's remaining MMAs: every group of a six-digit block,
-    // the last stage of a five-digit one
+    // the next block's MMAs, once every thread has written its A planes
     issue_lost = false;
     if (more && tid == 0) {
       tc_fence_after();
-      if (kStaged) {
-        if (next_ok) {
+      if (dg_wait_image(f, a, p, k + 1)) {
 #pragma unroll
-          for (int gi = 7; gi < 10; ++gi) dg_mma_group(f, sBn, dg_staged5(gi));
-          dg_commit(f, a, p, k + 1, bi + 1, obase, has_next);
-        } else {
-          issue_lost = true;
-        }
+        for (int gi = 0; gi < kDgGroupCount<D>; ++gi) dg_mma_group(f, sBn, dg_group<D>(gi));
+        dg_commit(f, a, p, k + 1, bi + 1, obase, has_next);
       } else {
-        if (dg_wait_image(f, a, p, k + 1)) {
-#pragma unroll
-          for (int gi = 0; gi < kDgGroupCount<D>; ++gi) dg_mma_group(f, sBn, dg_group<D>(gi));
-          dg_commit(f, a, p, k + 1, bi + 1, obase, has_next);
-        } else {
-          issue_lost = true;
-        }
+        issue_lost = true;
       }
     }
   }
