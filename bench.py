@@ -44,8 +44,10 @@ TILE_TRAFFIC_BYTES_PER_AMP = 32.08
 # complex128 digit block pass (k_tblock_dg): 2.102 GB / 2^26
 DIGIT_TRAFFIC_BYTES_PER_AMP = 31.33
 # Tensor work of one complex128 digit block on one 128-row tile (4096
-# amplitudes): 26 digit-pair products of 128 x 64 x 64, 2 flops each.
+# amplitudes): 26 digit-pair products of 128 x 64 x 64, 2 flops each, for a
+# six-digit tile; 20 for a five-digit tile.
 DIGIT_FLOPS_PER_AMP_BLOCK = 26 * 2 * 128 * 64 * 64 / 4096
+DIGIT_FLOPS_PER_AMP_BLOCK_FIVE = 20 * 2 * 128 * 64 * 64 / 4096
 N_QUBITS = 30
 LAYERS = 40
 SEED = 0
@@ -85,9 +87,11 @@ def measured_tensor_peak(sustained: bool) -> tuple[float, str]:
     return (1700.0 if sustained else 1900.0), "fallback bf16"
 
 
-def roofline_of(times: dict, plan: dict, n: int, S: float) -> dict:
+def roofline_of(times: dict, plan: dict, n: int, S: float, digit_tiles: tuple[int, int] = (0, 0)) -> dict:
     """Roofline of the pass class with the largest share of the timed region
-    (CUDA events around each pass on the state's stream)."""
+    (CUDA events around each pass on the state's stream).  digit_tiles: the
+    five- and six-digit tiles the timed digit passes ran (their digit
+    products per block differ)."""
     cls, (count, total_ms) = max(times.items(), key=lambda kv: kv[1][1])
     share = total_ms / sum(t for _, t in times.values())
     avg_ms = total_ms / count
@@ -96,12 +100,16 @@ def roofline_of(times: dict, plan: dict, n: int, S: float) -> dict:
     if cls == "block_digits":
         # the plan's block count over the timed passes (each step runs the plan once)
         blocks = plan["blocks"] * count / max(1, plan["block_passes"])
-        tflops = DIGIT_FLOPS_PER_AMP_BLOCK * (1 << n) * blocks / (total_ms * 1e-3) / 1e12
+        five, six = digit_tiles
+        per_amp_block = ((five * DIGIT_FLOPS_PER_AMP_BLOCK_FIVE + six * DIGIT_FLOPS_PER_AMP_BLOCK) / (five + six)
+                         if five + six else DIGIT_FLOPS_PER_AMP_BLOCK)
+        tflops = per_amp_block * (1 << n) * blocks / (total_ms * 1e-3) / 1e12
         peak, src = measured_tensor_peak(sustained=True)
         traffic = DIGIT_TRAFFIC_BYTES_PER_AMP * (1 << n)
         return {"bound": "tensor", "achieved": tflops, "peak": peak, "unit": "TFLOP/s", "frac": tflops / peak,
                 "traffic": traffic, "kernel": "bf::k_tblock_dg", "avg_launch_ms": avg_ms,
-                "flops_per_launch": DIGIT_FLOPS_PER_AMP_BLOCK * (1 << n) * blocks / count,
+                "flops_per_launch": per_amp_block * (1 << n) * blocks / count,
+                "digit_pairs_per_block": per_amp_block / (2 * 64 * 64 / 32),
                 "blocks_per_launch": blocks / count, "share_of_step": share, "launches": count,
                 "peak_source": f"{src} (bf16 tensor; digit products are bf16 x bf16 -> fp32)",
                 "hbm": {"achieved": hbm, "peak": hbm_peak, "unit": "GB/s", "frac": hbm / hbm_peak,
@@ -719,28 +727,35 @@ def run_ours(args) -> None:
                 times.append(time.perf_counter() - t0)
             return times
 
-        def host_arrays(pinned):
-            if pinned:
-                t_re = torch.zeros(N, dtype=torch.float64, pin_memory=True)
-                t_im = torch.zeros(N, dtype=torch.float64, pin_memory=True)
-                hre, him = t_re.numpy(), t_im.numpy()
-                keep = (t_re, t_im)
-            else:
-                hre, him = host_state(n)
-                keep = None
-            hre[0] = 1.0
-            return hre, him, keep
+        # Page-locked host arrays: the caller's own arrays, first touched by
+        # this process and then registered with CUDA (cudaHostRegister).
+        # Buffers from torch's pinned allocator copied at erratic rates on
+        # this host (medians of 171 ms up and 289 ms down for 16 GiB, against
+        # about 95 ms for registered arrays).
+        cudart = torch.cuda.cudart()
 
-        hre, him, keep = host_arrays(True)
+        def host_arrays(pinned):
+            hre, him = host_state(n)
+            if pinned:
+                for arr in (hre, him):
+                    rc = cudart.cudaHostRegister(arr.ctypes.data, arr.nbytes, 0)
+                    if int(rc) != 0:
+                        raise RuntimeError(f"cudaHostRegister failed: {rc}")
+            return hre, him
+
+        hre, him = host_arrays(True)
         e2e_run(st, hre, him, 1)  # warm-up
         times = e2e_run(st, hre, him, e2e_steps)
         dt = barrier_max(float(np.mean(times)), world)
         e2e = {"value": pg_bytes * world / dt / 1e9, "unit": "GB/s", "h2d_bytes_per_step": 2 * 8 * N,
                "d2h_bytes_per_step": 2 * 8 * N, "ms_per_step": dt * 1e3, "steps": e2e_steps,
-               "host_memory": "page-locked", "ms_min": min(times) * 1e3, "ms_max": max(times) * 1e3}
-        del hre, him, keep
+               "host_memory": "page-locked (registered with cudaHostRegister)", "ms_min": min(times) * 1e3,
+               "ms_max": max(times) * 1e3}
+        for arr in (hre, him):
+            cudart.cudaHostUnregister(arr.ctypes.data)
+        del hre, him
         if args.e2e_pageable_steps > 0:
-            hre, him, _ = host_arrays(False)
+            hre, him = host_arrays(False)
             ptimes = e2e_run(st, hre, him, args.e2e_pageable_steps)
             pdt = barrier_max(float(np.mean(ptimes)), world)
             e2e["pageable"] = {"value": pg_bytes * world / pdt / 1e9, "unit": "GB/s", "ms_per_step": pdt * 1e3,
@@ -789,7 +804,7 @@ def run_ours(args) -> None:
         "circuits_per_s": world / (ms_step * 1e-3),
         "per_gate_bytes_per_circuit": pg_bytes,
         "fused_plan": plan,
-        "roofline": roofline_of(pass_times, plan, n, S),
+        "roofline": roofline_of(pass_times, plan, n, S, (five_tiles, six_tiles)),
         "pass_times_ms": {k: {"passes": c, "ms": t} for k, (c, t) in pass_times.items()},
         "autotune": tune,
         "per_gate_path": per_gate,

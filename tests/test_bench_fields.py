@@ -84,3 +84,13 @@ def test_reference_arm_never_loads_the_engine(tmp_path):
     line = json.loads(lines[-2])
     assert line["impl"] == "reference" and line["config"]["qubits"] == 14
     assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_digit_roofline_counts_five_digit_tiles_at_20_pairs(bench):
+    n, S = 30, 16.0 * 2 ** 30
+    plan = {"tile_passes": 51, "block_passes": 50, "blocks": 124, "gate_kernels": 0}
+    times = {"block_digits": (150, 4500.0)}
+    r6 = bench.roofline_of(times, plan, n, S, (0, 100))
+    r5 = bench.roofline_of(times, plan, n, S, (100, 0))
+    assert r6["digit_pairs_per_block"] == pytest.approx(26) and r5["digit_pairs_per_block"] == pytest.approx(20)
+    assert r5["achieved"] == pytest.approx(r6["achieved"] * 20 / 26)
