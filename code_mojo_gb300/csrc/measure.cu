@@ -236,17 +236,31 @@ void measure(State& st, const int32_t* q, const int8_t* values, int32_t nq, int6
 }
 
 // ---- top-k ------------------------------------------------------------------
-// Each CTA keeps the running top kTopK of its grid-stride share in shared
-// memory: a chunk of 256 probabilities is added, and kTopK rounds of a
-// block-wide argmax pick the new top kTopK from the 256 + kTopK candidates.
-// Candidates are ordered by (probability desc, index asc).  The host merges
-// the per-CTA lists.
+// Each warp keeps a sorted list of its best candidates in registers: list
+// position j sits in lane j % 32, slot j / 32.  One ballot tests 32
+// probabilities against the warp's k-th best; the few lanes that beat it are
+// inserted one at a time with shuffles.  After the first few thousand
+// amplitudes almost no chunk holds one, so the pass streams the state at the
+// cost of the ballot.  An FP32 estimate of |amp|^2 from the leading bits of
+// each component skips the exact double-float square for amplitudes that
+// cannot reach the k-th best.  The CTA's warps merge their lists through
+// shared memory, and a one-CTA kernel merges the CTAs' lists, so the host
+// reads back the k winners only.  Candidates are ordered by (probability
+// desc, index asc).
 constexpr int kTopK = 64;
+constexpr int kTopUnroll = 4;            // loads in flight per thread
+constexpr int kTopMergeThreads = 1024;
+// The estimate is at least (1 - 2^-18) of the exact |amp|^2 and the k-th
+// best's hi part is within 2^-24 of its value, so an amplitude that beats
+// the k-th best has an estimate above its hi part times 1 - 2^-16.
+constexpr float kTopSlack = 1.0f - 1.0f / 65536.0f;
 
 struct Cand {
   float hi, lo;
   uint64_t idx;
 };
+
+__device__ __forceinline__ Cand cand_none() { return Cand{-1.f, 0.f, ~0ull}; }
 
 __device__ __forceinline__ bool cand_better(const Cand& a, const Cand& b) {
   if (a.hi != b.hi) return a.hi > b.hi;
@@ -254,96 +268,188 @@ __device__ __forceinline__ bool cand_better(const Cand& a, const Cand& b) {
   return a.idx < b.idx;
 }
 
+__device__ __forceinline__ Cand shfl_cand(const Cand& c, int src) {
+  return Cand{__shfl_sync(0xffffffffu, c.hi, src), __shfl_sync(0xffffffffu, c.lo, src),
+              __shfl_sync(0xffffffffu, c.idx, src)};
+}
+
+__device__ __forceinline__ Cand shfl_up_cand(const Cand& c) {
+  return Cand{__shfl_up_sync(0xffffffffu, c.hi, 1), __shfl_up_sync(0xffffffffu, c.lo, 1),
+              __shfl_up_sync(0xffffffffu, c.idx, 1)};
+}
+
+// |x| truncated to the 21 leading significant bits of the FP64 (its high
+// word), as FP32; 0 below the FP32 range, +inf above it (and for Inf/NaN) so
+// that the exact path decides those.
+__device__ __forceinline__ float lead_abs(double x) {
+  const unsigned hw = (unsigned)((unsigned long long)__double_as_longlong(x) >> 32);
+  const int ef = (int)((hw >> 20) & 0x7ffu) - 896;
+  if (ef <= 0) return 0.f;
+  if (ef >= 255) return __int_as_float(0x7f800000);
+  return __int_as_float((ef << 23) | (int)((hw & 0xfffffu) << 3));
+}
+
+// An FP32 estimate of |a|^2 that is at least (1 - 2^-18) of the exact value
+// (two 2^-20 truncations squared, two FP32 roundings).
 template <class T>
-__global__ void __launch_bounds__(kMeasThreads) k_topk(const T* __restrict__ s, uint64_t N, int k,
-                                                       Cand* __restrict__ out) {
-  __shared__ Cand pool[kMeasThreads + kTopK];
-  __shared__ Cand best[kTopK];
-  __shared__ int pick;
-  const int tid = threadIdx.x;
-  if (tid < kTopK) best[tid] = Cand{-1.f, 0.f, ~0ull};
-  __syncthreads();
-  const uint64_t stride = (uint64_t)gridDim.x * kMeasThreads;
-  for (uint64_t base = (uint64_t)blockIdx.x * kMeasThreads; base < N; base += stride) {
-    uint64_t i = base + tid;
-    Cand c{-1.f, 0.f, ~0ull};
-    if (i < N) {
-      dfl p = prob_df<T>(s[i]);
-      c = Cand{p.hi, p.lo, i};
+__device__ __forceinline__ float prob_estimate(T a);
+template <>
+__device__ __forceinline__ float prob_estimate<double2>(double2 a) {
+  const float r = lead_abs(a.x), i = lead_abs(a.y);
+  return fmaf(r, r, __fmul_rn(i, i));
+}
+template <>
+__device__ __forceinline__ float prob_estimate<float2>(float2 a) {
+  return fmaf(a.x, a.x, __fmul_rn(a.y, a.y));
+}
+
+// A warp's k best candidates, sorted, KB slots per lane (KB = 1 for k <= 32,
+// 2 for k <= 64).  Unused positions hold cand_none().
+template <int KB>
+struct WarpTop {
+  Cand s[KB];
+
+  __device__ __forceinline__ void init() {
+#pragma unroll
+    for (int b = 0; b < KB; ++b) s[b] = cand_none();
+  }
+  // position k - 1, in every lane
+  __device__ __forceinline__ Cand kth(int k) const {
+    if (KB == 2 && k > 32) return shfl_cand(s[KB - 1], k - 33);
+    return shfl_cand(s[0], k - 1);
+  }
+  // insert the warp-uniform x at its rank; the last position falls off
+  __device__ __forceinline__ void insert(const Cand& x, int lane) {
+    int pos = __popc(__ballot_sync(0xffffffffu, cand_better(s[0], x)));
+    if (KB == 2) pos += __popc(__ballot_sync(0xffffffffu, cand_better(s[KB - 1], x)));
+    const Cand up0 = shfl_up_cand(s[0]);
+    if (KB == 2) {
+      Cand up1 = shfl_up_cand(s[KB - 1]);
+      const Cand last0 = shfl_cand(s[0], 31);
+      if (lane == 0) up1 = last0;
+      const int j = lane + 32;
+      s[KB - 1] = j < pos ? s[KB - 1] : (j == pos ? x : up1);
     }
-    // skip the selection when no new probability beats the current k-th
-    if (!__syncthreads_or(cand_better(c, best[k - 1]) ? 1 : 0)) continue;
-    pool[tid] = c;
-    if (tid < k) pool[kMeasThreads + tid] = best[tid];
-    else if (tid < kTopK) pool[kMeasThreads + tid] = Cand{-1.f, 0.f, ~0ull};
-    __syncthreads();
-    // k rounds of argmax over the kMeasThreads + kTopK pool
-    for (int r = 0; r < k; ++r) {
-      int bi = tid;
-      Cand bc = pool[tid];
-      if (tid < kTopK && cand_better(pool[kMeasThreads + tid], bc)) {
-        bc = pool[kMeasThreads + tid];
-        bi = kMeasThreads + tid;
+    s[0] = lane < pos ? s[0] : (lane == pos ? x : up0);
+  }
+  // one candidate per lane (where `valid`); thr is the k-th best and follows
+  // the insertions
+  __device__ __forceinline__ void offer(const Cand& c, bool valid, Cand& thr, int k, int lane) {
+    unsigned m = __ballot_sync(0xffffffffu, valid && cand_better(c, thr));
+    while (m) {
+      const int src = __ffs(m) - 1;
+      m &= m - 1;
+      const Cand x = shfl_cand(c, src);
+      if (cand_better(x, thr)) {
+        insert(x, lane);
+        thr = kth(k);
       }
-      for (int off = 16; off > 0; off >>= 1) {
-        Cand oc;
-        oc.hi = __shfl_down_sync(0xffffffffu, bc.hi, off);
-        oc.lo = __shfl_down_sync(0xffffffffu, bc.lo, off);
-        oc.idx = __shfl_down_sync(0xffffffffu, bc.idx, off);
-        int ob = __shfl_down_sync(0xffffffffu, bi, off);
-        if (cand_better(oc, bc)) {
-          bc = oc;
-          bi = ob;
-        }
-      }
-      __shared__ Cand wc[kMeasThreads / 32];
-      __shared__ int wi[kMeasThreads / 32];
-      if ((tid & 31) == 0) {
-        wc[tid >> 5] = bc;
-        wi[tid >> 5] = bi;
-      }
-      __syncthreads();
-      if (tid == 0) {
-        Cand b = wc[0];
-        int bb = wi[0];
-        for (int w = 1; w < kMeasThreads / 32; ++w)
-          if (cand_better(wc[w], b)) {
-            b = wc[w];
-            bb = wi[w];
-          }
-        best[r] = b;
-        pick = bb;
-      }
-      __syncthreads();
-      if (tid == 0) pool[pick] = Cand{-2.f, 0.f, ~0ull};
-      __syncthreads();
     }
   }
-  if (tid < k) out[(size_t)blockIdx.x * k + tid] = best[tid];
+  __device__ __forceinline__ void store(Cand* dst, int k, int lane) const {
+#pragma unroll
+    for (int b = 0; b < KB; ++b)
+      if (lane + 32 * b < k) dst[lane + 32 * b] = s[b];
+  }
+};
+
+// The CTA's WARPS lists -> warp 0's list (valid in warp 0 only).
+template <int KB, int WARPS>
+__device__ __forceinline__ void merge_warps(WarpTop<KB>& top, Cand& thr, Cand (*lists)[kTopK], int k) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  top.store(lists[warp], k, lane);
+  __syncthreads();
+  if (warp != 0) return;
+  for (int w = 1; w < WARPS; ++w)
+    for (int j0 = 0; j0 < k; j0 += 32) {
+      const int j = j0 + lane;
+      top.offer(j < k ? lists[w][j] : cand_none(), j < k, thr, k, lane);
+    }
+}
+
+template <class T, int KB>
+__global__ void __launch_bounds__(kMeasThreads) k_topk(const T* __restrict__ s, uint64_t N, int k,
+                                                       Cand* __restrict__ out) {
+  constexpr int kWarps = kMeasThreads / 32;
+  __shared__ Cand lists[kWarps][kTopK];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  WarpTop<KB> top;
+  top.init();
+  Cand thr = cand_none();
+  const uint64_t chunk = 32ull * kTopUnroll;
+  const uint64_t step = (uint64_t)gridDim.x * kWarps * chunk;
+  for (uint64_t base = ((uint64_t)blockIdx.x * kWarps + warp) * chunk; base < N; base += step) {
+    T v[kTopUnroll];
+#pragma unroll
+    for (int u = 0; u < kTopUnroll; ++u) {
+      const uint64_t i = base + 32 * u + lane;
+      v[u] = i < N ? s[i] : T{};
+    }
+#pragma unroll
+    for (int u = 0; u < kTopUnroll; ++u) {
+      const uint64_t i = base + 32 * u + lane;
+      const bool valid = i < N && prob_estimate<T>(v[u]) >= thr.hi * kTopSlack;
+      Cand c{0.f, 0.f, i};
+      if (valid) {
+        const dfl p = prob_df<T>(v[u]);
+        c.hi = p.hi;
+        c.lo = p.lo;
+      }
+      top.offer(c, valid, thr, k, lane);
+    }
+  }
+  merge_warps<KB, kWarps>(top, thr, lists, k);
+  if (warp == 0) top.store(out + (size_t)blockIdx.x * k, k, lane);
+}
+
+// m candidates (the CTAs' lists) -> the k best, sorted.
+template <int KB>
+__global__ void __launch_bounds__(kTopMergeThreads) k_topk_merge(const Cand* __restrict__ in, int m, int k,
+                                                                 Cand* __restrict__ out) {
+  constexpr int kWarps = kTopMergeThreads / 32;
+  __shared__ Cand lists[kWarps][kTopK];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  WarpTop<KB> top;
+  top.init();
+  Cand thr = cand_none();
+  for (int j0 = warp * 32; j0 < m; j0 += kTopMergeThreads) {
+    const int j = j0 + lane;
+    top.offer(j < m ? in[j] : cand_none(), j < m, thr, k, lane);
+  }
+  merge_warps<KB, kWarps>(top, thr, lists, k);
+  if (warp == 0) top.store(out, k, lane);
+}
+
+template <class T, int KB>
+static void launch_topk(State& st, unsigned blocks, int k, Cand* part, Cand* fin) {
+  k_topk<T, KB><<<blocks, kMeasThreads, 0, st.stream>>>(static_cast<const T*>(st.amp), st.N, k, part);
+  BF_CUDA(cudaGetLastError());
+  k_topk_merge<KB><<<1, kTopMergeThreads, 0, st.stream>>>(part, (int)blocks * k, k, fin);
+  BF_CUDA(cudaGetLastError());
+  st.launches += 2;
 }
 
 void probs_topk(State& st, int k, uint64_t* idx, double* probs) {
   if (k < 1 || k > kTopK) fail(BF_EINVAL, "k must be in [1, %d]", kTopK);
   if ((uint64_t)k > st.N) fail(BF_EINVAL, "k exceeds the number of amplitudes");
-  unsigned blocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((st.N + kMeasThreads - 1) / kMeasThreads,
-                                                                        (uint64_t)st.num_sms * 2));
-  size_t need = (size_t)blocks * k * sizeof(Cand);
-  ensure_partials(st, (need + 2 * sizeof(double) - 1) / (2 * sizeof(double)));
-  Cand* d = reinterpret_cast<Cand*>(st.d_partial);
-  if (st.dtype == BF_C128)
-    k_topk<double2><<<blocks, kMeasThreads, 0, st.stream>>>(static_cast<const double2*>(st.amp), st.N, k, d);
-  else
-    k_topk<float2><<<blocks, kMeasThreads, 0, st.stream>>>(static_cast<const float2*>(st.amp), st.N, k, d);
-  BF_CUDA(cudaGetLastError());
-  st.launches++;
-  std::vector<Cand> h((size_t)blocks * k);
-  BF_CUDA(cudaMemcpyAsync(h.data(), d, need, cudaMemcpyDeviceToHost, st.stream));
+  static_assert(sizeof(Cand) == 2 * sizeof(double), "a candidate fills one partial-sum slot");
+  const uint64_t per_cta = (uint64_t)kMeasThreads * kTopUnroll;
+  const unsigned blocks = (unsigned)std::max<uint64_t>(
+      1, std::min<uint64_t>((st.N + per_cta - 1) / per_cta, (uint64_t)st.num_sms * 4));
+  ensure_partials(st, (size_t)blocks * k + k);
+  Cand* part = reinterpret_cast<Cand*>(st.d_partial);
+  Cand* fin = part + (size_t)blocks * k;
+  const bool wide = k > 32;
+  if (st.dtype == BF_C128) {
+    if (wide) launch_topk<double2, 2>(st, blocks, k, part, fin);
+    else launch_topk<double2, 1>(st, blocks, k, part, fin);
+  } else {
+    if (wide) launch_topk<float2, 2>(st, blocks, k, part, fin);
+    else launch_topk<float2, 1>(st, blocks, k, part, fin);
+  }
+  Cand* h = reinterpret_cast<Cand*>(st.h_partial);
+  BF_CUDA(cudaMemcpyAsync(h, fin, (size_t)k * sizeof(Cand), cudaMemcpyDeviceToHost, st.stream));
   sync_state(st);
-  std::sort(h.begin(), h.end(), [](const Cand& a, const Cand& b) {
-    double pa = (double)a.hi + (double)a.lo, pb = (double)b.hi + (double)b.lo;
-    if (pa != pb) return pa > pb;
-    return a.idx < b.idx;
-  });
   for (int i = 0; i < k; ++i) {
     idx[i] = h[i].idx;
     probs[i] = (double)h[i].hi + (double)h[i].lo;

@@ -483,6 +483,41 @@ def test_topk(n, k, dtype):
     assert np.max(np.abs(pr - ep) / ep) <= 1e-13  # double-float squares: ~2^-47 relative
 
 
+def _structured_state(kind, n):
+    N = 1 << n
+    i = np.arange(N, dtype=np.float64)
+    if kind == "uniform":  # every probability equal: the k lowest indices win
+        re, im = np.full(N, N ** -0.5), np.zeros(N)
+    elif kind == "ramp":  # probabilities rise with the index: every amplitude enters a list
+        re, im = np.sqrt(i + 1), np.zeros(N)
+    elif kind == "falling":
+        re, im = np.zeros(N), -np.sqrt(N - i)
+    elif kind == "sparse":  # 5 nonzero amplitudes: the rest of the top k are zeros by index
+        re, im = np.zeros(N), np.zeros(N)
+        for j, t in enumerate((N - 1, 7, N // 2 + 3, 1, N // 3)):
+            re[t], im[t] = 0.1 * (j + 1), -0.05 * j
+    else:  # two equal peaks in different CTAs' shares, the rest small
+        re, im = np.full(N, 1e-4), np.full(N, -1e-4)
+        re[N - 2] = re[3] = 0.5
+    s = math.sqrt(float(np.sum(re * re + im * im)))
+    return re / s, im / s
+
+
+@pytest.mark.parametrize("kind", ["uniform", "ramp", "falling", "sparse", "peaks"])
+@pytest.mark.parametrize("n,k", [(11, 64), (16, 16), (21, 33), (13, 1)])
+@pytest.mark.parametrize("dtype", ["c128", "c64"])
+def test_topk_structured(kind, n, k, dtype):
+    re, im = _structured_state(kind, n)
+    st = bfy.QuantumState.from_soa(re, im, dtype)
+    idx, pr = st.topk(k)
+    st.close()
+    if dtype == "c64":
+        re, im = re.astype(np.float32).astype(np.float64), im.astype(np.float32).astype(np.float64)
+    ei, ep = O.topk(re, im, k)
+    assert idx.tolist() == ei.tolist()
+    np.testing.assert_allclose(pr, ep, rtol=1e-13, atol=0)
+
+
 # ---- classical Grover passes ----------------------------------------------------
 @pytest.mark.parametrize("targets", [[], [0, 3, 5], [2, 4, 6, 8, 9, 10, 11, 12, 13], list(range(1, 15)), [14]])
 @pytest.mark.parametrize("dtype", ["c128", "c64"])
