@@ -120,16 +120,23 @@ void upload_program_reserve(State& st, size_t ops) {
   st.prog_event_live = false;
 }
 
-// Everything a plan uploads: tile ops, and for tensor-core passes the block
-// descriptors followed (at a 256-byte boundary) by their matrix images.
+// Everything a plan uploads: tile ops, and in the auxiliary buffer the
+// tensor-core passes' block descriptors, (at a 256-byte boundary) their
+// matrix images and destination tables, then (at a 16-byte boundary) the
+// unitary pool that the tile ops of dense unitaries index.
 struct Program {
   std::vector<TileOp> ops;
   std::vector<Blk5> blocks;
   std::vector<unsigned char> images;
   std::vector<uint16_t> offsets;
+  std::vector<double> umats;
   size_t images_offset() const { return (blocks.size() * sizeof(Blk5) + 255) & ~(size_t)255; }
   size_t offsets_offset() const { return images_offset() + images.size(); }
-  size_t aux_bytes() const { return blocks.empty() ? 0 : offsets_offset() + offsets.size() * sizeof(uint16_t); }
+  size_t umats_offset() const { return (offsets_offset() + offsets.size() * sizeof(uint16_t) + 15) & ~(size_t)15; }
+  size_t aux_bytes() const {
+    if (blocks.empty() && umats.empty()) return 0;
+    return umats_offset() + umats.size() * sizeof(double);
+  }
 };
 
 // id: the plan's cache id (0: not cached); a program already on the device
@@ -161,6 +168,7 @@ static void upload_program(State& st, const Program& pg, uint64_t id) {
     std::memcpy(st.h_aux, pg.blocks.data(), pg.blocks.size() * sizeof(Blk5));
     std::memcpy(st.h_aux + pg.images_offset(), pg.images.data(), pg.images.size());
     std::memcpy(st.h_aux + pg.offsets_offset(), pg.offsets.data(), pg.offsets.size() * sizeof(uint16_t));
+    std::memcpy(st.h_aux + pg.umats_offset(), pg.umats.data(), pg.umats.size() * sizeof(double));
     BF_CUDA(cudaMemcpyAsync(st.d_aux, st.h_aux, aux, cudaMemcpyHostToDevice, st.stream));
   }
   BF_CUDA(cudaEventRecord(st.prog_event, st.stream));
@@ -335,6 +343,7 @@ static double cuda_core_units(const TilePass& tp) {
       case GK_SWAP: u += 0.5; break;
       case GK_PHASE: u += 0.4; break;
       case GK_DIAG: u += 0.6; break;
+      case GK_UNITARY: u += (double)(1 << (t.um - 1)); break;  // 2^m products per amplitude
       default: u += 1.0; break;
     }
   }
@@ -410,7 +419,8 @@ static void build_steps(int n, const bf_op* ops, int64_t nops, const bf_exec_opt
         const double cu = cuda_core_units(ps.tile);
         int max_blocks = 0;
         while (max_blocks < kMaxPassBlocks && (double)(max_blocks + 1) * block_units < cu) ++max_blocks;
-        if (max_blocks > 0 && plan_blocks(ps.tile, pg.blocks, pg.images, pg.offsets, format, max_blocks) &&
+        if (max_blocks > 0 &&
+            plan_blocks(ps.tile, pg.blocks, pg.images, pg.offsets, format, max_blocks, pg.umats.data()) &&
             (double)(pg.blocks.size() - b0) * block_units < cu) {
           s.kind = Step::TBLOCK;
           s.digits = format == BLOCK_DIGITS;
@@ -432,6 +442,15 @@ static void build_steps(int n, const bf_op* ops, int64_t nops, const bf_exec_opt
         s.nprog = (int)ps.tile.ops.size();
         prog.insert(prog.end(), ps.tile.ops.begin(), ps.tile.ops.end());
         s.tile.ops.clear();
+      } else if (ps.gate.kind == GK_UNITARY) {
+        // a unitary the planner left on its own: its dense kernel
+        const GateInstr& g = ps.gate;
+        s.kind = Step::UNITARY;
+        const double* u = pg.umats.data() + g.uoff;
+        s.u.assign(u, u + 2 * ((size_t)1 << (2 * g.um)));
+        s.ut = g.target;
+        s.um = g.um;
+        s.uc = g.cmask ? __builtin_ctzll(g.cmask) : -1;
       } else {
         s.kind = Step::GATE;
         s.gate = ps.gate;
@@ -459,8 +478,25 @@ static void build_steps(int n, const bf_op* ops, int64_t nops, const bf_exec_opt
     s.src_of = src_of;
     steps.push_back(std::move(s));
   };
+  // a fused run's tile keeps its low min(K - 1, 5) qubits (all of them when
+  // it spans the state); an m-qubit unitary joins only when it fits beside them
+  const int run_low = K >= n ? std::min(K, kTileLowQubits) : std::min(K - 1, kTileLowQubits);
   auto emit_unitary = [&](const double* data, int t, int m, int ctl) {
     if (m <= 0) return;
+    if (fused && m >= 2 && m <= kTileUnitaryMax && (K >= n || K - run_low >= m)) {
+      // a dense unitary of a fused run: applied inside the tile pass (or
+      // multiplied into a tensor-core block) with the gates around it
+      GateInstr g;
+      std::memset(&g, 0, sizeof g);
+      g.kind = GK_UNITARY;
+      g.target = t;
+      g.cmask = ctl >= 0 ? 1ull << ctl : 0ull;
+      g.um = m;
+      g.uoff = (int32_t)pg.umats.size();
+      pg.umats.insert(pg.umats.end(), data, data + 2 * ((size_t)1 << (2 * m)));
+      run.push_back(g);
+      return;
+    }
     if (m == 1) {  // a 2x2: the gate kernels (and tile passes) take it
       bf_op g;
       std::memset(&g, 0, sizeof g);
@@ -673,7 +709,10 @@ static void run_steps(State& st, const std::vector<Step>& steps, const Program& 
     if (st.pass_timing) BF_CUDA(cudaEventRecord(pass_event(st, ev), st.stream));
     switch (s.kind) {
       case Step::GATE: launch_gate(st, s.gate); break;
-      case Step::TILE: launch_tile_pass(st, st.d_prog + s.prog_off, s.nprog, s.tile); break;
+      case Step::TILE:
+        launch_tile_pass(st, st.d_prog + s.prog_off, s.nprog, s.tile,
+                         pg.umats.empty() ? nullptr : reinterpret_cast<const double*>(st.d_aux + pg.umats_offset()));
+        break;
       case Step::TBLOCK:
         if (s.digits) {
           launch_block_pass_digits(st, reinterpret_cast<const Blk5*>(st.d_aux) + s.blk_off, s.nblk,

@@ -94,18 +94,35 @@ enum GKind : int32_t {
   GK_PHASE = 3,  // diag(1, e^{i theta}): m[6], m[7] = cos, sin (P, Z, CP, CZ, MCP)
   GK_DIAG = 4,   // diag(d0, d1): m[0..1] = d0, m[6..7] = d1 (RZ)
   GK_RY = 5,     // real rotation [[c,-s],[s,c]]: m[0] = c, m[4] = s
-  GK_DENSE_R = 6 // full 2x2 matrix whose m00 is real (m[1] == 0), as in every U3
+  GK_DENSE_R = 6, // full 2x2 matrix whose m00 is real (m[1] == 0), as in every U3
+  GK_UNITARY = 7  // dense 2^um x 2^um matrix on qubits target .. target + um - 1
 };
+
+// Dense unitaries of up to this many qubits join fused runs (tile passes
+// and tensor-core blocks); wider ones run as their own pass.
+constexpr int kTileUnitaryMax = 3;
 
 struct GateInstr {
   int32_t kind;     // GKind
-  int32_t target;
+  int32_t target;   // GK_UNITARY: the lowest of its qubits
   uint64_t cmask;   // control qubits (all must be 1)
   double m[8];      // re00 im00 re01 im01 re10 im10 re11 im11
   float mhl[16];    // the same eight values as (hi, lo) FP32 pairs
+  int32_t um;       // GK_UNITARY: qubit count (2..kTileUnitaryMax); 0 otherwise
+  int32_t uoff;     // GK_UNITARY: offset (in doubles) of its row-major
+                    // interleaved matrix in the run's unitary pool
 };
 
 inline bool gk_is_diagonal(int k) { return k == GK_PHASE || k == GK_DIAG; }
+// qubits a gate acts on non-diagonally, and all the qubits it touches
+inline uint64_t gate_xmask(const GateInstr& g) {
+  if (g.kind == GK_UNITARY) return ((1ull << g.um) - 1ull) << g.target;
+  return gk_is_diagonal(g.kind) ? 0ull : 1ull << g.target;
+}
+inline uint64_t gate_amask(const GateInstr& g) {
+  const uint64_t t = g.kind == GK_UNITARY ? ((1ull << g.um) - 1ull) << g.target : 1ull << g.target;
+  return g.cmask | t;
+}
 
 // Per-gate algorithmic bytes of one pass (read + write of every amplitude the
 // gate must touch), in units of the state's byte size S.
@@ -120,12 +137,17 @@ constexpr int kTileLowQubits = 5;
 struct TileOp {
   int32_t kind;       // GKind
   int32_t tloc;       // local bit of the target, or -1 (diagonal gate whose
-                      // target lies outside the tile)
+                      // target lies outside the tile); GK_UNITARY: local bit
+                      // of its lowest qubit (its qubits are consecutive
+                      // tile qubits, so they sit at tloc .. tloc + um - 1)
   int32_t tglob;      // global target qubit
   uint32_t cmask_loc; // control bits inside the tile (local positions)
   uint64_t cmask_out; // control bits outside the tile (global positions)
   double m[8];
   float mhl[16];
+  int32_t um;         // GK_UNITARY: qubit count; 0 otherwise
+  int32_t uoff;       // GK_UNITARY: offset (in doubles) of its matrix in the
+                      // program's unitary pool
 };
 
 struct TilePass {
@@ -177,8 +199,11 @@ constexpr uint32_t kDigitImageBytes = kDigits * 8192;
 // tile qubits or more than 3 outside qubits on its own), the pass needs more
 // than min(kMaxPassBlocks, max_blocks) blocks (checked before any matrix is
 // built), or (BLOCK_DIGITS) a block's matrix is not unitary to 1e-12.
+// `umats` is the unitary pool that GK_UNITARY ops index (may be null when
+// the pass has none).
 bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsigned char>& images,
-                 std::vector<uint16_t>& offsets, BlockFormat format = BLOCK_TF32, int max_blocks = kMaxPassBlocks);
+                 std::vector<uint16_t>& offsets, BlockFormat format = BLOCK_TF32, int max_blocks = kMaxPassBlocks,
+                 const double* umats = nullptr);
 #ifdef __CUDACC__
 #define BF_HOST_DEVICE __host__ __device__
 #else
@@ -293,7 +318,8 @@ void sync_state(State& st);
 // ---------------------------------------------------------------------------
 // Kernel launchers (device code lives in the .cu files).
 void launch_gate(State& s, const GateInstr& g);
-void launch_tile_pass(State& s, const TileOp* d_ops, int nops, const TilePass& p);
+// d_umats: the device copy of the program's unitary pool (null without GK_UNITARY ops)
+void launch_tile_pass(State& s, const TileOp* d_ops, int nops, const TilePass& p, const double* d_umats = nullptr);
 void launch_block_pass(State& st, const Blk5* d_blocks, int nblocks, const unsigned char* d_images,
                        const uint16_t* d_offsets, const TilePass& p);
 // complex128 digit blocks (BLOCK_DIGITS); d_exp holds the scale exponent

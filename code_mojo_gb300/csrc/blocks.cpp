@@ -109,7 +109,10 @@ struct BlockBuild {
   std::vector<const TileOp*> ops;
 };
 
-uint32_t local_set(const TileOp& t) { return t.cmask_loc | (t.tloc >= 0 ? (1u << t.tloc) : 0u); }
+uint32_t local_set(const TileOp& t) {
+  if (t.kind == GK_UNITARY) return t.cmask_loc | (((1u << t.um) - 1u) << t.tloc);
+  return t.cmask_loc | (t.tloc >= 0 ? (1u << t.tloc) : 0u);
+}
 uint64_t outside_set(const TileOp& t) { return t.cmask_out | (t.tloc < 0 ? (1ull << t.tglob) : 0ull); }
 
 }  // namespace
@@ -217,7 +220,7 @@ std::vector<BlockMap> conflict_free_maps(const std::vector<uint32_t>& qsets, int
 }  // namespace
 
 bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsigned char>& images,
-                 std::vector<uint16_t>& offsets, BlockFormat format, int max_blocks) {
+                 std::vector<uint16_t>& offsets, BlockFormat format, int max_blocks, const double* umats) {
   const uint32_t image_bytes = format == BLOCK_DIGITS ? kDigitImageBytes : kBlockImageBytes;
   // destination of complex element (g, j) of a block's operands, in the
   // units of the kernel's table (TF32: bytes / 8; digits: bytes / 4 in a plane)
@@ -295,6 +298,39 @@ bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsi
         uint32_t cb = 0;
         for (int pos = 0; pos < kBlockTileQubits; ++pos)
           if ((t->cmask_loc >> pos) & 1u) cb |= 1u << rank_of[pos];
+        if (t->kind == GK_UNITARY) {
+          // dense 2^um x 2^um on local bits tloc .. tloc+um-1 (unitary bit i
+          // at block rank rank_of[tloc + i]): every column of U, every group
+          // of rows that share the other bits and meet the controls
+          if (!umats) return false;
+          const int D = 1 << t->um;
+          const double* um = umats + t->uoff;
+          int rk[kTileUnitaryMax];
+          uint32_t umask = 0;
+          for (int i = 0; i < t->um; ++i) {
+            rk[i] = rank_of[t->tloc + i];
+            umask |= 1u << rk[i];
+          }
+          cd x[1 << kTileUnitaryMax];
+          for (int r0 = 0; r0 < 32; ++r0) {
+            if ((r0 & umask) || (r0 & cb) != cb) continue;
+            auto row = [&](int a) {
+              int r = r0;
+              for (int i = 0; i < t->um; ++i)
+                if ((a >> i) & 1) r |= 1 << rk[i];
+              return r;
+            };
+            for (int c = 0; c < 32; ++c) {
+              for (int a = 0; a < D; ++a) x[a] = U[row(a) * 32 + c];
+              for (int a = 0; a < D; ++a) {
+                cd acc(0.0, 0.0);
+                for (int b = 0; b < D; ++b) acc += cd(um[2 * (a * D + b)], um[2 * (a * D + b) + 1]) * x[b];
+                U[row(a) * 32 + c] = acc;
+              }
+            }
+          }
+          continue;
+        }
         const double* m = t->m;
         if (t->tloc < 0) {  // diagonal gate on an outside target: one entry for the variant
           const cd e = out_bit(t->tglob) ? cd(m[6], m[7]) : cd(m[0], m[1]);

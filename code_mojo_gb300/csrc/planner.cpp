@@ -222,6 +222,8 @@ static TileOp to_tile_op(const GateInstr& g, const int* loc_of) {
   t.kind = g.kind;
   t.tglob = g.target;
   t.tloc = loc_of[g.target];
+  t.um = g.um;
+  t.uoff = g.uoff;
   for (int b = 0; b < 64; ++b) {
     if (!((g.cmask >> b) & 1)) continue;
     if (loc_of[b] >= 0) t.cmask_loc |= 1u << loc_of[b];
@@ -239,9 +241,8 @@ static double pass_work(const std::vector<const GateInstr*>& remaining, uint64_t
   uint64_t blockedX = 0, blockedAll = 0;
   double w = 0;
   for (const GateInstr* g : remaining) {
-    const uint64_t tb = 1ull << g->target;
-    const uint64_t Xg = gk_is_diagonal(g->kind) ? 0 : tb;
-    const uint64_t Ag = g->cmask | tb;
+    const uint64_t Xg = gate_xmask(*g);
+    const uint64_t Ag = gate_amask(*g);
     if (!(Xg & blockedAll) && !(Ag & blockedX) && !(Xg & ~inQ)) {
       w += gate_bytes_fraction(*g);
     } else {
@@ -262,9 +263,8 @@ static int pass_blocks(const std::vector<const GateInstr*>& remaining, uint64_t 
   uint64_t bq[64], bo[64];
   int nb = 0;
   for (const GateInstr* g : remaining) {
-    const uint64_t tb = 1ull << g->target;
-    const uint64_t Xg = gk_is_diagonal(g->kind) ? 0 : tb;
-    const uint64_t Ag = g->cmask | tb;
+    const uint64_t Xg = gate_xmask(*g);
+    const uint64_t Ag = gate_amask(*g);
     if ((Xg & blockedAll) || (Ag & blockedX) || (Xg & ~inQ)) {
       blockedX |= Xg;
       blockedAll |= Ag;
@@ -296,21 +296,23 @@ static int pass_blocks(const std::vector<const GateInstr*>& remaining, uint64_t 
 
 // The CUDA-core tile kernel's cost of the gates a pass over inQ takes, in
 // dense-gate units (dense 1, exchange 0.5, phase 0.4, other diagonal 0.6, a
-// diagonal gate on an outside target 0.4).
+// diagonal gate on an outside target 0.4, an m-qubit unitary 2^(m-1): its
+// 2^m complex products per amplitude against a dense gate's 2).
 static double pass_core_units(const std::vector<const GateInstr*>& remaining, uint64_t inQ, uint64_t all) {
   uint64_t blockedX = 0, blockedAll = 0;
   double u = 0;
   for (const GateInstr* g : remaining) {
     const uint64_t tb = 1ull << g->target;
-    const uint64_t Xg = gk_is_diagonal(g->kind) ? 0 : tb;
-    const uint64_t Ag = g->cmask | tb;
+    const uint64_t Xg = gate_xmask(*g);
+    const uint64_t Ag = gate_amask(*g);
     if ((Xg & blockedAll) || (Ag & blockedX) || (Xg & ~inQ)) {
       blockedX |= Xg;
       blockedAll |= Ag;
       if ((blockedX & all) == all) break;
       continue;
     }
-    if (!(tb & inQ)) u += 0.4;
+    if (g->kind == GK_UNITARY) u += (double)(1 << (g->um - 1));
+    else if (!(tb & inQ)) u += 0.4;
     else if (g->kind == GK_SWAP) u += 0.5;
     else if (g->kind == GK_PHASE) u += 0.4;
     else if (g->kind == GK_DIAG) u += 0.6;
@@ -341,20 +343,20 @@ std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int
     // the qubits the remaining gates touch: once the deferred gates act
     // non-diagonally on all of them, no later gate can join a pass
     uint64_t all = 0;
-    for (const GateInstr* g : remaining) all |= g->cmask | (1ull << g->target);
+    for (const GateInstr* g : remaining) all |= gate_amask(*g);
     {
       uint64_t blockedX = 0, blockedAll = 0;
       for (const GateInstr* g : remaining) {
-        const uint64_t tb = 1ull << g->target;
-        const uint64_t Xg = gk_is_diagonal(g->kind) ? 0 : tb;
-        const uint64_t Ag = g->cmask | tb;
+        const uint64_t Xg = gate_xmask(*g);
+        const uint64_t Ag = gate_amask(*g);
         bool fits = false;
         if (!(Xg & blockedAll) && !(Ag & blockedX)) {
-          if ((Xg & ~inQ) == 0) {
+          const int extra = __builtin_popcountll(Xg & ~inQ);
+          if (extra == 0) {
             fits = true;
-          } else if (nQ + 1 <= K) {
+          } else if (nQ + extra <= K) {
             inQ |= Xg;
-            nQ += 1;
+            nQ += extra;
             fits = true;
           }
         }
@@ -367,8 +369,7 @@ std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int
     }
     if (nQ == K && K < n) {
       uint64_t targets = 0;
-      for (const GateInstr* g : remaining)
-        if (!gk_is_diagonal(g->kind)) targets |= 1ull << g->target;
+      for (const GateInstr* g : remaining) targets |= gate_xmask(*g);
       auto search = [&](uint64_t start, auto score) {
         uint64_t set = start;
         double best = score(set);
@@ -419,9 +420,8 @@ std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int
       size_t i = 0;
       for (; i < remaining.size(); ++i) {
         const GateInstr* g = remaining[i];
-        const uint64_t tb = 1ull << g->target;
-        const uint64_t Xg = gk_is_diagonal(g->kind) ? 0 : tb;
-        const uint64_t Ag = g->cmask | tb;
+        const uint64_t Xg = gate_xmask(*g);
+        const uint64_t Ag = gate_amask(*g);
         if (!(Xg & blockedAll) && !(Ag & blockedX) && !(Xg & ~inQ)) {
           taken.push_back(g);
         } else {

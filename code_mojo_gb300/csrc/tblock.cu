@@ -479,6 +479,25 @@ __device__ __forceinline__ float rint_div256(float t) {
   return __fsub_rn(__fmaf_rn(t, 0.00390625f, 12582912.0f), 12582912.0f);
 }
 
+// The carry step of two values at once in packed FP32 pairs (f32x2, one
+// instruction for both lanes, each lane rounded exactly as its scalar
+// form): t = d + c, q = rint(t / 256) as in rint_div256, d = t - 256 q,
+// c = q.
+__device__ __forceinline__ void carry_pair(float& d0, float& d1, float& c0, float& c1) {
+  const unsigned long long inv256 = 0x3B8000003B800000ull;  // (2^-8, 2^-8)
+  const unsigned long long magic = 0x4B4000004B400000ull;   // (1.5 * 2^23, 1.5 * 2^23)
+  const unsigned long long m256 = 0xC3800000C3800000ull;    // (-256, -256)
+  unsigned long long d, c, t, u, q;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(d0), "f"(d1));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(c) : "f"(c0), "f"(c1));
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(t) : "l"(d), "l"(c));
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(u) : "l"(t), "l"(inv256), "l"(magic));
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(q) : "l"(u), "l"(magic));
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(q), "l"(m256), "l"(t));
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(d0), "=f"(d1) : "l"(d));
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(c0), "=f"(c1) : "l"(q));
+}
+
 // two 8-column TMEM loads in flight, one wait; the wait names the registers
 // so that no use of them is scheduled before it
 __device__ __forceinline__ void tmem_ld8x2(uint32_t ta, uint32_t tb, float* va, float* vb) {
@@ -711,12 +730,7 @@ __device__ __forceinline__ bool dg_tile(const DgPassArgs& a, const DgFixed& f, D
     for (int c = 0; c < kDgCols; ++c) carry[c] = 0.f;
     auto carry_step = [&](float* d) {
 #pragma unroll
-      for (int c = 0; c < kDgCols; ++c) {
-        const float t = __fadd_rn(d[c], carry[c]);
-        const float q = rint_div256(t);
-        d[c] = __fmaf_rn(q, -256.0f, t);
-        carry[c] = q;
-      }
+      for (int c = 0; c < kDgCols; c += 2) carry_pair(d[c], d[c + 1], carry[c], carry[c + 1]);
     };
     if (more) {
       // positions 1 .. D-1 and 0 become the next block's A planes

@@ -24,14 +24,14 @@ namespace bf {
 template <class P>
 __global__ void __launch_bounds__(kTileThreads) k_tile(typename P::Glob* __restrict__ s,
                                                        const TileOp* __restrict__ ops, int nops,
-                                                       const TileGeom geo) {
+                                                       const TileGeom geo, const double* __restrict__ umats) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  run_tile<P>(s, ops, nops, geo, blockIdx.x, smem_raw);
+  run_tile<P>(s, ops, nops, geo, blockIdx.x, smem_raw, umats);
 }
 
 
 template <class P>
-static void launch_tile_p(State& st, const TileOp* d_ops, int nops, const TilePass& p) {
+static void launch_tile_p(State& st, const TileOp* d_ops, int nops, const TilePass& p, const double* d_umats) {
   TileGeom geo;
   geo.K = p.K;
   geo.L = p.L;
@@ -39,25 +39,25 @@ static void launch_tile_p(State& st, const TileOp* d_ops, int nops, const TilePa
   for (int j = 0; j < p.K; ++j) geo.q[j] = p.q[j];
   for (int j = 0; j < geo.L; ++j)
     if (geo.q[j] != j) fail(BF_EINVAL, "internal: tile qubits must start with 0..%d", geo.L - 1);
-  size_t smem = tile_smem_bytes<P>(p.K, geo.L);
+  size_t smem = tile_smem_bytes<P>(p.K, geo.L, d_umats != nullptr);
   static PerDeviceOnce configured;  // one per instantiation of P
   configured.run(st.device, [] {
     BF_CUDA(cudaFuncSetAttribute(k_tile<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)tile_smem_bytes<P>(kMaxTileQubits, 0)));
+                                 (int)tile_smem_bytes<P>(kMaxTileQubits, 0, true)));
   });
   uint64_t blocks = st.N >> p.K;
   if (blocks > 0x7fffffffull) fail(BF_EUNSUPPORTED, "tile grid too large");
   k_tile<P><<<(unsigned)blocks, kTileThreads, smem, st.stream>>>(static_cast<typename P::Glob*>(st.amp), d_ops,
-                                                                 nops, geo);
+                                                                 nops, geo, d_umats);
   BF_CUDA(cudaGetLastError());
   st.launches++;
 }
 
-void launch_tile_pass(State& st, const TileOp* d_ops, int nops, const TilePass& p) {
+void launch_tile_pass(State& st, const TileOp* d_ops, int nops, const TilePass& p, const double* d_umats) {
   switch (st.prec) {
-    case PREC_F64: launch_tile_p<PolF64>(st, d_ops, nops, p); break;
-    case PREC_DF: launch_tile_p<PolDF>(st, d_ops, nops, p); break;
-    default: launch_tile_p<PolF32>(st, d_ops, nops, p); break;
+    case PREC_F64: launch_tile_p<PolF64>(st, d_ops, nops, p, d_umats); break;
+    case PREC_DF: launch_tile_p<PolDF>(st, d_ops, nops, p, d_umats); break;
+    default: launch_tile_p<PolF32>(st, d_ops, nops, p, d_umats); break;
   }
 }
 

@@ -60,6 +60,39 @@ __device__ __forceinline__ void tile_gate(int kind, typename P::Smem* amp, int T
   }
 }
 
+// One in-tile dense unitary on the consecutive local bits tloc .. tloc+UM-1:
+// each thread takes whole groups of 2^UM amplitudes (the other bits fixed),
+// reads them, forms U x (rows of the row-major matrix `um` in shared memory)
+// and writes it back in place.
+template <class P, int UM, bool kCtl>
+__device__ __forceinline__ void tile_unitary(typename P::Smem* amp, int TS, int tloc, uint32_t cml,
+                                             const typename P::Smem* um) {
+  using R = typename P::R;
+  constexpr int D = 1 << UM;
+  const uint32_t low = (1u << tloc) - 1u;
+  for (int g = threadIdx.x; g < (TS >> UM); g += kTileThreads) {
+    const uint32_t base = (((uint32_t)g & ~low) << UM) | ((uint32_t)g & low);
+    if (kCtl && (base & cml) != cml) continue;
+    R x[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) x[c] = P::from_smem(amp[base | ((uint32_t)c << tloc)]);
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+      R acc = P::zero();
+#pragma unroll
+      for (int c = 0; c < D; ++c) acc = P::fma(P::from_smem(um[r * D + c]), x[c], acc);
+      amp[base | ((uint32_t)r << tloc)] = P::to_smem(acc);
+    }
+  }
+}
+
+// bytes of shared memory before the staged unitary matrix (16-byte aligned)
+template <class P>
+__host__ __device__ inline size_t tile_umat_offset(int K, int L) {
+  return ((((size_t)1 << K) * sizeof(typename P::Smem) + ((size_t)1 << (K - L)) * sizeof(uint64_t)) + 15) &
+         ~(size_t)15;
+}
+
 // One tile: load the 2^K amplitudes of tile `tile` (the non-tile qubits set
 // to the bits of `tile`), apply ops[0..nops) in shared memory, store.  Called
 // by every thread of a CTA of kTileThreads threads; `smem_raw` holds
@@ -67,9 +100,13 @@ __device__ __forceinline__ void tile_gate(int kind, typename P::Smem* amp, int T
 // kL2Loads: read the state with L2-only loads (__ldcg).  Needed when other
 // CTAs of the same launch wrote these amplitudes earlier (L1 is not coherent
 // across SMs); a separate launch per pass does not need it.
+// umats: the unitary pool of GK_UNITARY ops (row-major interleaved FP64);
+// with one, `smem_raw` also holds the staged matrix
+// (tile_smem_bytes(K, L, true)).
 template <class P, bool kL2Loads = false>
 __device__ __forceinline__ void run_tile(typename P::Glob* __restrict__ s, const TileOp* __restrict__ ops, int nops,
-                                         const TileGeom& geo, uint64_t tile, unsigned char* smem_raw) {
+                                         const TileGeom& geo, uint64_t tile, unsigned char* smem_raw,
+                                         const double* __restrict__ umats = nullptr) {
   using R = typename P::R;
   using S = typename P::Smem;
   const int K = geo.K, L = geo.L;
@@ -106,6 +143,28 @@ __device__ __forceinline__ void run_tile(typename P::Glob* __restrict__ s, const
     const int kind = __ldg(&op->kind);
     const int tloc = __ldg(&op->tloc);
     const uint32_t cml = __ldg(&op->cmask_loc);
+    if (kind == GK_UNITARY) {
+      // stage the matrix, then every group of the tile
+      const int um = __ldg(&op->um);
+      const double* u = umats + __ldg(&op->uoff);
+      S* mat = reinterpret_cast<S*>(smem_raw + tile_umat_offset<P>(K, L));
+      for (int e = tid; e < (1 << (2 * um)); e += kTileThreads) {
+        typename P::Glob gv;
+        if constexpr (sizeof(typename P::Glob) == 16) gv = make_double2(__ldg(u + 2 * e), __ldg(u + 2 * e + 1));
+        else gv = make_float2((float)__ldg(u + 2 * e), (float)__ldg(u + 2 * e + 1));
+        mat[e] = P::to_smem(P::from_glob(gv));
+      }
+      __syncthreads();
+      if (um == 2) {
+        if (cml) tile_unitary<P, 2, true>(amp, TS, tloc, cml, mat);
+        else tile_unitary<P, 2, false>(amp, TS, tloc, 0u, mat);
+      } else {
+        if (cml) tile_unitary<P, 3, true>(amp, TS, tloc, cml, mat);
+        else tile_unitary<P, 3, false>(amp, TS, tloc, 0u, mat);
+      }
+      __syncthreads();
+      continue;
+    }
     const typename P::Coef g = P::coef(op->m, op->mhl);
     if (tloc >= 0) {
       if (cml) tile_gate<P, true>(kind, amp, TS, tloc, cml, g);
@@ -132,8 +191,12 @@ __device__ __forceinline__ void run_tile(typename P::Glob* __restrict__ s, const
   }
 }
 
+// shared memory of run_tile; with_unitary: room for a staged
+// 2^kTileUnitaryMax-square matrix
 template <class P>
-inline size_t tile_smem_bytes(int K, int L) {
+inline size_t tile_smem_bytes(int K, int L, bool with_unitary = false) {
+  if (with_unitary)
+    return tile_umat_offset<P>(K, L) + ((size_t)1 << (2 * kTileUnitaryMax)) * sizeof(typename P::Smem);
   return ((size_t)1 << K) * sizeof(typename P::Smem) + ((size_t)1 << (K - L)) * sizeof(uint64_t);
 }
 

@@ -61,10 +61,33 @@ static void apply_gate(std::vector<cd>& s, int n, int target, uint64_t cmask, co
   }
 }
 
+// a dense 2^m x 2^m unitary (row-major, interleaved) on qubits t .. t+m-1
+static void apply_unitary(std::vector<cd>& s, int n, int t, int m, uint64_t cmask, const double* u) {
+  const int D = 1 << m;
+  const uint64_t groups = 1ull << (n - m), low = (1ull << t) - 1;
+  std::vector<cd> x((size_t)D);
+  for (uint64_t g = 0; g < groups; ++g) {
+    const uint64_t base = ((g & ~low) << m) | (g & low);
+    if ((base & cmask) != cmask) continue;
+    for (int c = 0; c < D; ++c) x[(size_t)c] = s[base | ((uint64_t)c << t)];
+    for (int r = 0; r < D; ++r) {
+      cd acc(0.0, 0.0);
+      for (int c = 0; c < D; ++c) acc += cd(u[2 * (r * D + c)], u[2 * (r * D + c) + 1]) * x[(size_t)c];
+      s[base | ((uint64_t)r << t)] = acc;
+    }
+  }
+}
+
+static std::vector<double> g_pool;  // the unitary pool of the circuit's dense unitaries
+
 static void apply_tile_op(std::vector<cd>& s, int n, const TilePass& tp, const TileOp& t) {
   uint64_t cm = t.cmask_out;
   for (int j = 0; j < tp.K; ++j)
     if ((t.cmask_loc >> j) & 1u) cm |= 1ull << tp.q[j];
+  if (t.kind == GK_UNITARY) {
+    apply_unitary(s, n, tp.q[t.tloc], t.um, cm, g_pool.data() + t.uoff);
+    return;
+  }
   if (t.tloc >= 0) {
     apply_gate(s, n, tp.q[t.tloc], cm, t.m);
     return;
@@ -375,13 +398,30 @@ int main(int argc, char** argv) {
   fi.read(reinterpret_cast<char*>(s.data()), (std::streamsize)(s.size() * sizeof(cd)));
   std::vector<GateInstr> gates;
   for (int64_t i = 0; i < nops; ++i) {
-    if (ops[i].kind != BF_OP_GATE) return 4;  // the model covers gate circuits
-    gates.push_back(lower_gate(ops[i], BF_SPEC_ALL));
+    const bf_op& o = ops[i];
+    if ((o.kind == BF_OP_UNITARY || o.kind == BF_OP_CUNITARY) && o.target2 >= 2 && o.target2 <= kTileUnitaryMax) {
+      // a dense unitary of a fused run, as the engine plans it
+      GateInstr g;
+      std::memset(&g, 0, sizeof g);
+      g.kind = GK_UNITARY;
+      g.target = o.target;
+      g.cmask = o.kind == BF_OP_CUNITARY ? o.controls : 0ull;
+      g.um = o.target2;
+      g.uoff = (int32_t)g_pool.size();
+      g_pool.insert(g_pool.end(), o.data, o.data + 2 * ((size_t)1 << (2 * o.target2)));
+      gates.push_back(g);
+      continue;
+    }
+    if (o.kind != BF_OP_GATE) return 4;  // the model covers gates and small unitaries
+    gates.push_back(lower_gate(o, BF_SPEC_ALL));
   }
   int block_passes = 0, tile_passes = 0, gate_steps = 0;
   for (const PlanStep& ps : plan_gates(n, gates, kBlockTileQubits, true, digits ? 5.0 : 3.3)) {
     if (!ps.is_tile) {
-      apply_gate(s, n, ps.gate.target, ps.gate.cmask, ps.gate.m);
+      if (ps.gate.kind == GK_UNITARY)
+        apply_unitary(s, n, ps.gate.target, ps.gate.um, ps.gate.cmask, g_pool.data() + ps.gate.uoff);
+      else
+        apply_gate(s, n, ps.gate.target, ps.gate.cmask, ps.gate.m);
       ++gate_steps;
       continue;
     }
@@ -389,7 +429,8 @@ int main(int argc, char** argv) {
     std::vector<unsigned char> images;
     std::vector<uint16_t> offsets;
     if (ps.tile.K == kBlockTileQubits && ps.tile.L == kTileLowQubits &&
-        plan_blocks(ps.tile, blocks, images, offsets, digits ? BLOCK_DIGITS : BLOCK_TF32)) {
+        plan_blocks(ps.tile, blocks, images, offsets, digits ? BLOCK_DIGITS : BLOCK_TF32, kMaxPassBlocks,
+                    g_pool.data())) {
       if (exact) {
         if (e_scale == 0) {
           double nrm2 = 0;

@@ -190,3 +190,55 @@ def test_five_digit_round_trip_keeps_the_norm(model, tmp_path):
     assert abs(float(np.sum(np.abs(got) ** 2)) - 1.0) <= 1e-11
     assert float(np.max(np.abs(got - (re + 1j * im)))) <= 2e-10
     del OA
+
+
+def random_unitary(dim, rng):
+    a = rng.normal(size=(dim, dim)) + 1j * rng.normal(size=(dim, dim))
+    q, r = np.linalg.qr(a)
+    return q * (np.diag(r) / np.abs(np.diag(r)))
+
+
+def unitary_circuit(n, count, seed):
+    """Gates mixed with dense 2- and 3-qubit unitaries, some controlled."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    qc = bfy.QuantumCircuit(n)
+    for _ in range(count):
+        kind = int(rng.integers(0, 4))
+        if kind <= 1:
+            m = 2 + kind
+            t = int(rng.integers(0, n - m + 1))
+            qc.unitary(random_unitary(1 << m, rng), t, m)
+        elif kind == 2:
+            m = 2
+            t = int(rng.integers(0, n - m + 1))
+            c = int(rng.choice([q for q in range(n) if q < t or q >= t + m]))
+            qc.c_unitary(random_unitary(4, rng), c, t, m)
+        else:
+            qs = [int(x) for x in rng.permutation(n)[:2]]
+            qc.u3(qs[0], float(rng.uniform(0, 6)), float(rng.uniform(0, 6)), float(rng.uniform(0, 6)))
+            qc.cx(qs[0], qs[1])
+    return qc
+
+
+UNITARY_CIRCUITS = {
+    "fused_layered14": lambda: __import__("code_mojo_gb300.fusion", fromlist=["fuse_circuit"]).fuse_circuit(
+        W.random_layered_circuit(14, 12, seed=5)),
+    "unitaries13": lambda: unitary_circuit(13, 60, 6),
+}
+
+
+@pytest.mark.parametrize("fmt", ["digits", "tf32", "digits-exact"])
+@pytest.mark.parametrize("name", list(UNITARY_CIRCUITS))
+def test_dense_unitaries_in_block_passes(model, fmt, name, tmp_path):
+    """Dense 2- and 3-qubit unitaries (from the fusion rewrites, or written
+    directly, some controlled) are multiplied into the tensor-core blocks of
+    the fused run around them."""
+    qc = UNITARY_CIRCUITS[name]()
+    assert any(isinstance(t, (bfy.UnitaryTransformation, bfy.ControlledUnitaryTransformation))
+               for t in qc.transformations)
+    re, im = W.random_normal_state(qc.num_qubits, 11)
+    got, block_passes = run_model(model, fmt, qc, re, im, tmp_path)
+    r, i = O.run(qc, re, im)
+    tol = 1e-12 if fmt.startswith("digits") else 1e-5
+    assert block_passes > 0
+    assert float(np.max(np.abs(got - (r + 1j * i)))) <= tol

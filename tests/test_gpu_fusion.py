@@ -70,3 +70,75 @@ def test_complex64_fused_value_encoding(n):
     got = run_gpu(FU.fuse_circuit_specialized_pairs(qc), bfy.ExecutionStrategy.GPU_FUSED, dtype="c64")
     exp = oracle_of(qc)
     assert 1 - abs(np.vdot(exp, got)) ** 2 <= 1e-6
+
+
+def _random_unitary(dim, rng):
+    a = rng.normal(size=(dim, dim)) + 1j * rng.normal(size=(dim, dim))
+    q, r = np.linalg.qr(a)
+    return q * (np.diag(r) / np.abs(np.diag(r)))
+
+
+def _unitary_circuit(n, count, seed):
+    """Gates mixed with dense 2- and 3-qubit unitaries, some controlled."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    qc = bfy.QuantumCircuit(n)
+    for _ in range(count):
+        kind = int(rng.integers(0, 4))
+        if kind <= 1:
+            m = 2 + kind
+            t = int(rng.integers(0, n - m + 1))
+            qc.unitary(_random_unitary(1 << m, rng), t, m)
+        elif kind == 2:
+            t = int(rng.integers(0, n - 1))
+            c = int(rng.choice([q for q in range(n) if q < t or q >= t + 2]))
+            qc.c_unitary(_random_unitary(4, rng), c, t, 2)
+        else:
+            qs = [int(x) for x in rng.permutation(n)[:2]]
+            qc.u3(qs[0], float(rng.uniform(0, 6)), float(rng.uniform(0, 6)), float(rng.uniform(0, 6)))
+            qc.cx(qs[0], qs[1])
+    return qc
+
+
+@pytest.mark.parametrize("n", [9, 13, 16])
+@pytest.mark.parametrize("tensor", [True, False])
+@pytest.mark.parametrize("dtype", ["c128", "c64"])
+def test_dense_unitaries_join_fused_runs(n, tensor, dtype):
+    """Dense 2- and 3-qubit unitaries run inside the fused run's tile passes
+    (CUDA-core tiles, or multiplied into tensor-core blocks): the plan has no
+    pass of its own for them, and the state matches the oracle."""
+    qc = _unitary_circuit(n, 50, 20 + n)
+    state = W.random_normal_state(n, 3)
+    ctx = bfy.ExecContext()
+    ctx.execution_strategy = bfy.ExecutionStrategy.GPU_FUSED
+    ctx.gpu_tensor_blocks = tensor
+    plan = bfy.plan_stats(qc, ctx, dtype)
+    assert plan["other_passes"] == 0 and plan["tile_passes"] > 0
+    if tensor and n >= 12:
+        assert plan["block_passes"] > 0
+    st = bfy.QuantumState.from_soa(*state, dtype)
+    bfy.execute(st, qc, ctx)
+    got = st.to_complex()
+    st.close()
+    exp = oracle_of(qc, state)
+    if dtype == "c128":
+        assert np.max(np.abs(got - exp)) <= 1e-12
+    else:
+        assert 1 - abs(np.vdot(exp, got)) ** 2 / (np.vdot(exp, exp).real * np.vdot(got, got).real) <= 1e-6
+
+
+@pytest.mark.parametrize("dtype", ["c128", "c64"])
+def test_fuse_circuit_layered_runs_in_tile_passes(dtype):
+    """fuse_circuit turns a layered circuit's neighbour pairs into 4x4
+    unitaries; under GPU_FUSED they stay in the tile passes."""
+    n = 18
+    qc = W.random_layered_circuit(n, 8, seed=3)
+    fq = FU.fuse_circuit(qc)
+    ctx = bfy.ExecContext()
+    ctx.execution_strategy = bfy.ExecutionStrategy.GPU_FUSED
+    assert bfy.plan_stats(fq, ctx, dtype)["other_passes"] == 0
+    got = run_gpu(fq, bfy.ExecutionStrategy.GPU_FUSED, dtype=dtype)
+    exp = oracle_of(qc)
+    if dtype == "c128":
+        assert np.max(np.abs(got - exp)) <= 1e-12
+    else:
+        assert 1 - abs(np.vdot(exp, got)) ** 2 <= 1e-6
