@@ -38,11 +38,12 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "30q HBM GB/s vs peak; served circuits/s, p50/p99 ms at fidelity≥1-1e-6"
 # DRAM bytes (read + write) per amplitude of one launch, from ncu captures of
-# the same kernels at 26 qubits; traffic grows in proportion to the amplitudes
-# a launch processes.  Double-float tile pass: 2.153 GB / 2^26.
+# the same kernels on smaller states; traffic grows in proportion to the
+# amplitudes a launch processes.  Double-float tile pass: 2.153 GB / 2^26.
 TILE_TRAFFIC_BYTES_PER_AMP = 32.08
-# complex128 digit block pass (k_tblock_dg): 2.102 GB / 2^26
-DIGIT_TRAFFIC_BYTES_PER_AMP = 31.33
+# complex128 digit block pass (k_tblock_dg), 28 qubits, 4 layers: 4.297 GB
+# read + 4.239 GB written / 2^28
+DIGIT_TRAFFIC_BYTES_PER_AMP = 31.80
 # Tensor work of one complex128 digit block on one 128-row tile (4096
 # amplitudes): 26 digit-pair products of 128 x 64 x 64, 2 flops each, for a
 # six-digit tile; 20 for a five-digit tile.
@@ -789,9 +790,10 @@ def run_ours(args) -> None:
         return
     value = pg_bytes * world / (ms_step * 1e-3) / 1e9
     digits = plan["block_passes"] > 0
-    arith = ("exact base-256 digit products on bf16 tensor cores (per 4096-amplitude tile: a power-of-two scale "
-             "from the tile's norm and five or six digits, rounding unit at most 2^-48 of the state's scale per "
-             "block pass) and double-float tile passes" if digits else "double-float arithmetic")
+    arith = ("exact base-256 digit products on bf16 tensor cores (fixed point: one unit, 2^-48 of a power-of-two "
+             "scale at least twice the state's norm; a 4096-amplitude tile whose norm is below 2^-9 of the scale "
+             "runs five digits, otherwise six, with the same integers; consecutive digit passes hand the state "
+             "over as those integers) and double-float tile passes" if digits else "double-float arithmetic")
     line = {
         "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",

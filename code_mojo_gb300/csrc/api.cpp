@@ -698,7 +698,9 @@ static cudaEvent_t pass_event(State& st, size_t k) {
 static void run_steps(State& st, const std::vector<Step>& steps, const Program& pg, uint64_t plan_id) {
   upload_program(st, pg, plan_id);
   bool scaled = false;
-  for (const auto& s : steps) {
+  auto digit_pass = [&](size_t i) { return i < steps.size() && steps[i].kind == Step::TBLOCK && steps[i].digits; };
+  for (size_t si = 0; si < steps.size(); ++si) {
+    const Step& s = steps[si];
     if (s.kind == Step::TBLOCK && s.digits && !scaled) {
       // the digit scale, from the norm before the first digit pass
       if (!st.d_scale) st.d_scale = static_cast<int*>(dev_alloc(st, 16));
@@ -715,10 +717,12 @@ static void run_steps(State& st, const std::vector<Step>& steps, const Program& 
         break;
       case Step::TBLOCK:
         if (s.digits) {
+          // consecutive digit passes hand the state over as its fixed-point
+          // integers; the first reads FP64 and the last writes it
           launch_block_pass_digits(st, reinterpret_cast<const Blk5*>(st.d_aux) + s.blk_off, s.nblk,
                                    st.d_aux + pg.images_offset(),
                                    reinterpret_cast<const uint16_t*>(st.d_aux + pg.offsets_offset()), s.tile,
-                                   st.d_scale);
+                                   st.d_scale, si > 0 && digit_pass(si - 1), digit_pass(si + 1));
         } else {
           launch_block_pass(st, reinterpret_cast<const Blk5*>(st.d_aux) + s.blk_off, s.nblk,
                             st.d_aux + pg.images_offset(),

@@ -324,8 +324,14 @@ void launch_block_pass(State& st, const Blk5* d_blocks, int nblocks, const unsig
                        const uint16_t* d_offsets, const TilePass& p);
 // complex128 digit blocks (BLOCK_DIGITS); d_exp holds the scale exponent
 // that launch_digit_scale computed from the state's norm
+// in_fixed: the state holds the previous digit pass's output as int64 pairs
+// (the integers V of the unit 2^-48 of the scale, not FP64 values);
+// out_fixed: write them so for the next digit pass.  Between two digit
+// passes of one circuit the state is in this form; any other reader needs
+// FP64, so the pass before it writes FP64.
 void launch_block_pass_digits(State& st, const Blk5* d_blocks, int nblocks, const unsigned char* d_images,
-                              const uint16_t* d_offsets, const TilePass& p, const int* d_exp);
+                              const uint16_t* d_offsets, const TilePass& p, const int* d_exp, bool in_fixed = false,
+                              bool out_fixed = false);
 void launch_digit_scale(State& st, int* d_exp);
 // the device counters of five- and six-digit tiles (allocated and zeroed on first use)
 unsigned long long* digit_tile_counters(State& st);

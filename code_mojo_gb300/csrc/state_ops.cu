@@ -351,8 +351,9 @@ void launch_renormalize(State& st, bool unit_before) {
 // ---- dense m-qubit unitary on contiguous qubits [t, t+m) ------------------
 // apply_unitary / apply_controlled_unitary (transformations_unitary.mojo:
 // 22-139): groups of 2^m amplitudes base + (k << t); out[row] =
-// sum_col u[row*dim + col] * in[col].  A CTA of 256 threads holds
-// G = 256 / dim groups in shared memory; thread (g, row) forms one output.
+// sum_col u[row*dim + col] * in[col].  For m >= 4 a CTA of 256 threads
+// holds G = 256 / dim groups in shared memory and thread (g, row) forms one
+// output; smaller unitaries run in registers (k_unitary_reg).
 constexpr int kUniThreads = 256;
 constexpr int kUniMaxM = 6;
 
@@ -420,6 +421,46 @@ __global__ void __launch_bounds__(kUniThreads) k_unitary(typename P::Glob* __res
   }
 }
 
+// m <= 3: each thread holds whole groups of 2^m amplitudes in registers
+// (all loads issued before the matrix-vector product), the matrix staged in
+// shared memory; consecutive threads take consecutive groups, so for a
+// target block above the low 5 qubits every load and store instruction of
+// a warp is one contiguous run.
+template <class P, int M>
+__global__ void __launch_bounds__(kUniThreads) k_unitary_reg(typename P::Glob* __restrict__ s,
+                                                             const double* __restrict__ u, const UniArgs a) {
+  using R = typename P::R;
+  using Sm = typename P::Smem;
+  constexpr int D = 1 << M;
+  __shared__ Sm mat[D * D];
+  for (int e = threadIdx.x; e < D * D; e += kUniThreads) {
+    typename P::Glob gv;
+    if constexpr (sizeof(typename P::Glob) == 16) gv = make_double2(u[2 * e], u[2 * e + 1]);
+    else gv = make_float2((float)u[2 * e], (float)u[2 * e + 1]);
+    mat[e] = P::to_smem(P::from_glob(gv));
+  }
+  __syncthreads();
+  const uint64_t stride = (uint64_t)gridDim.x * kUniThreads;
+  for (uint64_t gi = (uint64_t)blockIdx.x * kUniThreads + threadIdx.x; gi < a.groups; gi += stride) {
+    uint64_t x = gi;
+#pragma unroll
+    for (int i = 0; i < M + 1; ++i)  // the targets and at most one control
+      if (i < a.nfix) x = insert_zero_bit(x, a.fix[i]);
+    x |= a.cbit;
+    R v[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) v[c] = P::from_glob(s[x | ((uint64_t)c << a.t)]);
+    // one output row at a time keeps the register count near the group's
+#pragma unroll 1
+    for (int r = 0; r < D; ++r) {
+      R acc = P::zero();
+#pragma unroll
+      for (int c = 0; c < D; ++c) acc = P::fma(P::from_smem(mat[r * D + c]), v[c], acc);
+      s[x | ((uint64_t)r << a.t)] = P::to_glob(acc);
+    }
+  }
+}
+
 template <class P>
 static void launch_unitary_p(State& st, const double* h_u, int t, int m, int control) {
   int dim = 1 << m;
@@ -447,6 +488,16 @@ static void launch_unitary_p(State& st, const double* h_u, int t, int m, int con
   }
   double* d_u = st.d_umat;
   BF_CUDA(cudaMemcpyAsync(d_u, h_u, mbytes, cudaMemcpyHostToDevice, st.stream));
+  if (m <= 3) {
+    const uint64_t ctas = std::min<uint64_t>((a.groups + kUniThreads - 1) / kUniThreads, (uint64_t)st.num_sms * 8);
+    typename P::Glob* amp = static_cast<typename P::Glob*>(st.amp);
+    if (m == 1) k_unitary_reg<P, 1><<<(unsigned)ctas, kUniThreads, 0, st.stream>>>(amp, d_u, a);
+    else if (m == 2) k_unitary_reg<P, 2><<<(unsigned)ctas, kUniThreads, 0, st.stream>>>(amp, d_u, a);
+    else k_unitary_reg<P, 3><<<(unsigned)ctas, kUniThreads, 0, st.stream>>>(amp, d_u, a);
+    BF_CUDA(cudaGetLastError());
+    st.launches++;
+    return;
+  }
   size_t smem = ((size_t)dim * dim + kUniThreads) * sizeof(typename P::Smem);
   static PerDeviceOnce configured;  // one per instantiation of P
   configured.run(st.device, [] {

@@ -455,6 +455,8 @@ struct DgPassArgs {
   int32_t scale_shift;          // added to the state's scale exponent (0; a test moves it)
   int32_t five_digits;          // 1: tiles below the norm bound run five digits; 0: six always
   unsigned long long* digit_tiles;  // optional: [0] five-digit tiles, [1] six-digit tiles (counted per CTA)
+  int32_t in_fixed;             // 1: the state holds the previous digit pass's integers V (int64 pairs)
+  int32_t out_fixed;            // 1: write V itself for the next digit pass instead of FP64
 };
 
 __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
@@ -608,6 +610,43 @@ __device__ __forceinline__ uint32_t sq_bound_units(double x, int e) {
   const int k = 2 * (ex - e) - 2012;
   if (k >= 11) return kDgWarpBound;               // u2 >= 2^16: the term alone reaches the bound
   if (k >= 0) return min(u2 << k, kDgWarpBound);  // below 2^29 before the min
+  if (k <= -19) return 1;
+  return (u2 + (1u << -k) - 1) >> -k;
+}
+
+// digits_of for a value already held as its integer V of the unit (the
+// output of the previous digit pass): the same digits, no rounding
+template <int D>
+__device__ __forceinline__ bool digits_of_fixed(long long V, float* d) {
+  const bool ok = V < (1ll << (8 * D - 1)) && V > -(1ll << (8 * D - 1));
+  const unsigned long long W = (unsigned long long)(V + (D == 6 ? 0x808080808080ll : 0x8080808080ll));
+  const uint32_t wl = (uint32_t)W, wh = (uint32_t)(W >> 32);
+  d[D - 1] = byte_digit(wl, 0);
+  d[D - 2] = byte_digit(wl, 1);
+  d[D - 3] = byte_digit(wl, 2);
+  d[D - 4] = byte_digit(wl, 3);
+  if (D == 6) {
+    d[1] = byte_digit(wh, 0);
+    d[0] = __int_as_float((int)(0x4B400000u | (wh >> 8))) - 12583040.0f;
+  } else {
+    d[0] = __int_as_float((int)(0x4B400000u | wh)) - 12583040.0f;
+  }
+  return ok;
+}
+
+// sq_bound_units of x = V 2^(e - 48) from V: the exponent difference ex - e
+// is lead + 975 (lead = the position of V's leading one), so k = 2 lead - 62
+// whatever the scale, and m8 is the 8 bits below the leading one
+__device__ __forceinline__ uint32_t sq_bound_units_fixed(long long V) {
+  if (V == 0) return 0;
+  const unsigned long long a = (unsigned long long)(V < 0 ? -V : V);
+  const int lead = 63 - __clzll(a);
+  const uint32_t m8 = (uint32_t)((lead >= 8 ? a >> (lead - 8) : a << (8 - lead)) & 255u);
+  const uint32_t u = 257u + m8;
+  const uint32_t u2 = u * u;
+  const int k = 2 * lead - 62;
+  if (k >= 11) return kDgWarpBound;
+  if (k >= 0) return min(u2 << k, kDgWarpBound);
   if (k <= -19) return 1;
   return (u2 + (1u << -k) - 1) >> -k;
 }
@@ -802,7 +841,8 @@ __device__ __forceinline__ bool dg_tile(const DgPassArgs& a, const DgFixed& f, D
         const long long vi = (long long)(hi[2 * c + 1] + int_of_small(carry[2 * c + 1]) * (1 << (8 * (D - 4)))) *
                                  16777216ll +
                              (long long)lo[2 * c + 1];
-        stage[dest_at4(dest, c)] = make_double2(double_of(vr, e - 48), double_of(vi, e - 48));
+        stage[dest_at4(dest, c)] = a.out_fixed ? make_double2(__longlong_as_double(vr), __longlong_as_double(vi))
+                                               : make_double2(double_of(vr, e - 48), double_of(vi, e - 48));
       }
     }
     if (tid == 0 && lost && p.issued) p.mma_lost_phase = (int)(k & 1u);
@@ -952,9 +992,16 @@ __global__ void __launch_bounds__(kDgThreads, 1) k_tblock_dg(const DgPassArgs a)
 #pragma unroll
     for (int el = 0; el < 2 * kDgLoadIters; ++el) {
       float dr[kDgFewDigits], di[kDgFewDigits];
-      six |= !digits_of<kDgFewDigits>(v[el].x, sh, dr);
-      six |= !digits_of<kDgFewDigits>(v[el].y, sh, di);
-      tb += sq_bound_units(v[el].x, e) + sq_bound_units(v[el].y, e);
+      if (a.in_fixed) {
+        const long long vr = __double_as_longlong(v[el].x), vi = __double_as_longlong(v[el].y);
+        six |= !digits_of_fixed<kDgFewDigits>(vr, dr);
+        six |= !digits_of_fixed<kDgFewDigits>(vi, di);
+        tb += sq_bound_units_fixed(vr) + sq_bound_units_fixed(vi);
+      } else {
+        six |= !digits_of<kDgFewDigits>(v[el].x, sh, dr);
+        six |= !digits_of<kDgFewDigits>(v[el].y, sh, di);
+        tb += sq_bound_units(v[el].x, e) + sq_bound_units(v[el].y, e);
+      }
       const uint32_t off = dest_at4(load_dest, el) << 2;
 #pragma unroll
       for (int q = 0; q < kDgFewDigits; ++q)
@@ -969,8 +1016,13 @@ __global__ void __launch_bounds__(kDgThreads, 1) k_tblock_dg(const DgPassArgs a)
 #pragma unroll
       for (int el = 0; el < 2 * kDgLoadIters; ++el) {
         float dr[kDigits], di[kDigits];
-        p.range_ok &= digits_of<kDigits>(v[el].x, sh, dr);
-        p.range_ok &= digits_of<kDigits>(v[el].y, sh, di);
+        if (a.in_fixed) {
+          p.range_ok &= digits_of_fixed<kDigits>(__double_as_longlong(v[el].x), dr);
+          p.range_ok &= digits_of_fixed<kDigits>(__double_as_longlong(v[el].y), di);
+        } else {
+          p.range_ok &= digits_of<kDigits>(v[el].x, sh, dr);
+          p.range_ok &= digits_of<kDigits>(v[el].y, sh, di);
+        }
         const uint32_t off = dest_at4(load_dest, el) << 2;
 #pragma unroll
         for (int q = 0; q < kDigits; ++q)
@@ -1038,7 +1090,8 @@ void launch_digit_scale(State& st, int* d_exp) {
 }
 
 void launch_block_pass_digits(State& st, const Blk5* d_blocks, int nblocks, const unsigned char* d_images,
-                              const uint16_t* d_offsets, const TilePass& p, const int* d_exp) {
+                              const uint16_t* d_offsets, const TilePass& p, const int* d_exp, bool in_fixed,
+                              bool out_fixed) {
   if (st.dtype != BF_C128) fail(BF_EINVAL, "internal: digit blocks need a complex128 state");
   if (p.K != kBlockTileQubits || st.n < kBlockTileQubits) fail(BF_EINVAL, "internal: block pass needs a 12-qubit tile");
   if (nblocks < 1 || nblocks > kMaxPassBlocks) fail(BF_EINVAL, "internal: block pass of %d blocks", nblocks);
@@ -1069,6 +1122,8 @@ void launch_block_pass_digits(State& st, const Blk5* d_blocks, int nblocks, cons
   const char* five = std::getenv("BFGPU_DIGIT_FIVE");
   a.five_digits = (five && *five == '0') ? 0 : 1;
   a.digit_tiles = digit_tile_counters(st);
+  a.in_fixed = in_fixed ? 1 : 0;
+  a.out_fixed = out_fixed ? 1 : 0;
   static PerDeviceOnce configured;
   configured.run(st.device, [] {
     BF_CUDA(cudaFuncSetAttribute(k_tblock_dg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDgSmemAlloc));

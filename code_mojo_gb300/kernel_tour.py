@@ -24,6 +24,7 @@ import numpy as np
 from . import butterfly as bfy
 from . import opsarray as OA
 from . import workloads as W
+from .fusion import fuse_circuit
 
 
 def tour(n: int, dtype: str, reps: int) -> list[dict]:
@@ -60,7 +61,7 @@ def tour(n: int, dtype: str, reps: int) -> list[dict]:
          circ(lambda q: q.transformations.append(bfy.ClassicalTransformation("SWAP", [1, hi]))), per_gate),
         ("full bit reversal", "k_bitrev_tiles", 2.0, circ(lambda q: bfy.bit_reverse(q)), per_gate),
         ("qubit permutation", "k_permute", 2.0, circ(lambda q: bfy.permute_qubits(q, perm)), per_gate),
-        ("dense 3-qubit unitary", "k_unitary", 2.0,
+        ("dense 3-qubit unitary", "k_unitary_reg", 2.0,
          circ(lambda q: q.unitary(np.eye(8, dtype=complex) * np.exp(0.3j), hi - 2, 3)), per_gate),
         ("Grover diffuser (classical, all qubits)", "k_diff_sum/k_diff_mean/k_diff_update", 3.0,
          circ(lambda q: bfy.grover_diffuser(q)), per_gate),
@@ -69,6 +70,8 @@ def tour(n: int, dtype: str, reps: int) -> list[dict]:
              bfy.ClassicalTransformation("MOD_EXP", [n - 8, 8, 7, 255]))), per_gate),
         ("fused layered circuit, 2 layers", "k_tblock_dg / k_tblock / k_tile", None,
          W.random_layered_circuit(n, 2, seed=4), fused),
+        ("the same 2 layers after fuse_circuit (4x4 unitaries in the run)", "k_tblock_dg / k_tblock / k_tile", None,
+         fuse_circuit(W.random_layered_circuit(n, 2, seed=4)), fused),
     ]
     out = []
 

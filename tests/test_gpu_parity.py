@@ -227,6 +227,22 @@ def test_dense_unitaries(m, target, controlled, c128_math):
     assert maxdiff(run_gpu(qc, re, im, bfy.ExecutionStrategy.GPU), oracle(qc, re, im)) <= TOL128
 
 
+@pytest.mark.parametrize("m,target", [(1, 9), (2, 0), (2, 3), (3, 1), (3, 10)])
+@pytest.mark.parametrize("controlled", [False, True])
+def test_dense_unitaries_complex64(m, target, controlled):
+    n = 14
+    re, im = W.random_normal_state(n, 30 + m)
+    qc = bfy.QuantumCircuit(n)
+    u = random_unitary(1 << m, 7 * m + target)
+    if controlled:
+        qc.c_unitary(u, 13 if target + m <= 13 else 0, target, m)
+    else:
+        qc.unitary(u, target, m)
+    z = run_gpu(qc, re, im, bfy.ExecutionStrategy.GPU, dtype="c64")
+    exp = oracle(qc, re, im)
+    assert 1 - abs(np.vdot(exp, z)) ** 2 / (np.vdot(exp, exp).real * np.vdot(z, z).real) <= 1e-6
+
+
 # ---- ports of the reference's grid tests --------------------------------------
 @pytest.mark.parametrize("n,col_bits", [(10, 5), (12, 6), (14, 7)])
 def test_grid_tiling_cases(n, col_bits):
