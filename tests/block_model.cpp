@@ -307,7 +307,8 @@ static void run_digit_pass_exact(std::vector<cd>& s, int n, const TilePass& tp, 
         }
       if (!last) opnd.swap(next);
     }
-    for (uint32_t i = 0; i < 4096; ++i) s[gi(i)] = cd(stage_re[block_stage_slot(i)], stage_im[block_stage_slot(i)]);
+    // the digit kernel's last table names each result's tile element
+    for (uint32_t i = 0; i < 4096; ++i) s[gi(i)] = cd(stage_re[i], stage_im[i]);
   }
 }
 
@@ -365,8 +366,8 @@ static void run_block_pass(std::vector<cd>& s, int n, const TilePass& tp, const 
         }
       opnd.swap(next);
     }
-    // opnd now holds the staging slots
-    for (uint32_t i = 0; i < 4096; ++i) s[gi(i)] = opnd[block_stage_slot(i)];
+    // opnd now holds the staging slots (the digit kernel's: tile elements)
+    for (uint32_t i = 0; i < 4096; ++i) s[gi(i)] = opnd[digits ? i : block_stage_slot(i)];
   }
 }
 
