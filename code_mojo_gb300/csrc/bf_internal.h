@@ -195,7 +195,7 @@ constexpr uint32_t kDigitImageBytes = kDigits * 8192;
 // Partitions the ops of a 12-qubit tile pass into blocks and appends their
 // matrix images and destination tables (u16 per thread and element: the
 // next block's operand offset in the format's units, or after the last
-// block the staging slot); false when an op cannot be placed (more than 5
+// block the tile element); false when an op cannot be placed (more than 5
 // tile qubits or more than 3 outside qubits on its own), the pass needs more
 // than min(kMaxPassBlocks, max_blocks) blocks (checked before any matrix is
 // built), or (BLOCK_DIGITS) a block's matrix is not unitary to 1e-12.
@@ -220,8 +220,6 @@ BF_HOST_DEVICE inline uint32_t block_operand_offset(uint32_t g, uint32_t j) {
 BF_HOST_DEVICE inline uint32_t digit_operand_offset(uint32_t g, uint32_t j) {
   return (g << 7) + ((((j >> 2) ^ (g & 7))) << 4) + ((j & 3) << 2);
 }
-// staging slot of tile element i after the last block (pairs stay adjacent)
-BF_HOST_DEVICE inline uint32_t block_stage_slot(uint32_t i) { return i ^ (((i >> 5) & 15u) << 1); }
 // The matrix image of a 32x32 complex matrix u (row-major, interleaved
 // re/im): the real 64x64 operand R^T, split into TF32 hi and lo parts, in
 // the swizzled K-major layout of the block kernel.

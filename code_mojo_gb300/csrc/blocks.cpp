@@ -435,10 +435,9 @@ bool plan_blocks(const TilePass& tp, std::vector<Blk5>& blocks, std::vector<unsi
         if (k + 1 < maps.size()) {
           v = dest(lut[k + 1].g_of[i], lut[k + 1].j_of[i]);
         } else {
-          // after the last block: the TF32 kernel's staging slot, or for
-          // the digit kernel (which stores its results directly) the tile
-          // element itself
-          v = (uint16_t)(format == BLOCK_DIGITS ? i : block_stage_slot(i));
+          // after the last block: the tile element itself (both kernels
+          // store their results straight to the state)
+          v = (uint16_t)i;
         }
         offsets[at + (size_t)t * E + e] = v;
       }

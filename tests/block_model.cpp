@@ -366,8 +366,8 @@ static void run_block_pass(std::vector<cd>& s, int n, const TilePass& tp, const 
         }
       opnd.swap(next);
     }
-    // opnd now holds the staging slots (the digit kernel's: tile elements)
-    for (uint32_t i = 0; i < 4096; ++i) s[gi(i)] = opnd[digits ? i : block_stage_slot(i)];
+    // opnd now holds the results by tile element
+    for (uint32_t i = 0; i < 4096; ++i) s[gi(i)] = opnd[i];
   }
 }
 
