@@ -3,10 +3,13 @@
 // (butterfly/core/executors.mojo:268-319).
 #include <algorithm>
 #include <cmath>
+#include <condition_variable>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
+#include <thread>
 #include <vector>
 
 #include "bf_internal.h"
@@ -852,6 +855,7 @@ void release_state_members(State& st) {
   if (st.scratch) cudaFree(st.scratch);
   if (st.h_prog) cudaFreeHost(st.h_prog);
   if (st.d_stage) cudaFree(st.d_stage);
+  if (st.h_stage) cudaFreeHost(st.h_stage);
   for (int k = 0; k < 2; ++k) {
     if (st.stage_copied[k]) cudaEventDestroy(st.stage_copied[k]);
     if (st.stage_done[k]) cudaEventDestroy(st.stage_done[k]);
@@ -912,11 +916,146 @@ static double* stage_re(State& st, int k) {
 }
 static double* stage_im(State& st, int k) { return stage_re(st, k) + std::min<uint64_t>(st.N, kStageElems); }
 
+// ---- host threads for copies between pageable arrays and pinned staging ----
+// A copy from pageable memory goes through the driver's own staging, one
+// CPU thread at a time.  For large transfers the library instead copies
+// each chunk between the caller's arrays and pinned buffers with a pool of
+// host threads (the calling thread takes a share too) while the DMA engine
+// moves the previous chunk.
+class CopyPool {
+ public:
+  static CopyPool& get() {
+    static CopyPool pool;
+    return pool;
+  }
+  // dst[0, bytes) = src[0, bytes), split over the workers and the caller
+  void copy(void* dst, const void* src, size_t bytes) {
+    const size_t parts = workers_.size() + 1;
+    const size_t part = ((bytes / parts) + 255) & ~(size_t)255;
+    {
+      std::lock_guard<std::mutex> lk(m_);
+      dst_ = static_cast<char*>(dst);
+      src_ = static_cast<const char*>(src);
+      bytes_ = bytes;
+      part_ = part;
+      pending_ = (int)workers_.size();
+      ++gen_;
+    }
+    cv_.notify_all();
+    run_part(workers_.size());  // the caller's share: the last part
+    std::unique_lock<std::mutex> lk(m_);
+    done_.wait(lk, [&] { return pending_ == 0; });
+  }
+  ~CopyPool() {
+    {
+      std::lock_guard<std::mutex> lk(m_);
+      stop_ = true;
+      ++gen_;
+    }
+    cv_.notify_all();
+    for (auto& t : workers_) t.join();
+  }
+
+ private:
+  CopyPool() {
+    const unsigned hw = std::thread::hardware_concurrency();
+    const unsigned n = std::max(1u, std::min(16u, hw ? hw : 4u)) - 1;
+    for (unsigned i = 0; i < n; ++i) workers_.emplace_back([this, i] { loop(i); });
+  }
+  void run_part(size_t i) {
+    const size_t lo = std::min(bytes_, i * part_), hi = std::min(bytes_, lo + part_);
+    if (i == workers_.size()) {
+      if (lo < bytes_) std::memcpy(dst_ + lo, src_ + lo, bytes_ - lo);
+    } else if (hi > lo) {
+      std::memcpy(dst_ + lo, src_ + lo, hi - lo);
+    }
+  }
+  void loop(size_t i) {
+    uint64_t seen = 0;
+    for (;;) {
+      {
+        std::unique_lock<std::mutex> lk(m_);
+        cv_.wait(lk, [&] { return gen_ != seen; });
+        seen = gen_;
+        if (stop_) return;
+      }
+      run_part(i);
+      std::lock_guard<std::mutex> lk(m_);
+      if (--pending_ == 0) done_.notify_one();
+    }
+  }
+  std::vector<std::thread> workers_;
+  std::mutex m_;
+  std::condition_variable cv_, done_;
+  uint64_t gen_ = 0;
+  bool stop_ = false;
+  int pending_ = 0;
+  char* dst_ = nullptr;
+  const char* src_ = nullptr;
+  size_t bytes_ = 0, part_ = 0;
+};
+
+// Host arrays the DMA engine cannot read directly (ordinary pageable
+// memory), for transfers of at least one whole chunk: these go through the
+// pinned staging.
+static bool use_host_staging(const State& st, uint64_t count, const void* re, const void* im) {
+  if (count < kStageElems) return false;
+  for (const void* p : {re, im}) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    if (at.type != cudaMemoryTypeUnregistered) return false;
+  }
+  (void)st;
+  return true;
+}
+
+static void ensure_host_stage(State& st) {
+  const size_t want = (size_t)kStageElems * 2 * sizeof(double) * 2;
+  if (st.h_stage_bytes >= want) return;
+  if (st.h_stage) cudaFreeHost(st.h_stage);
+  st.h_stage = nullptr;
+  st.h_stage_bytes = 0;
+  st.h_stage = host_alloc(want);
+  st.h_stage_bytes = want;
+}
+static double* hstage_re(State& st, int k) { return static_cast<double*>(st.h_stage) + (size_t)k * 2 * kStageElems; }
+static double* hstage_im(State& st, int k) { return hstage_re(st, k) + kStageElems; }
+
 // Host SoA -> device.  Returns once every byte of re and im has been copied
 // out of host memory (the conversion kernels may still run, stream-ordered
 // before any later work on the state), so the caller may reuse the arrays.
 static void upload_soa(State& st, const double* re, const double* im) {
   ensure_stage(st);
+  if (use_host_staging(st, st.N, re, im)) {
+    // host threads fill pinned buffer k while the DMA of the other runs
+    ensure_host_stage(st);
+    CopyPool& pool = CopyPool::get();
+    const uint64_t chunk = kStageElems;
+    BF_CUDA(cudaEventRecord(st.stage_start, st.stream));
+    BF_CUDA(cudaStreamWaitEvent(st.copy_stream, st.stage_start, 0));
+    int k = 0;
+    for (uint64_t off = 0; off < st.N; off += chunk, k ^= 1) {
+      const uint64_t cnt = std::min(chunk, st.N - off);
+      // pinned buffer k is free once the DMA of two chunks back is done
+      if (off >= 2 * chunk) BF_CUDA(cudaEventSynchronize(st.stage_copied[k]));
+      pool.copy(hstage_re(st, k), re + off, cnt * sizeof(double));
+      pool.copy(hstage_im(st, k), im + off, cnt * sizeof(double));
+      if (off >= 2 * chunk) BF_CUDA(cudaStreamWaitEvent(st.copy_stream, st.stage_done[k], 0));
+      BF_CUDA(cudaMemcpyAsync(stage_re(st, k), hstage_re(st, k), cnt * sizeof(double), cudaMemcpyHostToDevice,
+                              st.copy_stream));
+      BF_CUDA(cudaMemcpyAsync(stage_im(st, k), hstage_im(st, k), cnt * sizeof(double), cudaMemcpyHostToDevice,
+                              st.copy_stream));
+      BF_CUDA(cudaEventRecord(st.stage_copied[k], st.copy_stream));
+      BF_CUDA(cudaStreamWaitEvent(st.stream, st.stage_copied[k], 0));
+      launch_interleave(st, stage_re(st, k), stage_im(st, k), off, cnt);
+      BF_CUDA(cudaEventRecord(st.stage_done[k], st.stream));
+    }
+    BF_CUDA(cudaStreamSynchronize(st.copy_stream));
+    return;
+  }
   const uint64_t chunk = std::min<uint64_t>(st.N, kStageElems);
   // the staging buffers' earlier users are on the state's stream
   BF_CUDA(cudaEventRecord(st.stage_start, st.stream));
@@ -951,6 +1090,37 @@ static void download_soa(State& st, uint64_t offset, uint64_t count, double* re,
   const uint64_t nchunks = (count + chunk - 1) / chunk;
   BF_CUDA(cudaEventRecord(st.stage_start, st.copy_stream));
   BF_CUDA(cudaStreamWaitEvent(st.stream, st.stage_start, 0));
+  if (use_host_staging(st, count, re, im)) {
+    // the DMA of chunk c+1 into pinned buffer (c+1) & 1 runs while host
+    // threads copy chunk c out of buffer c & 1
+    ensure_host_stage(st);
+    CopyPool& pool = CopyPool::get();
+    auto convert_and_fetch = [&](uint64_t c) {
+      const int k = (int)(c & 1);
+      const uint64_t cnt = std::min(chunk, count - c * chunk);
+      if (c >= 2) BF_CUDA(cudaStreamWaitEvent(st.stream, st.stage_copied[k], 0));
+      launch_deinterleave(st, stage_re(st, k), stage_im(st, k), offset + c * chunk, cnt);
+      BF_CUDA(cudaEventRecord(st.stage_done[k], st.stream));
+      BF_CUDA(cudaStreamWaitEvent(st.copy_stream, st.stage_done[k], 0));
+      BF_CUDA(cudaMemcpyAsync(hstage_re(st, k), stage_re(st, k), cnt * sizeof(double), cudaMemcpyDeviceToHost,
+                              st.copy_stream));
+      BF_CUDA(cudaMemcpyAsync(hstage_im(st, k), stage_im(st, k), cnt * sizeof(double), cudaMemcpyDeviceToHost,
+                              st.copy_stream));
+      BF_CUDA(cudaEventRecord(st.stage_copied[k], st.copy_stream));
+    };
+    convert_and_fetch(0);
+    for (uint64_t c = 0; c < nchunks; ++c) {
+      // pinned buffer (c+1) & 1 was emptied by the host copy of chunk c-1
+      if (c + 1 < nchunks) convert_and_fetch(c + 1);
+      const int k = (int)(c & 1);
+      const uint64_t cnt = std::min(chunk, count - c * chunk);
+      BF_CUDA(cudaEventSynchronize(st.stage_copied[k]));
+      pool.copy(re + c * chunk, hstage_re(st, k), cnt * sizeof(double));
+      pool.copy(im + c * chunk, hstage_im(st, k), cnt * sizeof(double));
+    }
+    sync_state(st);
+    return;
+  }
   auto convert = [&](uint64_t c) {
     const int k = (int)(c & 1);
     if (c >= 2) BF_CUDA(cudaStreamWaitEvent(st.stream, st.stage_copied[k], 0));

@@ -255,6 +255,11 @@ struct State {
   cudaEvent_t stage_copied[2] = {nullptr, nullptr};  // copy into / out of buffer k done
   cudaEvent_t stage_done[2] = {nullptr, nullptr};    // conversion kernel on buffer k done
   cudaEvent_t stage_start = nullptr;                 // the state's earlier work
+  // pinned host staging for large transfers from or to pageable host arrays
+  // (two chunk buffers, re and im each): host threads copy between the
+  // caller's arrays and these while the DMA engine moves the other buffer
+  void* h_stage = nullptr;
+  size_t h_stage_bytes = 0;
   // dense unitary matrix (device copy of the current op's matrix)
   double* d_umat = nullptr;
   // norms before / after a complex64 circuit and the rescale factor
