@@ -355,10 +355,11 @@ static double cuda_core_units(const TilePass& tp) {
 
 // complex128 digit blocks against the double-float tile kernel: one block
 // costs about this many double-float dense gates (on the 30-qubit layered
-// circuit a digit pass costs about 9 ms plus 8.3 ms per block, a dense gate
-// in a double-float tile pass about 2.4 ms; the charge leaves room for the
-// pass's fixed cost)
-constexpr double kDigitBlockUnits = 5.0;
+// circuit a digit pass costs about 8 ms plus 5.8 ms per block, a dense gate
+// in a double-float tile pass about 2.4 ms).  Measured against 5.0: the
+// 30-qubit circuit 1144 against 1152 ms, value encoding at 22, 24 and 25
+// (fused pairs) qubits 1.95 / 5.25 / 10.8 against 2.47 / 7.00 / 13.6 ms.
+constexpr double kDigitBlockUnits = 2.5;
 
 // A block pass costs about this many blocks besides its blocks (loading,
 // converting and storing the tile).
