@@ -115,7 +115,7 @@ def roofline_of(times: dict, plan: dict, n: int, S: float, digit_tiles: tuple[in
                 "peak_source": f"{src} (bf16 tensor; digit products are bf16 x bf16 -> fp32)",
                 "hbm": {"achieved": hbm, "peak": hbm_peak, "unit": "GB/s", "frac": hbm / hbm_peak,
                         "bytes_per_launch": 2 * S, "peak_source": f"{hbm_src} hbm_gbs"}}
-    kernel = {"tile": "bf::k_tile<bf::PolDF>", "gate": "bf::k_gate<bf::PolDF>",
+    kernel = {"tile": "bf::k_tile<bf::PolDF, false>", "gate": "bf::k_gate<bf::PolDF>",
               "block_tf32": "bf::k_tblock"}.get(cls, cls)
     traffic = TILE_TRAFFIC_BYTES_PER_AMP * (1 << n) if cls == "tile" else None
     return {"bound": "hbm", "achieved": hbm, "peak": hbm_peak, "unit": "GB/s", "frac": hbm / hbm_peak,

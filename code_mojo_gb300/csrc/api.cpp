@@ -202,6 +202,7 @@ struct Step {
   int nblk = 0;
   uint64_t base = 0, modulus = 0;  // modexp: a (or a^-1 mod N) and N; a = n_exp
   bool digits = false;             // tensor-core pass in the complex128 digit form
+  bool unitaries = false;          // tile pass: holds dense unitaries (GK_UNITARY ops)
 };
 
 // a^-1 mod N for gcd(a, N) = 1 (extended Euclid, as modinv in algos/shor.mojo:46-53)
@@ -444,6 +445,7 @@ static void build_steps(int n, const bf_op* ops, int64_t nops, const bf_exec_opt
         s.tile = ps.tile;
         s.prog_off = prog.size();
         s.nprog = (int)ps.tile.ops.size();
+        for (const TileOp& t : ps.tile.ops) s.unitaries |= t.kind == GK_UNITARY;
         prog.insert(prog.end(), ps.tile.ops.begin(), ps.tile.ops.end());
         s.tile.ops.clear();
       } else if (ps.gate.kind == GK_UNITARY) {
@@ -717,7 +719,7 @@ static void run_steps(State& st, const std::vector<Step>& steps, const Program& 
       case Step::GATE: launch_gate(st, s.gate); break;
       case Step::TILE:
         launch_tile_pass(st, st.d_prog + s.prog_off, s.nprog, s.tile,
-                         pg.umats.empty() ? nullptr : reinterpret_cast<const double*>(st.d_aux + pg.umats_offset()));
+                         s.unitaries ? reinterpret_cast<const double*>(st.d_aux + pg.umats_offset()) : nullptr);
         break;
       case Step::TBLOCK:
         if (s.digits) {

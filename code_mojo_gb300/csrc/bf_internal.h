@@ -99,8 +99,9 @@ enum GKind : int32_t {
 };
 
 // Dense unitaries of up to this many qubits join fused runs (tile passes
-// and tensor-core blocks); wider ones run as their own pass.
-constexpr int kTileUnitaryMax = 3;
+// and tensor-core blocks, whose 5 qubits bound it); wider ones run as their
+// own pass.
+constexpr int kTileUnitaryMax = 5;
 
 struct GateInstr {
   int32_t kind;     // GKind

@@ -21,12 +21,14 @@
 
 namespace bf {
 
-template <class P>
+// kUnitaries: the pass holds dense unitaries (a separate form, so that
+// passes without them keep the gate loop's small register count)
+template <class P, bool kUnitaries>
 __global__ void __launch_bounds__(kTileThreads) k_tile(typename P::Glob* __restrict__ s,
                                                        const TileOp* __restrict__ ops, int nops,
                                                        const TileGeom geo, const double* __restrict__ umats) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  run_tile<P>(s, ops, nops, geo, blockIdx.x, smem_raw, umats);
+  run_tile<P, false, kUnitaries>(s, ops, nops, geo, blockIdx.x, smem_raw, umats);
 }
 
 
@@ -39,16 +41,20 @@ static void launch_tile_p(State& st, const TileOp* d_ops, int nops, const TilePa
   for (int j = 0; j < p.K; ++j) geo.q[j] = p.q[j];
   for (int j = 0; j < geo.L; ++j)
     if (geo.q[j] != j) fail(BF_EINVAL, "internal: tile qubits must start with 0..%d", geo.L - 1);
-  size_t smem = tile_smem_bytes<P>(p.K, geo.L, d_umats != nullptr);
+  const bool uni = d_umats != nullptr;
+  size_t smem = tile_smem_bytes<P>(p.K, geo.L, uni);
   static PerDeviceOnce configured;  // one per instantiation of P
   configured.run(st.device, [] {
-    BF_CUDA(cudaFuncSetAttribute(k_tile<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    BF_CUDA(cudaFuncSetAttribute(k_tile<P, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)tile_smem_bytes<P>(kMaxTileQubits, 0)));
+    BF_CUDA(cudaFuncSetAttribute(k_tile<P, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)tile_smem_bytes<P>(kMaxTileQubits, 0, true)));
   });
   uint64_t blocks = st.N >> p.K;
   if (blocks > 0x7fffffffull) fail(BF_EUNSUPPORTED, "tile grid too large");
-  k_tile<P><<<(unsigned)blocks, kTileThreads, smem, st.stream>>>(static_cast<typename P::Glob*>(st.amp), d_ops,
-                                                                 nops, geo, d_umats);
+  auto* amp = static_cast<typename P::Glob*>(st.amp);
+  if (uni) k_tile<P, true><<<(unsigned)blocks, kTileThreads, smem, st.stream>>>(amp, d_ops, nops, geo, d_umats);
+  else k_tile<P, false><<<(unsigned)blocks, kTileThreads, smem, st.stream>>>(amp, d_ops, nops, geo, nullptr);
   BF_CUDA(cudaGetLastError());
   st.launches++;
 }

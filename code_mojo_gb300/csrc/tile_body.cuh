@@ -86,6 +86,45 @@ __device__ __forceinline__ void tile_unitary(typename P::Smem* amp, int TS, int 
   }
 }
 
+// A wider in-tile unitary (UM = 4 or 5 qubits): a thread's outputs (rows of
+// groups) are formed from the group's inputs in shared memory into
+// registers, 2 per thread at a time over whole groups, then written after
+// a barrier (the groups of one round are disjoint from the next round's).
+// The staged matrix is transposed (`umt[c * D + r]`), so that the lanes of a
+// warp, which take consecutive rows of a group, read consecutive entries.
+// Every thread runs the same number of rounds (the barriers are uniform).
+template <class P, int UM, bool kCtl>
+__device__ __forceinline__ void tile_unitary_wide(typename P::Smem* amp, int TS, int tloc, uint32_t cml,
+                                                  const typename P::Smem* umt) {
+  using R = typename P::R;
+  constexpr int D = 1 << UM;
+  constexpr int kPer = 2;  // outputs per thread per round (more cost registers of every unitary pass)
+  const uint32_t low = (1u << tloc) - 1u;
+  for (int round = 0; round < TS; round += kPer * kTileThreads) {
+    R out[kPer];
+    uint32_t where[kPer];
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+      const int o = round + j * kTileThreads + (int)threadIdx.x;
+      where[j] = 0xffffffffu;
+      if (o >= TS) continue;
+      const uint32_t g = (uint32_t)o >> UM, r = (uint32_t)o & (D - 1);
+      const uint32_t base = ((g & ~low) << UM) | (g & low);
+      if (kCtl && (base & cml) != cml) continue;
+      R acc = P::zero();
+#pragma unroll 1
+      for (int c = 0; c < D; ++c)
+        acc = P::fma(P::from_smem(umt[c * D + r]), P::from_smem(amp[base | ((uint32_t)c << tloc)]), acc);
+      out[j] = acc;
+      where[j] = base | (r << tloc);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kPer; ++j)
+      if (where[j] != 0xffffffffu) amp[where[j]] = P::to_smem(out[j]);
+  }
+}
+
 // bytes of shared memory before the staged unitary matrix (16-byte aligned)
 template <class P>
 __host__ __device__ inline size_t tile_umat_offset(int K, int L) {
@@ -100,10 +139,11 @@ __host__ __device__ inline size_t tile_umat_offset(int K, int L) {
 // kL2Loads: read the state with L2-only loads (__ldcg).  Needed when other
 // CTAs of the same launch wrote these amplitudes earlier (L1 is not coherent
 // across SMs); a separate launch per pass does not need it.
-// umats: the unitary pool of GK_UNITARY ops (row-major interleaved FP64);
-// with one, `smem_raw` also holds the staged matrix
-// (tile_smem_bytes(K, L, true)).
-template <class P, bool kL2Loads = false>
+// kUnitaries: the ops may include GK_UNITARY (their register-heavy loop is
+// compiled only into this form; passes without them keep the lean one);
+// umats is then the unitary pool (row-major interleaved FP64), and
+// `smem_raw` also holds the staged matrix (tile_smem_bytes(K, L, true)).
+template <class P, bool kL2Loads = false, bool kUnitaries = false>
 __device__ __forceinline__ void run_tile(typename P::Glob* __restrict__ s, const TileOp* __restrict__ ops, int nops,
                                          const TileGeom& geo, uint64_t tile, unsigned char* smem_raw,
                                          const double* __restrict__ umats = nullptr) {
@@ -143,24 +183,38 @@ __device__ __forceinline__ void run_tile(typename P::Glob* __restrict__ s, const
     const int kind = __ldg(&op->kind);
     const int tloc = __ldg(&op->tloc);
     const uint32_t cml = __ldg(&op->cmask_loc);
-    if (kind == GK_UNITARY) {
+    if (kUnitaries && kind == GK_UNITARY) {
       // stage the matrix, then every group of the tile
       const int um = __ldg(&op->um);
       const double* u = umats + __ldg(&op->uoff);
       S* mat = reinterpret_cast<S*>(smem_raw + tile_umat_offset<P>(K, L));
-      for (int e = tid; e < (1 << (2 * um)); e += kTileThreads) {
+      const int dim = 1 << um;
+      for (int e = tid; e < dim * dim; e += kTileThreads) {
         typename P::Glob gv;
         if constexpr (sizeof(typename P::Glob) == 16) gv = make_double2(__ldg(u + 2 * e), __ldg(u + 2 * e + 1));
         else gv = make_float2((float)__ldg(u + 2 * e), (float)__ldg(u + 2 * e + 1));
-        mat[e] = P::to_smem(P::from_glob(gv));
+        // row-major for the narrow forms, transposed for the wide ones
+        const int at = um <= 3 ? e : (e % dim) * dim + e / dim;
+        mat[at] = P::to_smem(P::from_glob(gv));
       }
       __syncthreads();
-      if (um == 2) {
-        if (cml) tile_unitary<P, 2, true>(amp, TS, tloc, cml, mat);
-        else tile_unitary<P, 2, false>(amp, TS, tloc, 0u, mat);
-      } else {
-        if (cml) tile_unitary<P, 3, true>(amp, TS, tloc, cml, mat);
-        else tile_unitary<P, 3, false>(amp, TS, tloc, 0u, mat);
+      switch (um) {
+        case 2:
+          if (cml) tile_unitary<P, 2, true>(amp, TS, tloc, cml, mat);
+          else tile_unitary<P, 2, false>(amp, TS, tloc, 0u, mat);
+          break;
+        case 3:
+          if (cml) tile_unitary<P, 3, true>(amp, TS, tloc, cml, mat);
+          else tile_unitary<P, 3, false>(amp, TS, tloc, 0u, mat);
+          break;
+        case 4:
+          if (cml) tile_unitary_wide<P, 4, true>(amp, TS, tloc, cml, mat);
+          else tile_unitary_wide<P, 4, false>(amp, TS, tloc, 0u, mat);
+          break;
+        default:
+          if (cml) tile_unitary_wide<P, 5, true>(amp, TS, tloc, cml, mat);
+          else tile_unitary_wide<P, 5, false>(amp, TS, tloc, 0u, mat);
+          break;
       }
       __syncthreads();
       continue;

@@ -35,7 +35,7 @@ def test_tile_roofline_without_tensor_blocks(bench):
     n, S = 30, 16.0 * 2 ** 30
     times = {"tile": (74, 4200.0), "gate": (1, 2.0)}
     r = bench.roofline_of(times, {"tile_passes": 74, "block_passes": 0, "blocks": 0}, n, S)
-    assert r["kernel"] == "bf::k_tile<bf::PolDF>" and r["bound"] == "hbm" and r["unit"] == "GB/s"
+    assert r["kernel"] == "bf::k_tile<bf::PolDF, false>" and r["bound"] == "hbm" and r["unit"] == "GB/s"
     assert r["achieved"] == pytest.approx(2 * S / (4200.0 / 74 * 1e-3) / 1e9)
     assert r["traffic"] == pytest.approx(bench.TILE_TRAFFIC_BYTES_PER_AMP * 2 ** n)
 

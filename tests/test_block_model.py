@@ -199,13 +199,13 @@ def random_unitary(dim, rng):
 
 
 def unitary_circuit(n, count, seed):
-    """Gates mixed with dense 2- and 3-qubit unitaries, some controlled."""
+    """Gates mixed with dense 2- to 5-qubit unitaries, some controlled."""
     rng = np.random.Generator(np.random.PCG64(seed))
     qc = bfy.QuantumCircuit(n)
     for _ in range(count):
-        kind = int(rng.integers(0, 4))
-        if kind <= 1:
-            m = 2 + kind
+        kind = int(rng.integers(0, 6))
+        if kind <= 1 or kind >= 4:
+            m = 2 + kind if kind <= 1 else kind  # 2, 3, 4 or 5 qubits
             t = int(rng.integers(0, n - m + 1))
             qc.unitary(random_unitary(1 << m, rng), t, m)
         elif kind == 2:
@@ -230,7 +230,7 @@ UNITARY_CIRCUITS = {
 @pytest.mark.parametrize("fmt", ["digits", "tf32", "digits-exact"])
 @pytest.mark.parametrize("name", list(UNITARY_CIRCUITS))
 def test_dense_unitaries_in_block_passes(model, fmt, name, tmp_path):
-    """Dense 2- and 3-qubit unitaries (from the fusion rewrites, or written
+    """Dense 2- to 5-qubit unitaries (from the fusion rewrites, or written
     directly, some controlled) are multiplied into the tensor-core blocks of
     the fused run around them."""
     qc = UNITARY_CIRCUITS[name]()

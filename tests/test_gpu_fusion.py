@@ -79,13 +79,13 @@ def _random_unitary(dim, rng):
 
 
 def _unitary_circuit(n, count, seed):
-    """Gates mixed with dense 2- and 3-qubit unitaries, some controlled."""
+    """Gates mixed with dense 2- to 5-qubit unitaries, some controlled."""
     rng = np.random.Generator(np.random.PCG64(seed))
     qc = bfy.QuantumCircuit(n)
     for _ in range(count):
-        kind = int(rng.integers(0, 4))
-        if kind <= 1:
-            m = 2 + kind
+        kind = int(rng.integers(0, 6))
+        if kind <= 1 or kind >= 4:
+            m = 2 + kind if kind <= 1 else kind  # 2, 3, 4 or 5 qubits
             t = int(rng.integers(0, n - m + 1))
             qc.unitary(_random_unitary(1 << m, rng), t, m)
         elif kind == 2:
@@ -103,16 +103,17 @@ def _unitary_circuit(n, count, seed):
 @pytest.mark.parametrize("tensor", [True, False])
 @pytest.mark.parametrize("dtype", ["c128", "c64"])
 def test_dense_unitaries_join_fused_runs(n, tensor, dtype):
-    """Dense 2- and 3-qubit unitaries run inside the fused run's tile passes
-    (CUDA-core tiles, or multiplied into tensor-core blocks): the plan has no
-    pass of its own for them, and the state matches the oracle."""
+    """Dense 2- to 5-qubit unitaries run inside the fused run's tile passes
+    (CUDA-core tiles, or multiplied into tensor-core blocks), and the state
+    matches the oracle.  A unitary that would be alone in its pass runs as its
+    own kernel (the same 2S of traffic), so at most one such pass remains."""
     qc = _unitary_circuit(n, 50, 20 + n)
     state = W.random_normal_state(n, 3)
     ctx = bfy.ExecContext()
     ctx.execution_strategy = bfy.ExecutionStrategy.GPU_FUSED
     ctx.gpu_tensor_blocks = tensor
     plan = bfy.plan_stats(qc, ctx, dtype)
-    assert plan["other_passes"] == 0 and plan["tile_passes"] > 0
+    assert plan["other_passes"] <= 1 and plan["tile_passes"] > 0
     if tensor and n >= 12:
         assert plan["block_passes"] > 0
     st = bfy.QuantumState.from_soa(*state, dtype)
