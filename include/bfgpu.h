@@ -196,7 +196,10 @@ int bf_state_set_basis(bf_state* st, uint64_t idx);
  * before later work on the state).  Download blocks until re and im hold
  * the amplitudes.  Both move 4 Mi-amplitude chunks through two device
  * buffers so that one chunk's host copy overlaps the next chunk's
- * conversion. */
+ * conversion.  Transfers of at least one chunk from or to pageable arrays
+ * go through the state's pinned host buffers (128 MiB, allocated on first
+ * use), filled or drained by a pool of library host threads while the DMA
+ * engine moves the other chunk. */
 int bf_state_upload_soa(bf_state* st, const double* re, const double* im);
 int bf_state_download_soa(bf_state* st, double* re, double* im);
 /* Copies amplitudes [offset, offset+count) to host SoA arrays (blocks). */
