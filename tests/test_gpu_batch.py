@@ -94,8 +94,8 @@ def test_batch_at_full_spec_matches_the_oracle_per_circuit(dtype):
 
 def test_batch_autotuning_record_and_result():
     """With tile_qubits = 0 a batch times the candidate tile widths per qubit
-    count at creation and keeps the fastest; the tuned batch still matches
-    the oracle circuit by circuit."""
+    count at creation and keeps the widest within 3% of the fastest; the
+    tuned batch still matches the oracle circuit by circuit."""
     circs = W.batch_workload(count=40, seed=9, nmin=6, nmax=13, depth=6)
     b = B.Batch(circs, dtype="c128")
     rows = b.tuning()
@@ -105,8 +105,10 @@ def test_batch_autotuning_record_and_result():
         cand = [r for r in rows if r["qubits"] == n]
         assert [r["width"] for r in cand] == list(range(8, min(n, 12) + 1))
         assert sum(r["chosen"] for r in cand) == 1 and all(r["ms"] > 0 for r in cand)
-        best = min(cand, key=lambda r: r["ms"])
-        assert best["chosen"]
+        # the widest width within 3% of the fastest run is kept
+        fastest = min(r["ms"] for r in cand)
+        keep = max(r["width"] for r in cand if r["ms"] <= 1.03 * fastest)
+        assert [r["width"] for r in cand if r["chosen"]] == [keep]
     b.run()
     for c, qc in enumerate(circs):
         assert np.max(np.abs(b.download(c) - expected(qc))) <= 1e-12
