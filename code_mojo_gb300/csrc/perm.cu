@@ -175,10 +175,83 @@ __global__ void __launch_bounds__(256) k_modexp(const T* __restrict__ in, T* __r
   }
 }
 
+// The same map as a gather over slabs, for a value register of at most
+// 10 qubits and an invertible base: a CTA takes XW consecutive exponents x
+// (XW amplitudes = 128 bytes of each row y) and every row, reads the slab
+// into shared memory with 128-byte row reads, and writes each output row
+// (x, y_out) from (x, y_out * base^-x mod N) with 128-byte row writes.  The
+// scatter form above writes single amplitudes to scattered rows (partial
+// DRAM sectors: 5 S of traffic for 2 S of algorithmic bytes at 26 qubits).
+template <class T, int XW>
+__global__ void __launch_bounds__(256) k_modexp_slab(const T* __restrict__ in, T* __restrict__ out, int n_exp,
+                                                     uint32_t Y, uint32_t m, const uint64_t* __restrict__ inv_table) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* slab = reinterpret_cast<T*>(smem_raw);  // Y rows of XW amplitudes
+  const uint64_t x0 = (uint64_t)blockIdx.x * XW;
+  const uint32_t total = Y * XW;
+  for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) {
+    const uint32_t y = t / XW, xi = t % XW;
+    slab[t] = in[(x0 + xi) | ((uint64_t)y << n_exp)];
+  }
+  __syncthreads();
+  for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) {
+    const uint32_t y_out = t / XW, xi = t % XW;
+    uint32_t y_in = y_out;
+    if (y_out < m) y_in = (uint32_t)(((uint64_t)y_out * __ldg(inv_table + x0 + xi)) % m);
+    out[(x0 + xi) | ((uint64_t)y_out << n_exp)] = slab[y_in * XW + xi];
+  }
+}
+
+// a^-1 mod m (extended Euclid), or 0 when gcd(a, m) != 1
+static uint64_t inverse_mod(uint64_t a, uint64_t m) {
+  int64_t r0 = (int64_t)m, r1 = (int64_t)(a % m), t0 = 0, t1 = 1;
+  while (r1 != 0) {
+    const int64_t q = r0 / r1, r = r0 - q * r1, t = t0 - q * t1;
+    r0 = r1;
+    r1 = r;
+    t0 = t1;
+    t1 = t;
+  }
+  if (r0 != 1) return 0;
+  return (uint64_t)((t0 % (int64_t)m + (int64_t)m) % (int64_t)m);
+}
+
+template <class T>
+static bool launch_modexp_slab(State& st, int n_exp, uint64_t base, uint64_t modulus) {
+  constexpr int XW = 128 / (int)sizeof(T);
+  const int ny = st.n - n_exp;
+  if (ny > 10 || n_exp < 7 || n_exp > 22 || modulus > (1ull << ny)) return false;
+  const uint64_t inv = inverse_mod(base, modulus);
+  if (inv == 0) return false;  // not a permutation: the scatter form keeps the reference's behaviour
+  const uint64_t xcount = 1ull << n_exp;
+  uint64_t* table = static_cast<uint64_t*>(dev_alloc(st, xcount * sizeof(uint64_t)));
+  const unsigned tb = (unsigned)std::min<uint64_t>((xcount + 255) / 256, (uint64_t)st.num_sms * 16);
+  k_powtable<<<tb, 256, 0, st.stream>>>(table, xcount, inv, modulus);
+  BF_CUDA(cudaGetLastError());
+  st.launches++;
+  const uint32_t Y = 1u << ny;
+  const size_t smem = (size_t)Y * XW * sizeof(T);
+  static PerDeviceOnce configured;  // one per instantiation of T
+  configured.run(st.device, [] {
+    BF_CUDA(cudaFuncSetAttribute(k_modexp_slab<T, 128 / (int)sizeof(T)>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(1024 * 128)));
+  });
+  k_modexp_slab<T, XW><<<(unsigned)(xcount / XW), 256, smem, st.stream>>>(
+      static_cast<const T*>(st.amp), static_cast<T*>(st.scratch), n_exp, Y, (uint32_t)modulus, table);
+  BF_CUDA(cudaGetLastError());
+  st.launches++;
+  dev_free(st, table);  // stream-ordered: after the gather
+  std::swap(st.amp, st.scratch);
+  return true;
+}
+
 void launch_modexp(State& st, int n_exp, uint64_t base, uint64_t modulus) {
   if (n_exp <= 0 || n_exp >= st.n) fail(BF_EINVAL, "internal: modexp register of %d qubits", n_exp);
   if (modulus < 2) fail(BF_EINVAL, "internal: modexp modulus %llu", (unsigned long long)modulus);
   ensure_scratch(st);
+  if (st.dtype == BF_C128 ? launch_modexp_slab<double2>(st, n_exp, base, modulus)
+                          : launch_modexp_slab<float2>(st, n_exp, base, modulus))
+    return;
   uint64_t* table = nullptr;
   const uint64_t xcount = 1ull << n_exp;
   if (n_exp <= 22) {

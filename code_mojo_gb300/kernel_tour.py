@@ -65,7 +65,7 @@ def tour(n: int, dtype: str, reps: int) -> list[dict]:
          circ(lambda q: q.unitary(np.eye(8, dtype=complex) * np.exp(0.3j), hi - 2, 3)), per_gate),
         ("Grover diffuser (classical, all qubits)", "k_diff_sum/k_diff_mean/k_diff_update", 3.0,
          circ(lambda q: bfy.grover_diffuser(q)), per_gate),
-        ("modular exponentiation", "k_modexp", 2.0,
+        ("modular exponentiation", "k_modexp_slab", 2.0,
          circ(lambda q: q.transformations.append(
              bfy.ClassicalTransformation("MOD_EXP", [n - 8, 8, 7, 255]))), per_gate),
         ("fused layered circuit, 2 layers", "k_tblock_dg / k_tblock / k_tile", None,

@@ -105,7 +105,10 @@ def test_order_finding_on_the_oracle_finds_the_order_of_7_mod_15():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("case", CASES + [(10, 11, 1234, 2047), (12, 12, 65, 4091)])
+# (the last four take the slab-gather form: a value register of at most
+# 10 qubits and an exponent register of at least 7)
+@pytest.mark.parametrize("case", CASES + [(10, 11, 1234, 2047), (12, 12, 65, 4091), (8, 8, 7, 255),
+                                          (9, 7, 5, 127), (12, 10, 77, 1000), (16, 8, 7, 255)])
 @pytest.mark.parametrize("dtype", ["c128", "c64"])
 @pytest.mark.parametrize("inverse", [False, True])
 def test_gpu_modexp_is_bit_exact(case, dtype, inverse):
