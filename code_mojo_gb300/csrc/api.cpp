@@ -12,6 +12,8 @@
 #include <thread>
 #include <vector>
 
+#include <unistd.h>
+
 #include "bf_internal.h"
 
 namespace bf {
@@ -927,12 +929,23 @@ static double* stage_im(State& st, int k) { return stage_re(st, k) + std::min<ui
 // moves the previous chunk.
 class CopyPool {
  public:
+  // created on first use and never destroyed: its idle workers end with the
+  // process (a destructor would join them, and in a forked child, whose
+  // workers do not exist, the join would fail)
   static CopyPool& get() {
-    static CopyPool pool;
-    return pool;
+    static CopyPool* pool = new CopyPool();
+    return *pool;
   }
-  // dst[0, bytes) = src[0, bytes), split over the workers and the caller
+  // dst[0, bytes) = src[0, bytes), split over the workers and the caller.
+  // One job at a time (callers on other threads wait their turn); in a
+  // process forked after the pool started, whose workers do not exist, the
+  // caller copies alone.
   void copy(void* dst, const void* src, size_t bytes) {
+    if (getpid() != pid_) {
+      std::memcpy(dst, src, bytes);
+      return;
+    }
+    std::lock_guard<std::mutex> one_job(job_m_);
     const size_t parts = workers_.size() + 1;
     const size_t part = ((bytes / parts) + 255) & ~(size_t)255;
     {
@@ -949,21 +962,14 @@ class CopyPool {
     std::unique_lock<std::mutex> lk(m_);
     done_.wait(lk, [&] { return pending_ == 0; });
   }
-  ~CopyPool() {
-    {
-      std::lock_guard<std::mutex> lk(m_);
-      stop_ = true;
-      ++gen_;
-    }
-    cv_.notify_all();
-    for (auto& t : workers_) t.join();
-  }
-
  private:
-  CopyPool() {
+  CopyPool() : pid_(getpid()) {
     const unsigned hw = std::thread::hardware_concurrency();
     const unsigned n = std::max(1u, std::min(16u, hw ? hw : 4u)) - 1;
-    for (unsigned i = 0; i < n; ++i) workers_.emplace_back([this, i] { loop(i); });
+    for (unsigned i = 0; i < n; ++i) {
+      workers_.emplace_back([this, i] { loop(i); });
+      workers_.back().detach();
+    }
   }
   void run_part(size_t i) {
     const size_t lo = std::min(bytes_, i * part_), hi = std::min(bytes_, lo + part_);
@@ -980,18 +986,18 @@ class CopyPool {
         std::unique_lock<std::mutex> lk(m_);
         cv_.wait(lk, [&] { return gen_ != seen; });
         seen = gen_;
-        if (stop_) return;
       }
       run_part(i);
       std::lock_guard<std::mutex> lk(m_);
       if (--pending_ == 0) done_.notify_one();
     }
   }
+  const pid_t pid_;
   std::vector<std::thread> workers_;
+  std::mutex job_m_;  // held by the caller for a whole job
   std::mutex m_;
   std::condition_variable cv_, done_;
   uint64_t gen_ = 0;
-  bool stop_ = false;
   int pending_ = 0;
   char* dst_ = nullptr;
   const char* src_ = nullptr;

@@ -60,7 +60,7 @@ def tour(n: int, dtype: str, reps: int) -> list[dict]:
         ("qubit swap (classical)", "k_swap_bits", 1.0,
          circ(lambda q: q.transformations.append(bfy.ClassicalTransformation("SWAP", [1, hi]))), per_gate),
         ("full bit reversal", "k_bitrev_tiles", 2.0, circ(lambda q: bfy.bit_reverse(q)), per_gate),
-        ("qubit permutation", "k_permute", 2.0, circ(lambda q: bfy.permute_qubits(q, perm)), per_gate),
+        ("qubit permutation", "k_permute_tiles", 2.0, circ(lambda q: bfy.permute_qubits(q, perm)), per_gate),
         ("dense 3-qubit unitary", "k_unitary_reg", 2.0,
          circ(lambda q: q.unitary(np.eye(8, dtype=complex) * np.exp(0.3j), hi - 2, 3)), per_gate),
         ("Grover diffuser (classical, all qubits)", "k_diff_sum/k_diff_mean/k_diff_update", 3.0,

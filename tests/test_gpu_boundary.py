@@ -63,3 +63,26 @@ def test_page_locked_and_pageable_arrays_agree():
                 cudart.cudaHostUnregister(a.ctypes.data)
     assert np.array_equal(locked_r, re) and np.array_equal(locked_i, im)
     assert np.array_equal(plain_r, re) and np.array_equal(plain_i, im)
+
+
+def test_concurrent_transfers_from_two_threads():
+    """Two host threads move two states at once: the library's copy threads
+    take one transfer's chunk at a time, and both arrive exactly."""
+    import threading
+    n = 23
+    states = [soa(n, 21), soa(n, 22)]
+    out = [None, None]
+
+    def work(k):
+        re, im = states[k]
+        st = bfy.QuantumState.from_soa(re, im, "c128")
+        out[k] = st.download()
+        st.close()
+
+    th = [threading.Thread(target=work, args=(k,)) for k in range(2)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    for k in range(2):
+        assert np.array_equal(out[k][0], states[k][0]) and np.array_equal(out[k][1], states[k][1])
