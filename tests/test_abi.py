@@ -215,3 +215,16 @@ def test_random_op_records_are_validated_without_crashing():
         statuses.add(F.lib().bf_plan_stats(n, arr, nops, C.byref(ctx), C.byref(t), C.byref(g), C.byref(x),
                                            C.byref(b), C.byref(bp), C.byref(nb)))
     assert F.BF_EINVAL in statuses
+
+
+@pytest.mark.parametrize("dtype", ["c128", "c64"])
+def test_fuse_circuit_layered_30q_plans_unitaries_into_block_passes(dtype):
+    """The reference's fuse_circuit turns the benchmark circuit's neighbour
+    pairs into 4x4 unitaries; they stay inside the fused run (no pass of their
+    own) and nearly every pass runs as tensor-core blocks."""
+    from code_mojo_gb300 import fusion as FU
+    ctx = bfy.ExecContext()
+    ctx.execution_strategy = bfy.ExecutionStrategy.GPU_FUSED
+    s = bfy.plan_stats(FU.fuse_circuit(W.random_layered_circuit(30, 40, 0)), ctx, dtype)
+    assert s["other_passes"] == 0 and s["gate_kernels"] == 0
+    assert s["block_passes"] >= s["tile_passes"] - 2 and s["tile_passes"] <= 110
