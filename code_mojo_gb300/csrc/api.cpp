@@ -418,7 +418,8 @@ static void build_steps(int n, const bf_op* ops, int64_t nops, const bf_exec_opt
   std::vector<GateInstr> run;
   auto flush = [&]() {
     if (run.empty()) return;
-    for (auto& ps : plan_gates(n, run, K, true, tensor ? block_units : 0.0, pass_cost)) {
+    for (auto& ps : plan_gates(n, run, K, true, tensor ? block_units : 0.0, pass_cost,
+                               tensor && format == BLOCK_DIGITS)) {
       Step s;
       if (ps.is_tile && tensor && ps.tile.K == kBlockTileQubits && ps.tile.L == kTileLowQubits) {
         size_t b0 = pg.blocks.size(), i0 = pg.images.size(), o0 = pg.offsets.size();

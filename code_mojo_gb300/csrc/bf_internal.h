@@ -386,9 +386,11 @@ struct PlanStep {
 // costing that many dense gates of the CUDA-core tile kernel; a pass whose
 // blocks would be cheaper gets its tile chosen for work per unit of
 // block-pass time rather than work per pass, a pass costing pass_cost
-// blocks besides its blocks
+// blocks besides its blocks.  keep_wide_unitaries: a pass that would hold
+// only a dense unitary of 4 or 5 qubits stays a pass (the complex128 digit
+// blocks run it faster than the double-float unitary kernel)
 std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int K, bool allow_single = true,
-                                 double block_units = 0, double pass_cost = 2.5);
+                                 double block_units = 0, double pass_cost = 2.5, bool keep_wide_unitaries = false);
 
 // bf_execute's body on a prepared state; stream, event and SM count of a
 // state; releasing every buffer a state owns (api.cpp).

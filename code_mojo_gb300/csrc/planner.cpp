@@ -322,7 +322,7 @@ static double pass_core_units(const std::vector<const GateInstr*>& remaining, ui
 }
 
 std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int K, bool allow_single,
-                                 double block_units, double pass_cost) {
+                                 double block_units, double pass_cost, bool keep_wide_unitaries) {
   std::vector<PlanStep> steps;
   if (gates.empty()) return steps;
   K = std::max(1, std::min(K, std::min(n, kMaxTileQubits)));
@@ -438,9 +438,18 @@ std::vector<PlanStep> plan_gates(int n, const std::vector<GateInstr>& gates, int
     }
     if (taken.empty()) fail(BF_EINVAL, "internal: tile planner made no progress (K=%d, n=%d)", K, n);
     double single_bytes = 0;
-    for (const GateInstr* g : taken) single_bytes += gate_bytes_fraction(*g);
-    if (allow_single && single_bytes <= 2.0) {
-      // a tile pass moves 2S; the gates on their own move no more
+    bool wide_unitary = false;
+    for (const GateInstr* g : taken) {
+      single_bytes += gate_bytes_fraction(*g);
+      wide_unitary |= g->kind == GK_UNITARY && g->um >= 4;
+    }
+    // a tile pass moves 2S; the gates on their own move no more.  With
+    // keep_wide_unitaries a unitary of 4 or 5 qubits stays a pass (one
+    // tensor-core block): on its own, a double-float kernel does 2^m complex
+    // products per amplitude (at 26 qubits a lone 5-qubit unitary took 8.2
+    // ms that way and 1.9 ms as a digit pass; a 3-qubit one 1.8 ms either
+    // way, so it keeps its kernel)
+    if (allow_single && single_bytes <= 2.0 && !(wide_unitary && keep_wide_unitaries)) {
       for (const GateInstr* g : taken) {
         PlanStep st;
         st.is_tile = false;
