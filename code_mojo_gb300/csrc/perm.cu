@@ -8,12 +8,13 @@
 //    pair (m, rev m); every global access is a 512 B run (complex128).
 //  * Any other permutation of qubit positions (partial reversal,
 //    permute_qubits, qubit reversal of a subset) out of place into the
-//    scratch buffer, the two buffers then swapped: from 10 qubits up as
-//    shared-memory tiles whose reads and writes both run over the low 5
-//    qubits (k_permute_tiles: 2S of DRAM traffic, 0.43 ms at 26 qubits),
-//    below that as a gather dst[j] = src[map(j)] with map(j) assembled from
-//    a per-CTA table of 8-bit chunks (k_permute, whose scattered 16-byte
-//    reads moved 3.9S and took 0.64 ms at 26 qubits).
+//    scratch buffer, the two buffers then swapped: complex128 states from
+//    10 qubits up as shared-memory tiles whose reads and writes both run
+//    over the low 5 qubits (k_permute_tiles: 2S of DRAM traffic, 0.43 ms at
+//    26 qubits), otherwise as a gather dst[j] = src[map(j)] with map(j)
+//    assembled from a per-CTA table of 8-bit chunks (k_permute, whose
+//    scattered 16-byte reads moved 3.9S and took 0.64 ms at 26 qubits,
+//    complex128).
 #include <algorithm>
 #include <cstring>
 #include <utility>
@@ -186,8 +187,11 @@ void launch_permute(State& st, const int32_t* src_of) {
   PermArgs a;
   a.n = st.n;
   for (int p = 0; p < 64; ++p) a.src_of[p] = p < st.n ? src_of[p] : 0;
-  if (st.n >= 10) {
-    // the tiled form (global accesses in 32-amplitude runs)
+  if (st.n >= 10 && st.dtype == BF_C128) {
+    // the tiled form (global accesses in 32-amplitude runs); at complex64
+    // the gather below measured faster (0.26 against 0.36 ms at 26 qubits:
+    // its 8-byte reads waste less of a sector, the tiles' runs are half as
+    // long)
     PermTiles t;
     std::memset(&t, 0, sizeof t);
     bool inP[64] = {false}, fromP[64] = {false};
