@@ -242,3 +242,15 @@ def test_dense_unitaries_in_block_passes(model, fmt, name, tmp_path):
     tol = 1e-12 if fmt.startswith("digits") else 1e-5
     assert block_passes > 0
     assert float(np.max(np.abs(got - (r + 1j * i)))) <= tol
+
+
+@pytest.mark.parametrize("seed", [31, 32, 33, 34])
+@pytest.mark.parametrize("fmt", ["digits", "tf32"])
+def test_random_unitary_circuits_in_block_passes(model, fmt, seed, tmp_path):
+    """Seeded mixes of gates and 2- to 5-qubit unitaries (some controlled) on
+    13 qubits: every plan's grouping and matrices match the oracle."""
+    qc = unitary_circuit(13, 40, seed)
+    re, im = W.random_normal_state(13, seed)
+    got, _ = run_model(model, fmt, qc, re, im, tmp_path)
+    r, i = O.run(qc, re, im)
+    assert float(np.max(np.abs(got - (r + 1j * i)))) <= (1e-12 if fmt == "digits" else 1e-5)
